@@ -1,0 +1,366 @@
+#!/usr/bin/env python
+"""Throughput of the StrangSplitting hot path on GB300, one JSON line.
+
+Workload: the two-component exciton-polariton problem on a 512 x 512 grid (L = 256,
+2x2 matrix dispersion, G = diag(0, g|u2|^2), Gaussian photon pump with a linear
+ramp, dt = 0.05), FP64 fields.  One "step" is one full Strang step of every
+trajectory in the batch.  The batch holds independent copies of the field so that
+the working set (fields + tables) is more than twice the 129 MB L2: every pass
+streams from HBM.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference] [--dtype c128|c64]
+
+value      : grid-point-steps/s over all ranks, inputs resident in HBM, CUDA-event timed
+e2e        : the same through the C ABI with host buffers: H2D of the state from pinned
+             memory, K steps, D2H of the final state, wall-clock timed
+roofline   : dominant kernel, algorithmic bytes per launch / its mean event-timed
+             duration, against the measured HBM copy bandwidth
+cpu_baseline: the FP64 oracle (scipy FFT, all host threads) on a bounded sample
+--impl reference: the reference's algorithm on the host cores (the Julia reference
+             cannot run here; its restatement in oracle/ is the reference arm)
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import subprocess
+import sys
+import threading
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+N_GRID, L_BOX, DT = 512, 256.0, 0.05
+POL = dict(hbar=0.6582, m=1 / 6, dc=-0.5, dx=0.0, gc=0.05, gx=0.005, Om=5.07, g=0.003, A=5.0, ramp=200.0, w=50.0)
+L2_BYTES = 129 * 2 ** 20
+
+
+def measured_peaks():
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        d = json.loads(p.read_text())
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def dist_env():
+    return int(os.environ.get("RANK", 0)), int(os.environ.get("WORLD_SIZE", 1)), int(os.environ.get("LOCAL_RANK", 0))
+
+
+def polariton_closures():
+    p = POL
+
+    def disp(k, _):
+        k2 = k[0] ** 2 + k[1] ** 2
+        return [[p["hbar"] * k2 / (2 * p["m"]) - p["dc"] - 1j * p["gc"], p["Om"]], [p["Om"], -p["dx"] - 1j * p["gx"]]]
+
+    def nonl(u, _):
+        return [0 * u[0], p["g"] * np.abs(u[1]) ** 2]
+
+    def pump(r, _, t):
+        a = p["A"] * min(t / p["ramp"], 1.0)
+        return [a * np.exp(-((r[0] - L_BOX / 2) ** 2 + (r[1] - L_BOX / 2) ** 2) / p["w"] ** 2), 0]
+
+    return disp, nonl, pump
+
+
+def batch_for(dtype) -> int:
+    per = 2 * N_GRID * N_GRID * (16 if dtype == np.complex128 else 8)
+    return int(2 ** math.ceil(math.log2(2 * L2_BYTES / per)))
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled every 200 ms."""
+
+    FIELDS = "clocks.sm,clocks.max.sm,clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown," \
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap"
+
+    def __init__(self, index: int):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.FIELDS}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except OSError:
+            self.proc = None
+        time.sleep(0.3)
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], 0.0, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [x.strip() for x in ln.split(",")]
+            if len(parts) < 6:
+                continue
+            try:
+                sm.append(float(parts[0]))
+                mx = max(mx, float(parts[1]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[2:6]):
+                if v.lower().startswith("active"):
+                    reasons.add(nm)
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": mx or None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def cpu_baseline(steps_hint: int = 0):
+    """FP64 oracle on the host cores: one trajectory of the workload, scipy FFT with all
+    threads, steps chosen for ~10 s of work."""
+    from oracle import gpe_oracle as O
+    prob = oracle_problem(O)
+    cores = os.cpu_count() or 1
+    it = O.OracleIterator(prob, (0.0, 200.0), DT, 100, fft_workers=cores)
+    t = 0.0
+    it.step(t + DT, DT)  # warm-up
+    t0 = time.perf_counter()
+    n = 0
+    while True:
+        t += DT
+        it.step(t, DT)
+        n += 1
+        el = time.perf_counter() - t0
+        if (steps_hint and n >= steps_hint) or (not steps_hint and (el > 10.0 or n >= 4000)):
+            break
+    el = time.perf_counter() - t0
+    P = N_GRID * N_GRID
+    return {"value": P * n / el, "unit": "grid-point-steps/s", "cores": cores, "kind": "port",
+            "sample": f"{n} Strang steps of one 512^2 two-component trajectory, FP64 numpy/scipy.fft "
+                      f"with workers={cores}, {el:.1f} s"}
+
+
+def oracle_problem(O):
+    p = POL
+    dg, rg = O.grids((L_BOX, L_BOX), (N_GRID, N_GRID))
+    X, Y = O.mesh(dg)
+    prof = np.exp(-((X - L_BOX / 2) ** 2 + (Y - L_BOX / 2) ** 2) / p["w"] ** 2)
+
+    def disp(k, _):
+        k2 = k[0] ** 2 + k[1] ** 2
+        one = np.ones_like(k2)
+        return np.array([[p["hbar"] * k2 / (2 * p["m"]) - p["dc"] - 1j * p["gc"], p["Om"] * one],
+                         [p["Om"] * one, (-p["dx"] - 1j * p["gx"]) * one]])
+
+    z = np.zeros((N_GRID, N_GRID), np.complex128)
+    return O.OracleProblem(u0=(z, z.copy()), lengths=(L_BOX, L_BOX), dispersion=disp,
+                           nonlin_g=np.array([[0, 0], [0, p["g"]]], np.complex128),
+                           pump_profile=np.stack([prof, 0 * prof]).astype(np.complex128),
+                           pump_amp=lambda t: np.array([p["A"] * min(t / p["ramp"], 1.0), 0.0]))
+
+
+def run_reference(args, rank, world):
+    """The reference arm: the reference's algorithm (oracle restatement) on the host."""
+    if rank != 0:
+        return
+    from oracle import gpe_oracle as O
+    prob = oracle_problem(O)
+    cores = os.cpu_count() or 1
+    it = O.OracleIterator(prob, (0.0, 200.0), DT, 100, fft_workers=cores)
+    t = 0.0
+    for _ in range(args.warmup):
+        t += DT
+        it.step(t, DT)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        t += DT
+        it.step(t, DT)
+    el = time.perf_counter() - t0
+    P = N_GRID * N_GRID
+    v = P * args.steps / el
+    line = {"metric": "grid-point-steps/s", "value": v, "unit": "grid-point-steps/s", "impl": "reference",
+            "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * el / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": config_dict(np.complex128, batch_for(np.complex128), world),
+            "cpu_baseline": {"value": v, "unit": "grid-point-steps/s", "cores": cores, "kind": "port",
+                             "sample": f"each step = one Strang step of one 512^2 two-component trajectory "
+                                       f"(FP64 numpy/scipy.fft, workers={cores}); the Julia reference has no "
+                                       f"julia binary on this box, so its algorithm runs as the oracle restatement"},
+            "e2e": {"value": v, "unit": "grid-point-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def config_dict(dtype, B, world):
+    fb = 2 * N_GRID * N_GRID * B * (16 if dtype == np.complex128 else 8)
+    return {"workload": f"2-component exciton-polariton {N_GRID}x{N_GRID}, L={L_BOX:g}, 2x2 matrix dispersion, "
+                        f"pumped photon, dt={DT}; {B} independent copies per GPU",
+            "grid": [N_GRID, N_GRID], "components": 2, "batch_per_gpu": B, "global_batch": B * world,
+            "field_bytes_per_gpu": fb,
+            "l2_policy": f"inputs larger than L2: fields {fb / 2**20:.0f} MiB + tables per GPU vs 129 MB L2",
+            "parallelism": f"replicas x{world}" if world > 1 else "single GPU"}
+
+
+def algorithmic_bytes(dtype):
+    """Bytes per grid point per launch of each pass (fields read + written once, tables
+    and pump profile read once).  c = complex size, r = real size."""
+    c = 16 if dtype == np.complex128 else 8
+    r = c // 2
+    row = 2 * 2 * c + r       # 2 components in + out, photon pump profile
+    col = 2 * 2 * c + 4 * c   # 2 components in + out, 2x2 k-space table
+    return {"row": row, "col": col}
+
+
+def run_gpu(args, rank, world, local_rank):
+    import __graft_entry__ as G
+    pkg = G.load_package()
+    import ctypes
+    L = sys.modules["gpe_gb300._lib"]
+    lib = pkg.load_library()
+    dist = None
+    if world > 1:
+        import torch
+        import torch.distributed as tdist
+        torch.cuda.set_device(local_rank)
+        tdist.init_process_group("nccl")
+        dist = tdist
+    dtype = np.complex128 if args.dtype == "c128" else np.complex64
+    B = args.batch or batch_for(dtype)
+    disp, nonl, pump = polariton_closures()
+    u0 = np.zeros((N_GRID, N_GRID, B), dtype, order="F")
+    prob = pkg.GrossPitaevskiiProblem((u0, u0.copy()), (L_BOX, L_BOX), dispersion=disp, nonlinearity=nonl, pump=pump)
+    total = args.warmup + 3 * args.steps + 8
+    it = pkg.StrangSplittingIterator(prob, (0.0, 200.0), dt=DT, nsaves=100, total_steps=max(total, 4000),
+                                     device=local_rank)
+    h = it.h
+    P = N_GRID * N_GRID
+    # warm-up
+    it.step(args.warmup)
+
+    def barrier():
+        if dist:
+            dist.barrier()
+
+    # ---- device-resident throughput (value), per-kernel events on
+    L.check(lib, h, lib.gpe_set_timing(h, 1))
+    barrier()
+    with ClockSampler(local_rank) as clk:
+        L.check(lib, h, lib.gpe_run(h, args.steps, 0, None, None))
+    barrier()
+    ms = lib.gpe_last_run_ms(h)
+    launches = lib.gpe_last_run_launches(h)
+    kms = np.zeros(3)
+    kn = np.zeros(3, np.int64)
+    L.check(lib, h, lib.gpe_kernel_times(h, L.ptr(kms), L.ptr(kn)))
+    L.check(lib, h, lib.gpe_set_timing(h, 0))
+    # the event-bracketed run above has per-launch events; time a clean run for value
+    L.check(lib, h, lib.gpe_run(h, args.steps, 0, None, None))
+    ms_clean = lib.gpe_last_run_ms(h)
+    if dist:
+        import torch
+        t = torch.tensor([ms_clean], device=f"cuda:{local_rank}")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms_clean = float(t.item())
+    value = P * B * args.steps * world / (ms_clean * 1e-3)
+
+    # ---- end to end through the C ABI with host buffers
+    try:
+        import torch
+        pinned = [torch.zeros(B * P * 2, dtype=torch.float64 if dtype == np.complex128 else torch.float32).pin_memory()
+                  for _ in range(2)]
+        hbufs = [pb.numpy().view(dtype) for pb in pinned]
+    except Exception:
+        hbufs = [np.zeros(B * P, dtype) for _ in range(2)]
+    for m in range(2):
+        hbufs[m][:] = 0
+    out = np.empty((2, 1, B * P), dtype)
+    barrier()
+    t0 = time.perf_counter()
+    for m in range(2):
+        L.check(lib, h, lib.gpe_set_field(h, m, L.ptr(hbufs[m])))
+    L.check(lib, h, lib.gpe_run(h, args.steps, args.steps, L.ptr(out), None))
+    e2e_s = time.perf_counter() - t0
+    barrier()
+    if dist:
+        import torch
+        t = torch.tensor([e2e_s], device=f"cuda:{local_rank}")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        e2e_s = float(t.item())
+    e2e_value = P * B * args.steps * world / e2e_s
+    state_bytes = 2 * B * P * np.dtype(dtype).itemsize
+    it.close()
+
+    if rank != 0:
+        return
+    ab = algorithmic_bytes(dtype)
+    peak, peak_kind = measured_peaks()
+    per_launch = {"row": (kms[0] / max(kn[0], 1), ab["row"]), "col": (kms[1] / max(kn[1], 1), ab["col"])}
+    dom = max(per_launch, key=lambda k: kms[0] if k == "row" else kms[1])
+    d_ms, d_b = per_launch[dom]
+    achieved = d_b * P * B / (d_ms * 1e-3) / 1e9
+    traffic = None
+    tp = ROOT / "profiles" / "traffic.json"
+    if tp.exists():
+        try:
+            traffic = json.loads(tp.read_text()).get(f"{args.dtype}_{dom}_bytes_per_point")
+            if traffic is not None:
+                traffic = traffic * P * B
+        except Exception:
+            traffic = None
+    line = {
+        "metric": "grid-point-steps/s", "value": value, "unit": "grid-point-steps/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_clean / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64" if dtype == np.complex128 else "f32",
+        "data": "synthetic (zero initial field, pumped; the reference's polariton parameters)",
+        "config": config_dict(dtype, B, world),
+        "e2e": {"value": e2e_value, "unit": "grid-point-steps/s", "h2d_bytes_per_step": state_bytes / args.steps,
+                "d2h_bytes_per_step": state_bytes / args.steps},
+        "gpu_launches": int(launches),
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                     "traffic": traffic, "kernel": f"{dom} pass", "peak_source": f"{peak_kind} hbm_gbs",
+                     "algorithmic_bytes_per_point": d_b, "launch_ms": d_ms,
+                     "kernels": {k: {"launches": int(kn[i]), "total_ms": float(kms[i]),
+                                     "mean_ms": float(kms[i] / max(kn[i], 1)),
+                                     "achieved_gbs": float(ab[k] * P * B / (kms[i] / max(kn[i], 1) * 1e-3) / 1e9)}
+                                 for i, k in enumerate(["row", "col"])}},
+        "clocks": clk.summary(),
+    }
+    if not args.no_cpu:
+        line["cpu_baseline"] = cpu_baseline()
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=200)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--dtype", default="c128", choices=["c128", "c64"])
+    ap.add_argument("--batch", type=int, default=0)
+    ap.add_argument("--no-cpu", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        ap.error("--warmup must be >= 3")
+    rank, world, local_rank = dist_env()
+    if args.impl == "reference":
+        run_reference(args, rank, world)
+        return
+    run_gpu(args, rank, world, local_rank)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,220 @@
+// fft.cuh -- shared-memory Stockham line FFTs for sm_103a.
+//
+// The reference transforms each component with an FFTW / cuFFT plan over the
+// spatial dims (src/misc.jl:53-64): an unnormalised forward transform, and an
+// inverse scaled by 1/P.  Here a line of N = 2^LOGN points is transformed by
+// T = N/E threads that each hold E points in registers.  Thread t always holds
+// the points t + T*i (i < E) before and after every stage, so global loads and
+// stores of a line are fully coalesced and the output is in natural order
+// (Stockham autosort: no bit-reversal pass).  A stage of radix R (R | E) does
+// E/R radix-R DFTs in registers; between stages the points are exchanged once
+// through shared memory.  With R = E = 16 a 1024-point line takes 3 stages and
+// 2 exchanges.
+//
+// Stage s (span NS = product of the earlier radices, radix R), butterfly j:
+//   inputs  x[j + r*N/R], r < R
+//   twiddle x_r *= w_N^{(j mod NS) * r * N/(NS*R)}
+//   outputs y[(j/NS)*NS*R + (j mod NS) + r*NS] = DFT_R(x)_r
+// (the self-sorting Stockham formulation of Van Loan, "Computational Frameworks
+// for the Fast Fourier Transform", SIAM 1992, sec. 1.7).  In the last stage the
+// output index equals the input slot, so no exchange follows it.
+//
+// Twiddles come from a per-length FP64-built table w_N^k = exp(-2 pi i k / N);
+// the inverse uses its conjugate.  The in-register radix-R DFTs use exact
+// constants cos(2 pi k / 16).
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace gpe {
+
+template <typename Real> struct CT;
+template <> struct CT<double> { using T = double2; };
+template <> struct CT<float> { using T = float2; };
+
+template <typename C> __device__ __forceinline__ C cadd(C a, C b) { C r; r.x = a.x + b.x; r.y = a.y + b.y; return r; }
+template <typename C> __device__ __forceinline__ C csub(C a, C b) { C r; r.x = a.x - b.x; r.y = a.y - b.y; return r; }
+template <typename C> __device__ __forceinline__ C cmul(C a, C b) {
+  C r;
+  r.x = a.x * b.x - a.y * b.y;
+  r.y = a.x * b.y + a.y * b.x;
+  return r;
+}
+// a * conj(b)
+template <typename C> __device__ __forceinline__ C cmulc(C a, C b) {
+  C r;
+  r.x = a.x * b.x + a.y * b.y;
+  r.y = a.y * b.x - a.x * b.y;
+  return r;
+}
+template <typename C, typename R> __device__ __forceinline__ C cscale(C a, R s) { C r; r.x = a.x * s; r.y = a.y * s; return r; }
+template <typename C> __device__ __forceinline__ C cmake(double x, double y) { C r; r.x = x; r.y = y; return r; }
+
+// cos(2 pi k / 16), k in [0, 16): exact constants of the regular 16-gon.
+__host__ __device__ constexpr double cos16(int k) {
+  k &= 15;
+  return k == 0 ? 1.0
+       : k == 1 || k == 15 ? 0.92387953251128675613
+       : k == 2 || k == 14 ? 0.70710678118654752440
+       : k == 3 || k == 13 ? 0.38268343236508977173
+       : k == 4 || k == 12 ? 0.0
+       : k == 5 || k == 11 ? -0.38268343236508977173
+       : k == 6 || k == 10 ? -0.70710678118654752440
+       : k == 7 || k == 9 ? -0.92387953251128675613
+       : -1.0;
+}
+__host__ __device__ constexpr double sin16(int k) { return cos16(k - 4); }
+
+__host__ __device__ constexpr int ilog2(int n) { return n <= 1 ? 0 : 1 + ilog2(n >> 1); }
+__host__ __device__ constexpr int bitrev(int v, int bits) {
+  int r = 0;
+  for (int i = 0; i < bits; ++i) r |= ((v >> i) & 1) << (bits - 1 - i);
+  return r;
+}
+
+// d * w_n^i with w_n = exp(DIR * 2 pi i / n), n in {2,4,8,16}
+template <int DIR, int n, int i, typename C>
+__device__ __forceinline__ C twc(C d) {
+  constexpr int k = (i * 16 / n) & 15;
+  if constexpr (k == 0) {
+    return d;
+  } else if constexpr (k == 4) {  // w = DIR * i
+    C r; r.x = -DIR * d.y; r.y = DIR * d.x; return r;
+  } else if constexpr (k == 8) {
+    C r; r.x = -d.x; r.y = -d.y; return r;
+  } else if constexpr (k == 12) {  // w = -DIR * i
+    C r; r.x = DIR * d.y; r.y = -DIR * d.x; return r;
+  } else {
+    using R = decltype(d.x);
+    const R c = (R)cos16(k), s = (R)(DIR * sin16(k));
+    C r; r.x = d.x * c - d.y * s; r.y = d.x * s + d.y * c; return r;
+  }
+}
+
+// Radix-2 decimation-in-frequency layer of half-size H over an array of R points.
+template <int R, int DIR, int H, int B, int I, typename C>
+__device__ __forceinline__ void dif_bfly(C (&v)[R]) {
+  C a = v[B + I], c = v[B + I + H];
+  v[B + I] = cadd(a, c);
+  v[B + I + H] = twc<DIR, 2 * H, I>(csub(a, c));
+}
+template <int R, int DIR, int H, int B, int I, typename C>
+__device__ __forceinline__ void dif_row(C (&v)[R]) {
+  if constexpr (I < H) {
+    dif_bfly<R, DIR, H, B, I>(v);
+    dif_row<R, DIR, H, B, I + 1>(v);
+  }
+}
+template <int R, int DIR, int H, int B, typename C>
+__device__ __forceinline__ void dif_blocks(C (&v)[R]) {
+  if constexpr (B < R) {
+    dif_row<R, DIR, H, B, 0>(v);
+    dif_blocks<R, DIR, H, B + 2 * H>(v);
+  }
+}
+template <int R, int DIR, int H, typename C>
+__device__ __forceinline__ void dif_layers(C (&v)[R]) {
+  if constexpr (H >= 1) {
+    dif_blocks<R, DIR, H, 0>(v);
+    dif_layers<R, DIR, H / 2>(v);
+  }
+}
+
+// In-register DFT of R points (R in {1,2,4,8,16}), natural order in and out.
+template <int R, int DIR, typename C>
+__device__ __forceinline__ void dft_regs(C (&v)[R]) {
+  if constexpr (R > 1) {
+    dif_layers<R, DIR, R / 2>(v);
+    C tmp[R];
+#pragma unroll
+    for (int k = 0; k < R; ++k) tmp[k] = v[bitrev(k, ilog2(R))];
+#pragma unroll
+    for (int k = 0; k < R; ++k) v[k] = tmp[k];
+  }
+}
+
+// ---------------------------------------------------------------- layouts
+// Row layout: each line owns N consecutive shared-memory slots.  The exchange
+// after a stage (NS, R) XOR-swizzles the slot within each 128-byte row with a key
+// taken from the row number, chosen so that both the scattered stage writes and
+// the strided reads of the next stage are free of bank conflicts.
+template <typename C>
+struct RowLayout {
+  C* base;
+  static constexpr int S = 128 / (int)sizeof(C);  // complex slots per 128-byte row
+  static constexpr int LOGS = ilog2(S);
+  template <int NS, int R>
+  __device__ __forceinline__ int addr(int idx) const {
+    constexpr int LOGR = ilog2(R);
+    constexpr int A = (NS == 1) ? (LOGR > LOGS ? LOGR - LOGS : 0) : 0;
+    constexpr int B = (NS > 1 && NS < S) ? (LOGS > LOGR ? LOGS - LOGR : 0) : 0;
+    const int row = idx >> LOGS;
+    return idx ^ (((row >> A) << B) & (S - 1));
+  }
+};
+
+// Column layout: CC lines (columns) interleaved, point n of column c at n*CC + c.
+// Threads of the same row touch consecutive slots, so no swizzle is needed.
+template <typename C, int CC>
+struct ColLayout {
+  C* base;  // already offset by the column index
+  template <int NS, int R>
+  __device__ __forceinline__ int addr(int idx) const { return idx * CC; }
+};
+
+// One Stockham stage.  x: this thread's E points; t: thread index in the line.
+template <typename C, int N, int E, int R, int NS, int DIR, bool LAST, class Lay>
+__device__ __forceinline__ void fft_stage(C (&x)[E], int t, const Lay& lay, const C* __restrict__ tw) {
+  constexpr int T = N / E, Q = E / R;
+#pragma unroll
+  for (int q = 0; q < Q; ++q) {
+    C v[R];
+#pragma unroll
+    for (int r = 0; r < R; ++r) v[r] = x[q + r * Q];
+    const int j = t + q * T;
+    if constexpr (NS > 1) {
+      const int k = j & (NS - 1);
+      constexpr int TS = N / (NS * R);
+#pragma unroll
+      for (int r = 1; r < R; ++r) {
+        const C w = __ldg(tw + k * r * TS);
+        v[r] = (DIR < 0) ? cmul(v[r], w) : cmulc(v[r], w);
+      }
+    }
+    dft_regs<R, DIR>(v);
+    if constexpr (LAST) {
+#pragma unroll
+      for (int r = 0; r < R; ++r) x[q + r * Q] = v[r];
+    } else {
+      const int jb = (j / NS) * NS * R + (j & (NS - 1));
+#pragma unroll
+      for (int r = 0; r < R; ++r) lay.base[lay.template addr<NS, R>(jb + r * NS)] = v[r];
+    }
+  }
+}
+
+template <typename C, int N, int E, int DIR, int NS, class Lay>
+__device__ __forceinline__ void fft_stages(C (&x)[E], int t, const Lay& lay, const C* __restrict__ tw) {
+  constexpr int REM = N / NS;
+  constexpr int R = REM >= E ? E : REM;
+  constexpr bool LAST = (NS * R == N);
+  constexpr int T = N / E;
+  fft_stage<C, N, E, R, NS, DIR, LAST>(x, t, lay, tw);
+  if constexpr (!LAST) {
+    __syncthreads();
+#pragma unroll
+    for (int i = 0; i < E; ++i) x[i] = lay.base[lay.template addr<NS, R>(t + T * i)];
+    __syncthreads();
+    fft_stages<C, N, E, DIR, NS * R>(x, t, lay, tw);
+  }
+}
+
+// Transform one line held as x[i] = point t + T*i.  DIR = -1 forward (unnormalised),
+// DIR = +1 inverse (unnormalised; the 1/P factor is folded into the k-space table).
+// Every thread of the block must call this the same number of times.
+template <typename C, int N, int E, int DIR, class Lay>
+__device__ __forceinline__ void fft_line(C (&x)[E], int t, const Lay& lay, const C* __restrict__ tw) {
+  fft_stages<C, N, E, DIR, 1>(x, t, lay, tw);
+}
+
+}  // namespace gpe

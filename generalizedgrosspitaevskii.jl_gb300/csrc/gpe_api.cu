@@ -1,0 +1,833 @@
+// gpe_api.cu -- the C ABI of include/gpe.h: handle lifetime, host-side table
+// construction in FP64 and the launch sequence of gpe_run.
+//
+// Reference correspondence (paths in GeneralizedGrossPitaevskii.jl):
+//   gpe_create            init(prob, StrangSplitting(), ...)   src/strang_splitting.jl:32-67
+//   gpe_set_dispersion    get_exponential(dispersion, ..., dt)  src/misc.jl:12-20, :53 (1/P of inv(plan))
+//   gpe_set_potential     get_exponential(potential, ..., dt/2) src/strang_splitting.jl:54
+//   gpe_set_pump          get_pump_buffer / evaluate_pump!      src/misc.jl:22-42
+//   gpe_set_noise         sample_noise! + noise term            src/misc.jl:44-51, src/kernels.jl:42
+//   gpe_run               solve! host loop + step!              src/fixed_time_stepping.jl:26-54,
+//                                                              src/strang_splitting.jl:69-90
+#include <cuda_runtime.h>
+
+#include <cmath>
+#include <complex>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "../../include/gpe.h"
+#include "kernels.h"
+
+using cd = std::complex<double>;
+
+namespace gpe {
+template <typename Real, int M> int launch_row_t(int, const PassArgs&, int64_t, cudaStream_t);
+template <typename Real, int M> int launch_col_t(int, const PassArgs&, cudaStream_t);
+template <typename Real, int M> int launch_line1d_t(int, const PassArgs&, cudaStream_t);
+template <typename Real, int M> int launch_nl_only_t(const PassArgs&, cudaStream_t);
+template <typename Real, int M> int launch_norm_t(const PassArgs&, double*, cudaStream_t);
+
+#define GPE_DISPATCH(FN, ...)                                          \
+  if (dtype == GPE_C128) return M == 1 ? FN<double, 1>(__VA_ARGS__)   \
+                                       : FN<double, 2>(__VA_ARGS__);  \
+  return M == 1 ? FN<float, 1>(__VA_ARGS__) : FN<float, 2>(__VA_ARGS__);
+
+int launch_row(int dtype, int M, int logn, const PassArgs& a, int64_t nl, cudaStream_t s) { GPE_DISPATCH(launch_row_t, logn, a, nl, s) }
+int launch_col(int dtype, int M, int logn, const PassArgs& a, cudaStream_t s) { GPE_DISPATCH(launch_col_t, logn, a, s) }
+int launch_line1d(int dtype, int M, int logn, const PassArgs& a, cudaStream_t s) { GPE_DISPATCH(launch_line1d_t, logn, a, s) }
+int launch_nl_only(int dtype, int M, const PassArgs& a, cudaStream_t s) { GPE_DISPATCH(launch_nl_only_t, a, s) }
+int launch_norm(int dtype, int M, const PassArgs& a, double* out, cudaStream_t s) { GPE_DISPATCH(launch_norm_t, a, out, s) }
+}  // namespace gpe
+
+using gpe::PassArgs;
+
+struct gpe_handle {
+  gpe_desc d{};
+  int dev = 0;
+  int M = 1, dtype = GPE_C128, ndim = 2;
+  size_t rsz = 8, csz = 16;  // bytes per real / complex
+  int64_t n[3] = {1, 1, 1};
+  int logn[3] = {0, 0, 0};
+  int64_t P = 1, B = 1;
+  double dV = 1.0;
+  cudaStream_t stream = nullptr;
+  cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+  void* u[2] = {nullptr, nullptr};
+  void* tw[3] = {nullptr, nullptr, nullptr};
+  void* ktab = nullptr;
+  int kkind = GPE_TABLE_NONE;
+  std::vector<cd> Dsamples;  // dispersion samples kept for gpe_energy
+  int dkind = GPE_TABLE_NONE;
+  void* vtab = nullptr;
+  int vkind = GPE_TABLE_NONE;
+  std::vector<cd> Vsamples;
+  int vskind = GPE_TABLE_NONE;
+  void* pprof[2] = {nullptr, nullptr};
+  int pprof_cplx = 0;
+  std::vector<cd> pprof_host[2];
+  double2* pamp[2] = {nullptr, nullptr};
+  int64_t pamp_n[2] = {0, 0};
+  void* etaprof[2] = {nullptr, nullptr};
+  int noise = GPE_NOISE_OFF;
+  uint64_t seed = 0;
+  double eta[2][2] = {{0, 0}, {0, 0}};
+  double g[2][2][2] = {};
+  double c[2][2] = {};
+  int nl_on[2] = {0, 0};
+  double t = 0.0;
+  int64_t steps = 0;
+  void* save_buf = nullptr;
+  size_t save_cap = 0;
+  void* xi_buf = nullptr;
+  size_t xi_cap = 0;
+  double* red = nullptr;  // reduction scratch (4 doubles)
+  double last_ms = 0.0;
+  int64_t last_launches = 0;
+  // per-launch timing (gpe_set_timing)
+  int timing = 0;
+  std::vector<cudaEvent_t> evpool;
+  std::vector<int> evkind;  // kernel kind of each recorded pair
+  double kms[3] = {0, 0, 0};
+  int64_t kn[3] = {0, 0, 0};
+  std::string err;
+};
+
+static std::string g_create_error;
+static const char* kVersion = "libgpe " "1.0" " (sm_103a; StrangSplitting backend)";
+
+static int fail(gpe_handle* h, int code, const char* fmt, ...) {
+  char buf[512];
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(buf, sizeof buf, fmt, ap);
+  va_end(ap);
+  if (h) h->err = buf;
+  else g_create_error = buf;
+  return code;
+}
+
+#define CK(h, call)                                                                        \
+  do {                                                                                     \
+    cudaError_t e_ = (call);                                                               \
+    if (e_ != cudaSuccess)                                                                 \
+      return fail(h, e_ == cudaErrorMemoryAllocation ? GPE_ERR_NOMEM : GPE_ERR_CUDA,      \
+                  "%s failed: %s", #call, cudaGetErrorString(e_));                        \
+  } while (0)
+
+#define LK(h, call)                                                                        \
+  do {                                                                                     \
+    int e_ = (call);                                                                       \
+    if (e_ != 0) return fail(h, GPE_ERR_CUDA, "kernel launch failed: %s", cudaGetErrorString((cudaError_t)e_)); \
+  } while (0)
+
+static bool is_pow2(int64_t v) { return v > 0 && (v & (v - 1)) == 0; }
+static int ilog2i(int64_t v) { int r = 0; while ((1ll << r) < v) ++r; return r; }
+
+// Upload n complex FP64 values converted to the handle precision.
+static int upload_complex(gpe_handle* h, void** dst, const cd* src, size_t n) {
+  if (!*dst) CK(h, cudaMalloc(dst, n * h->csz));
+  if (h->dtype == GPE_C128) {
+    CK(h, cudaMemcpy(*dst, src, n * 16, cudaMemcpyHostToDevice));
+  } else {
+    std::vector<float> tmp(2 * n);
+    for (size_t i = 0; i < n; ++i) { tmp[2 * i] = (float)src[i].real(); tmp[2 * i + 1] = (float)src[i].imag(); }
+    CK(h, cudaMemcpy(*dst, tmp.data(), n * 8, cudaMemcpyHostToDevice));
+  }
+  return GPE_OK;
+}
+static int upload_real(gpe_handle* h, void** dst, const double* src, size_t n) {
+  if (!*dst) CK(h, cudaMalloc(dst, n * h->rsz));
+  if (h->dtype == GPE_C128) {
+    CK(h, cudaMemcpy(*dst, src, n * 8, cudaMemcpyHostToDevice));
+  } else {
+    std::vector<float> tmp(n);
+    for (size_t i = 0; i < n; ++i) tmp[i] = (float)src[i];
+    CK(h, cudaMemcpy(*dst, tmp.data(), n * 4, cudaMemcpyHostToDevice));
+  }
+  return GPE_OK;
+}
+
+// exp(A) for a 2x2 complex matrix: e^{tr/2} [cosh(s) I + sinh(s)/s (A - tr/2 I)],
+// s^2 = ((a-d)/2)^2 + bc; sinh(s)/s by its series for small |s|.
+static void expm2(const cd A[4], cd out[4]) {
+  const cd a = A[0], b = A[1], c = A[2], d = A[3];
+  const cd ht = 0.5 * (a + d);
+  const cd s = std::sqrt(0.25 * (a - d) * (a - d) + b * c);
+  const cd ch = std::cosh(s);
+  cd sh;
+  if (std::abs(s) < 1e-3) {
+    const cd s2 = s * s;
+    sh = 1.0 + s2 / 6.0 + s2 * s2 / 120.0;
+  } else {
+    sh = std::sinh(s) / s;
+  }
+  const cd e = std::exp(ht);
+  out[0] = e * (ch + sh * (a - ht));
+  out[3] = e * (ch + sh * (d - ht));
+  out[1] = e * sh * b;
+  out[2] = e * sh * c;
+}
+
+static int table_entries(const gpe_handle* h, int kind) {
+  return kind == GPE_TABLE_SCALAR ? 1 : kind == GPE_TABLE_DIAG ? h->M : kind == GPE_TABLE_MATRIX ? h->M * h->M : 0;
+}
+
+// Build cis(-delta * f) * scale for samples f of the given kind; returns the kind
+// actually stored (a 1x1 matrix or a 1-vector is stored as a scalar).
+static int build_cis(gpe_handle* h, const double* f, int kind, double delta, double scale, std::vector<cd>& out) {
+  const int64_t P = h->P;
+  const int ne = table_entries(h, kind);
+  const cd* fs = reinterpret_cast<const cd*>(f);
+  out.resize((size_t)ne * P);
+  if (kind == GPE_TABLE_MATRIX && h->M == 2) {
+    for (int64_t p = 0; p < P; ++p) {
+      cd A[4], E[4];
+      for (int q = 0; q < 4; ++q) A[q] = cd(0.0, -delta) * fs[(size_t)q * P + p];
+      expm2(A, E);
+      for (int q = 0; q < 4; ++q) out[(size_t)q * P + p] = E[q] * scale;
+    }
+    return GPE_TABLE_MATRIX;
+  }
+  for (size_t i = 0; i < (size_t)ne * P; ++i) out[i] = std::exp(cd(0.0, -delta) * fs[i]) * scale;
+  if (h->M == 1) return GPE_TABLE_SCALAR;
+  return kind;
+}
+
+static bool all_finite(const double* v, size_t n) {
+  for (size_t i = 0; i < n; ++i)
+    if (!std::isfinite(v[i])) return false;
+  return true;
+}
+
+extern "C" {
+
+const char* gpe_version(void) { return kVersion; }
+
+const char* gpe_last_error(const gpe_handle* h) { return h ? h->err.c_str() : g_create_error.c_str(); }
+
+int gpe_create(const gpe_desc* desc, gpe_handle** out) {
+  if (!desc || !out) return fail(nullptr, GPE_ERR_INVALID, "null argument");
+  *out = nullptr;
+  if (desc->abi_version != GPE_ABI_VERSION)
+    return fail(nullptr, GPE_ERR_INVALID, "abi_version %d, library has %d", desc->abi_version, GPE_ABI_VERSION);
+  if (desc->ndim < 1 || desc->ndim > 3) return fail(nullptr, GPE_ERR_INVALID, "ndim must be 1, 2 or 3");
+  if (desc->ncomp < 1 || desc->ncomp > 2) return fail(nullptr, GPE_ERR_UNSUPPORTED, "ncomp must be 1 or 2");
+  if (desc->dtype != GPE_C128 && desc->dtype != GPE_C64) return fail(nullptr, GPE_ERR_INVALID, "bad dtype");
+  if (desc->batch < 1) return fail(nullptr, GPE_ERR_INVALID, "batch must be >= 1");
+  if (!(desc->dt > 0) || !std::isfinite(desc->dt)) return fail(nullptr, GPE_ERR_INVALID, "dt must be positive and finite");
+  if (!std::isfinite(desc->t0)) return fail(nullptr, GPE_ERR_INVALID, "t0 must be finite");
+  if (desc->ndim == 3) return fail(nullptr, GPE_ERR_UNSUPPORTED, "3D grids are not supported by this build");
+  for (int a = 0; a < desc->ndim; ++a) {
+    if (!is_pow2(desc->n[a]) || desc->n[a] < 16 || desc->n[a] > 4096)
+      return fail(nullptr, GPE_ERR_UNSUPPORTED, "axis %d: n = %lld, need a power of two in [16, 4096]", a, (long long)desc->n[a]);
+    if (!(desc->lengths[a] > 0) || !std::isfinite(desc->lengths[a]))
+      return fail(nullptr, GPE_ERR_INVALID, "axis %d: length must be positive", a);
+  }
+  int dev = desc->device;
+  if (dev >= 0) {
+    cudaError_t se = cudaSetDevice(dev);
+    if (se != cudaSuccess) return fail(nullptr, GPE_ERR_CUDA, "cudaSetDevice(%d) failed: %s", dev, cudaGetErrorString(se));
+  } else if (cudaGetDevice(&dev) != cudaSuccess) {
+    return fail(nullptr, GPE_ERR_CUDA, "no CUDA device");
+  }
+  gpe_handle* h = new gpe_handle();
+  h->d = *desc;
+  h->dev = dev;
+  h->M = desc->ncomp;
+  h->dtype = desc->dtype;
+  h->ndim = desc->ndim;
+  h->rsz = desc->dtype == GPE_C128 ? 8 : 4;
+  h->csz = 2 * h->rsz;
+  h->B = desc->batch;
+  h->P = 1;
+  h->dV = 1.0;
+  for (int a = 0; a < h->ndim; ++a) {
+    h->n[a] = desc->n[a];
+    h->logn[a] = ilog2i(desc->n[a]);
+    h->P *= desc->n[a];
+    h->dV *= desc->lengths[a] / (double)desc->n[a];
+  }
+  h->t = desc->t0;
+  auto bail = [&](int code) { gpe_destroy(h); return code; };
+  cudaError_t e;
+  if ((e = cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking)) != cudaSuccess ||
+      (e = cudaEventCreate(&h->ev0)) != cudaSuccess || (e = cudaEventCreate(&h->ev1)) != cudaSuccess) {
+    fail(nullptr, GPE_ERR_CUDA, "stream/event creation failed: %s", cudaGetErrorString(e));
+    return bail(GPE_ERR_CUDA);
+  }
+  const size_t bytes = (size_t)h->P * h->B * h->csz;
+  for (int m = 0; m < h->M; ++m) {
+    if ((e = cudaMalloc(&h->u[m], bytes)) != cudaSuccess) {
+      fail(nullptr, GPE_ERR_NOMEM, "cudaMalloc of %zu bytes failed: %s", bytes, cudaGetErrorString(e));
+      return bail(GPE_ERR_NOMEM);
+    }
+    cudaMemset(h->u[m], 0, bytes);
+  }
+  if ((e = cudaMalloc((void**)&h->red, 4 * sizeof(double))) != cudaSuccess) {
+    fail(nullptr, GPE_ERR_NOMEM, "cudaMalloc failed: %s", cudaGetErrorString(e));
+    return bail(GPE_ERR_NOMEM);
+  }
+  // twiddles w_N^k = exp(-2 pi i k / N) per axis, built in FP64
+  for (int a = 0; a < h->ndim; ++a) {
+    const int64_t N = h->n[a];
+    std::vector<cd> w((size_t)N);
+    for (int64_t k = 0; k < N; ++k) {
+      const double th = -2.0 * M_PI * (double)k / (double)N;
+      w[(size_t)k] = cd(std::cos(th), std::sin(th));
+    }
+    int rc = upload_complex(h, &h->tw[a], w.data(), (size_t)N);
+    if (rc) { g_create_error = h->err; return bail(rc); }
+  }
+  cudaDeviceSynchronize();
+  *out = h;
+  return GPE_OK;
+}
+
+int gpe_destroy(gpe_handle* h) {
+  if (!h) return GPE_OK;
+  if (h->stream) cudaStreamSynchronize(h->stream);
+  for (int m = 0; m < 2; ++m) {
+    cudaFree(h->u[m]);
+    cudaFree(h->pprof[m]);
+    cudaFree(h->pamp[m]);
+    cudaFree(h->etaprof[m]);
+  }
+  for (int a = 0; a < 3; ++a) cudaFree(h->tw[a]);
+  cudaFree(h->ktab);
+  cudaFree(h->vtab);
+  cudaFree(h->save_buf);
+  cudaFree(h->xi_buf);
+  cudaFree(h->red);
+  for (cudaEvent_t e : h->evpool) cudaEventDestroy(e);
+  if (h->ev0) cudaEventDestroy(h->ev0);
+  if (h->ev1) cudaEventDestroy(h->ev1);
+  if (h->stream) cudaStreamDestroy(h->stream);
+  delete h;
+  return GPE_OK;
+}
+
+static int check_comp(gpe_handle* h, int comp) {
+  if (!h) return GPE_ERR_INVALID;
+  cudaSetDevice(h->dev);
+  if (comp < 0 || comp >= h->M) return fail(h, GPE_ERR_INVALID, "component %d out of range [0, %d)", comp, h->M);
+  return GPE_OK;
+}
+
+int gpe_set_field(gpe_handle* h, int comp, const void* host) {
+  int rc = check_comp(h, comp);
+  if (rc) return rc;
+  if (!host) return fail(h, GPE_ERR_INVALID, "null field");
+  const size_t n = (size_t)h->P * h->B;
+  if (h->dtype == GPE_C128) {
+    if (!all_finite((const double*)host, 2 * n)) return fail(h, GPE_ERR_NONFINITE, "field %d has NaN or Inf", comp);
+  } else {
+    const float* f = (const float*)host;
+    for (size_t i = 0; i < 2 * n; ++i)
+      if (!std::isfinite(f[i])) return fail(h, GPE_ERR_NONFINITE, "field %d has NaN or Inf", comp);
+  }
+  CK(h, cudaMemcpy(h->u[comp], host, n * h->csz, cudaMemcpyHostToDevice));
+  return GPE_OK;
+}
+
+int gpe_get_field(gpe_handle* h, int comp, void* host) {
+  int rc = check_comp(h, comp);
+  if (rc) return rc;
+  if (!host) return fail(h, GPE_ERR_INVALID, "null destination");
+  CK(h, cudaStreamSynchronize(h->stream));
+  CK(h, cudaMemcpy(host, h->u[comp], (size_t)h->P * h->B * h->csz, cudaMemcpyDeviceToHost));
+  return GPE_OK;
+}
+
+int gpe_set_field_dev(gpe_handle* h, int comp, const void* dev) {
+  int rc = check_comp(h, comp);
+  if (rc) return rc;
+  if (!dev) return fail(h, GPE_ERR_INVALID, "null field");
+  CK(h, cudaMemcpyAsync(h->u[comp], dev, (size_t)h->P * h->B * h->csz, cudaMemcpyDeviceToDevice, h->stream));
+  CK(h, cudaStreamSynchronize(h->stream));
+  return GPE_OK;
+}
+
+int gpe_get_field_dev(gpe_handle* h, int comp, void* dev) {
+  int rc = check_comp(h, comp);
+  if (rc) return rc;
+  if (!dev) return fail(h, GPE_ERR_INVALID, "null destination");
+  CK(h, cudaMemcpyAsync(dev, h->u[comp], (size_t)h->P * h->B * h->csz, cudaMemcpyDeviceToDevice, h->stream));
+  CK(h, cudaStreamSynchronize(h->stream));
+  return GPE_OK;
+}
+
+static int check_kind(gpe_handle* h, int kind) {
+  if (kind != GPE_TABLE_SCALAR && kind != GPE_TABLE_DIAG && kind != GPE_TABLE_MATRIX)
+    return fail(h, GPE_ERR_INVALID, "bad table kind %d", kind);
+  return GPE_OK;
+}
+
+static int store_ktable(gpe_handle* h, const std::vector<cd>& tab, int kind) {
+  cudaFree(h->ktab);
+  h->ktab = nullptr;
+  h->kkind = GPE_TABLE_NONE;
+  int rc = upload_complex(h, &h->ktab, tab.data(), tab.size());
+  if (rc) return rc;
+  h->kkind = kind;
+  return GPE_OK;
+}
+
+int gpe_set_dispersion(gpe_handle* h, const double* D, int kind) {
+  if (!h) return GPE_ERR_INVALID;
+  int rc = check_kind(h, kind);
+  if (rc) return rc;
+  if (!D) return fail(h, GPE_ERR_INVALID, "null dispersion");
+  const size_t ne = (size_t)table_entries(h, kind) * h->P;
+  if (!all_finite(D, 2 * ne)) return fail(h, GPE_ERR_NONFINITE, "dispersion has NaN or Inf");
+  std::vector<cd> tab;
+  // exp(-i dt D) with the 1/P of the normalised inverse transform folded in (exact: P is 2^k)
+  const int stored = build_cis(h, D, kind, h->d.dt, 1.0 / (double)h->P, tab);
+  h->Dsamples.assign(reinterpret_cast<const cd*>(D), reinterpret_cast<const cd*>(D) + ne);
+  h->dkind = kind;
+  return store_ktable(h, tab, stored);
+}
+
+int gpe_set_ktable(gpe_handle* h, const double* table, int kind) {
+  if (!h) return GPE_ERR_INVALID;
+  int rc = check_kind(h, kind);
+  if (rc) return rc;
+  if (!table) return fail(h, GPE_ERR_INVALID, "null table");
+  const size_t ne = (size_t)table_entries(h, kind) * h->P;
+  if (!all_finite(table, 2 * ne)) return fail(h, GPE_ERR_NONFINITE, "k-space table has NaN or Inf");
+  std::vector<cd> tab(ne);
+  const cd* src = reinterpret_cast<const cd*>(table);
+  const double s = 1.0 / (double)h->P;
+  for (size_t i = 0; i < ne; ++i) tab[i] = src[i] * s;
+  int stored = kind;
+  if (h->M == 1) stored = GPE_TABLE_SCALAR;
+  h->Dsamples.clear();
+  h->dkind = GPE_TABLE_NONE;
+  return store_ktable(h, tab, stored);
+}
+
+static int store_vtable(gpe_handle* h, const std::vector<cd>& tab, int kind) {
+  if (kind == GPE_TABLE_MATRIX && (h->nl_on[0] || h->nl_on[1]))
+    return fail(h, GPE_ERR_UNSUPPORTED, "a matrix potential with a diagonal nonlinearity is undefined (SVector * SMatrix)");
+  cudaFree(h->vtab);
+  h->vtab = nullptr;
+  h->vkind = GPE_TABLE_NONE;
+  int rc = upload_complex(h, &h->vtab, tab.data(), tab.size());
+  if (rc) return rc;
+  h->vkind = kind;
+  return GPE_OK;
+}
+
+int gpe_set_potential(gpe_handle* h, const double* V, int kind) {
+  if (!h) return GPE_ERR_INVALID;
+  int rc = check_kind(h, kind);
+  if (rc) return rc;
+  if (!V) return fail(h, GPE_ERR_INVALID, "null potential");
+  const size_t ne = (size_t)table_entries(h, kind) * h->P;
+  if (!all_finite(V, 2 * ne)) return fail(h, GPE_ERR_NONFINITE, "potential has NaN or Inf");
+  std::vector<cd> tab;
+  const int stored = build_cis(h, V, kind, 0.5 * h->d.dt, 1.0, tab);
+  h->Vsamples.assign(reinterpret_cast<const cd*>(V), reinterpret_cast<const cd*>(V) + ne);
+  h->vskind = kind;
+  return store_vtable(h, tab, stored);
+}
+
+int gpe_set_vtable(gpe_handle* h, const double* table, int kind) {
+  if (!h) return GPE_ERR_INVALID;
+  int rc = check_kind(h, kind);
+  if (rc) return rc;
+  if (!table) return fail(h, GPE_ERR_INVALID, "null table");
+  const size_t ne = (size_t)table_entries(h, kind) * h->P;
+  if (!all_finite(table, 2 * ne)) return fail(h, GPE_ERR_NONFINITE, "potential table has NaN or Inf");
+  std::vector<cd> tab(reinterpret_cast<const cd*>(table), reinterpret_cast<const cd*>(table) + ne);
+  h->Vsamples.clear();
+  h->vskind = GPE_TABLE_NONE;
+  return store_vtable(h, tab, h->M == 1 ? GPE_TABLE_SCALAR : kind);
+}
+
+int gpe_set_nonlinearity(gpe_handle* h, const double* g, const double* c) {
+  if (!h) return GPE_ERR_INVALID;
+  const int M = h->M;
+  double gg[2][2][2] = {}, cc[2][2] = {};
+  if (g) {
+    if (!all_finite(g, 2 * M * M)) return fail(h, GPE_ERR_NONFINITE, "nonlinearity g has NaN or Inf");
+    for (int j = 0; j < M; ++j)
+      for (int l = 0; l < M; ++l) { gg[j][l][0] = g[2 * (j * M + l)]; gg[j][l][1] = g[2 * (j * M + l) + 1]; }
+  }
+  if (c) {
+    if (!all_finite(c, 2 * M)) return fail(h, GPE_ERR_NONFINITE, "nonlinearity c has NaN or Inf");
+    for (int j = 0; j < M; ++j) { cc[j][0] = c[2 * j]; cc[j][1] = c[2 * j + 1]; }
+  }
+  int on[2] = {0, 0};
+  for (int j = 0; j < M; ++j) {
+    for (int l = 0; l < M; ++l) on[j] |= (gg[j][l][0] != 0 || gg[j][l][1] != 0);
+    on[j] |= (cc[j][0] != 0 || cc[j][1] != 0);
+  }
+  if ((on[0] || on[1]) && h->vkind == GPE_TABLE_MATRIX)
+    return fail(h, GPE_ERR_UNSUPPORTED, "a diagonal nonlinearity with a matrix potential is undefined (SVector * SMatrix)");
+  memcpy(h->g, gg, sizeof gg);
+  memcpy(h->c, cc, sizeof cc);
+  h->nl_on[0] = on[0];
+  h->nl_on[1] = on[1];
+  return GPE_OK;
+}
+
+int gpe_set_pump(gpe_handle* h, int comp, const double* profile, int profile_complex, const double* amp, int64_t n_amp) {
+  int rc = check_comp(h, comp);
+  if (rc) return rc;
+  cudaFree(h->pprof[comp]);
+  h->pprof[comp] = nullptr;
+  cudaFree(h->pamp[comp]);
+  h->pamp[comp] = nullptr;
+  h->pamp_n[comp] = 0;
+  h->pprof_host[comp].clear();
+  if (!profile) return GPE_OK;
+  if (!amp || n_amp < 1) return fail(h, GPE_ERR_INVALID, "pump needs at least one amplitude");
+  const size_t P = (size_t)h->P;
+  if (!all_finite(profile, profile_complex ? 2 * P : P)) return fail(h, GPE_ERR_NONFINITE, "pump profile has NaN or Inf");
+  if (!all_finite(amp, 2 * (size_t)n_amp)) return fail(h, GPE_ERR_NONFINITE, "pump amplitude has NaN or Inf");
+  std::vector<cd>& ph = h->pprof_host[comp];
+  ph.resize(P);
+  for (size_t p = 0; p < P; ++p) ph[p] = profile_complex ? cd(profile[2 * p], profile[2 * p + 1]) : cd(profile[p], 0.0);
+  CK(h, cudaMalloc((void**)&h->pamp[comp], (size_t)n_amp * sizeof(double2)));
+  CK(h, cudaMemcpy(h->pamp[comp], amp, (size_t)n_amp * sizeof(double2), cudaMemcpyHostToDevice));
+  h->pamp_n[comp] = n_amp;
+  // All pumped components share one profile format: complex if any profile is complex.
+  int want_cplx = 0;
+  for (int m = 0; m < h->M; ++m)
+    for (const cd& v : h->pprof_host[m])
+      if (v.imag() != 0.0) { want_cplx = 1; break; }
+  h->pprof_cplx = want_cplx;
+  for (int m = 0; m < h->M; ++m) {
+    cudaFree(h->pprof[m]);
+    h->pprof[m] = nullptr;
+    if (h->pprof_host[m].empty()) continue;
+    if (want_cplx) {
+      rc = upload_complex(h, &h->pprof[m], h->pprof_host[m].data(), P);
+    } else {
+      std::vector<double> re(P);
+      for (size_t p = 0; p < P; ++p) re[p] = h->pprof_host[m][p].real();
+      rc = upload_real(h, &h->pprof[m], re.data(), P);
+    }
+    if (rc) return rc;
+  }
+  return GPE_OK;
+}
+
+int gpe_set_noise(gpe_handle* h, int mode, uint64_t seed, const double* eta, const double* eta_profile) {
+  if (!h) return GPE_ERR_INVALID;
+  if (mode != GPE_NOISE_OFF && mode != GPE_NOISE_PHILOX && mode != GPE_NOISE_REPLAY)
+    return fail(h, GPE_ERR_INVALID, "bad noise mode %d", mode);
+  for (int m = 0; m < 2; ++m) { cudaFree(h->etaprof[m]); h->etaprof[m] = nullptr; }
+  h->noise = mode;
+  h->seed = seed;
+  memset(h->eta, 0, sizeof h->eta);
+  if (mode == GPE_NOISE_OFF) return GPE_OK;
+  if (!eta) return fail(h, GPE_ERR_INVALID, "noise needs eta");
+  if (!all_finite(eta, 2 * h->M)) return fail(h, GPE_ERR_NONFINITE, "eta has NaN or Inf");
+  for (int m = 0; m < h->M; ++m) { h->eta[m][0] = eta[2 * m]; h->eta[m][1] = eta[2 * m + 1]; }
+  if (eta_profile) {
+    if (!all_finite(eta_profile, (size_t)h->M * h->P)) return fail(h, GPE_ERR_NONFINITE, "eta profile has NaN or Inf");
+    for (int m = 0; m < h->M; ++m) {
+      int rc = upload_real(h, &h->etaprof[m], eta_profile + (size_t)m * h->P, (size_t)h->P);
+      if (rc) return rc;
+    }
+  }
+  return GPE_OK;
+}
+
+// Event pair around one launch when timing is on.
+struct TimedLaunch {
+  gpe_handle* h;
+  int kind;
+  size_t idx = 0;
+  TimedLaunch(gpe_handle* hh, int k) : h(hh), kind(k) {
+    if (!h->timing) return;
+    idx = h->evkind.size();
+    while (h->evpool.size() < 2 * (idx + 1)) {
+      cudaEvent_t e;
+      cudaEventCreate(&e);
+      h->evpool.push_back(e);
+    }
+    h->evkind.push_back(kind);
+    cudaEventRecord(h->evpool[2 * idx], h->stream);
+  }
+  ~TimedLaunch() {
+    if (h->timing) cudaEventRecord(h->evpool[2 * idx + 1], h->stream);
+  }
+};
+
+// Fill the coefficient part of the pass arguments.
+static PassArgs base_args(gpe_handle* h) {
+  PassArgs a;
+  memset(&a, 0, sizeof a);
+  a.n0 = (int32_t)h->n[0];
+  a.n1 = (int32_t)h->n[1];
+  a.n2 = (int32_t)h->n[2];
+  a.P = h->P;
+  a.B = h->B;
+  for (int m = 0; m < h->M; ++m) a.u[m] = h->u[m];
+  a.ktab = h->ktab;
+  a.kkind = h->kkind;
+  a.vtab = h->vtab;
+  a.vkind = h->vkind;
+  for (int j = 0; j < 2; ++j) {
+    a.nl_on[j] = h->nl_on[j];
+    for (int l = 0; l < 2; ++l)
+      for (int r = 0; r < 2; ++r) { a.g[j][l][r] = h->g[j][l][r]; a.gf[j][l][r] = (float)h->g[j][l][r]; }
+    for (int r = 0; r < 2; ++r) { a.c[j][r] = h->c[j][r]; a.cf[j][r] = (float)h->c[j][r]; }
+  }
+  for (int m = 0; m < h->M; ++m) {
+    a.pprof[m] = h->pprof[m];
+    a.pamp[m] = h->pamp[m];
+    a.pamp_n[m] = h->pamp_n[m];
+    a.etaprof[m] = h->etaprof[m];
+  }
+  a.pprof_cplx = h->pprof_cplx;
+  a.noise = h->noise;
+  a.seed_lo = (uint32_t)h->seed;
+  a.seed_hi = (uint32_t)(h->seed >> 32);
+  // -i sqrt(dt/2) eta  (src/kernels.jl:42 with delta = dt/2)
+  const double sq = std::sqrt(0.5 * h->d.dt);
+  for (int m = 0; m < h->M; ++m) {
+    a.nfac[m][0] = sq * h->eta[m][1];
+    a.nfac[m][1] = -sq * h->eta[m][0];
+    a.nfacf[m][0] = (float)a.nfac[m][0];
+    a.nfacf[m][1] = (float)a.nfac[m][1];
+  }
+  a.dt = h->d.dt;
+  a.dthf = (float)(0.5 * h->d.dt);
+  a.hA = a.hB = -1;
+  return a;
+}
+
+static int ensure(gpe_handle* h, void** buf, size_t* cap, size_t bytes) {
+  if (*cap >= bytes) return GPE_OK;
+  cudaFree(*buf);
+  *buf = nullptr;
+  *cap = 0;
+  CK(h, cudaMalloc(buf, bytes));
+  *cap = bytes;
+  return GPE_OK;
+}
+
+// Enqueue nsteps steps; saves go to save_dev (layout [m][slot][b][p]) with nsaves_total
+// slots per component.  Returns the number of launches in *launches.
+static int enqueue_steps(gpe_handle* h, int64_t nsteps, int64_t save_every, void* save_dev, int64_t nsaves_total,
+                         const void* xi_dev, int64_t* launches) {
+  PassArgs a = base_args(h);
+  const int64_t k0 = h->steps;
+  a.xi = xi_dev;
+  a.xi_h0 = 2 * k0;  // replayed xi are indexed from this run's first half step
+  const int64_t plane = h->P * h->B;
+  const bool has_k = h->ktab != nullptr;
+  int64_t nl = 0;
+  auto slot_ptrs = [&](PassArgs& pa, int64_t slot) {
+    for (int m = 0; m < h->M; ++m)
+      pa.save[m] = (char*)save_dev + ((size_t)m * nsaves_total + slot) * plane * h->csz;
+  };
+  if (!has_k || h->ndim == 1) {
+    // pointwise-only problems and 1D lines run all steps in one resident launch
+    a.nsteps = nsteps;
+    a.step0 = k0;
+    a.save_every = save_every;
+    a.save_stride = plane;
+    if (save_every > 0) slot_ptrs(a, 0);
+    TimedLaunch tl(h, 2);
+    if (!has_k) {
+      LK(h, gpe::launch_nl_only(h->dtype, h->M, a, h->stream));
+    } else {
+      a.tw = h->tw[0];
+      LK(h, gpe::launch_line1d(h->dtype, h->M, h->logn[0], a, h->stream));
+    }
+    *launches = 1;
+    return GPE_OK;
+  }
+  // 2D: entry row pass, then (column pass, row pass) per step
+  const int64_t nrows = h->P / h->n[0] * h->B;
+  PassArgs r = a;
+  r.tw = h->tw[0];
+  r.do_ifft = 0;
+  r.do_fft = 1;
+  r.hA = 2 * k0;
+  r.hB = -1;
+  {
+    TimedLaunch tl(h, 0);
+    LK(h, gpe::launch_row(h->dtype, h->M, h->logn[0], r, nrows, h->stream));
+  }
+  ++nl;
+  PassArgs c = a;
+  c.tw = h->tw[1];
+  c.ld = h->n[0];
+  c.ostride = 0;
+  c.nouter = 1;
+  c.col_fwd = 1;
+  c.col_inv = 1;
+  for (int64_t s = 0; s < nsteps; ++s) {
+    {
+      TimedLaunch tl(h, 1);
+      LK(h, gpe::launch_col(h->dtype, h->M, h->logn[1], c, h->stream));
+    }
+    const bool last = (s == nsteps - 1);
+    PassArgs rr = a;
+    rr.tw = h->tw[0];
+    rr.do_ifft = 1;
+    rr.hA = 2 * (k0 + s) + 1;
+    rr.hB = last ? -1 : 2 * (k0 + s + 1);
+    rr.do_fft = last ? 0 : 1;
+    if (save_every > 0 && (s + 1) % save_every == 0) slot_ptrs(rr, (s + 1) / save_every - 1);
+    {
+      TimedLaunch tl(h, 0);
+      LK(h, gpe::launch_row(h->dtype, h->M, h->logn[0], rr, nrows, h->stream));
+    }
+    nl += 2;
+  }
+  *launches = nl;
+  return GPE_OK;
+}
+
+static int run_common(gpe_handle* h, int64_t nsteps, int64_t save_every, void* out, bool out_is_dev, double* ts_out,
+                      const void* xi_host) {
+  if (!h) return GPE_ERR_INVALID;
+  CK(h, cudaSetDevice(h->dev));
+  if (nsteps < 0) return fail(h, GPE_ERR_INVALID, "nsteps must be >= 0");
+  if (save_every < 0) return fail(h, GPE_ERR_INVALID, "save_every must be >= 0");
+  if (save_every > 0 && nsteps % save_every != 0)
+    return fail(h, GPE_ERR_INVALID, "nsteps (%lld) must be a multiple of save_every (%lld)", (long long)nsteps,
+                (long long)save_every);
+  const int64_t nsaves = save_every > 0 ? nsteps / save_every : 0;
+  if (nsaves > 0 && !out) return fail(h, GPE_ERR_INVALID, "null save buffer");
+  for (int m = 0; m < h->M; ++m)
+    if (h->pprof[m] && h->pamp_n[m] > 1 && h->pamp_n[m] < 2 * (h->steps + nsteps) + 1)
+      return fail(h, GPE_ERR_INVALID, "pump %d has %lld amplitudes, %lld steps need %lld", m, (long long)h->pamp_n[m],
+                  (long long)(h->steps + nsteps), (long long)(2 * (h->steps + nsteps) + 1));
+  if (h->noise == GPE_NOISE_REPLAY && !xi_host)
+    return fail(h, GPE_ERR_INVALID, "noise mode is replay: use gpe_run_replay");
+  if (xi_host && h->noise != GPE_NOISE_REPLAY) return fail(h, GPE_ERR_INVALID, "gpe_run_replay needs noise mode replay");
+  h->last_ms = 0.0;
+  h->last_launches = 0;
+  if (nsteps == 0) return GPE_OK;
+  const size_t plane_bytes = (size_t)h->P * h->B * h->csz;
+  if (xi_host) {
+    const size_t xb = (size_t)2 * nsteps * h->M * plane_bytes;
+    int rc = ensure(h, &h->xi_buf, &h->xi_cap, xb);
+    if (rc) return rc;
+    CK(h, cudaMemcpy(h->xi_buf, xi_host, xb, cudaMemcpyHostToDevice));
+  }
+  void* save_dev = nullptr;
+  if (nsaves > 0) {
+    if (out_is_dev) {
+      save_dev = out;
+    } else {
+      int rc = ensure(h, &h->save_buf, &h->save_cap, (size_t)h->M * nsaves * plane_bytes);
+      if (rc) return rc;
+      save_dev = h->save_buf;
+    }
+  }
+  h->evkind.clear();
+  CK(h, cudaEventRecord(h->ev0, h->stream));
+  int64_t launches = 0;
+  int rc = enqueue_steps(h, nsteps, save_every, save_dev, nsaves, xi_host ? h->xi_buf : nullptr, &launches);
+  if (rc) return rc;
+  CK(h, cudaEventRecord(h->ev1, h->stream));
+  CK(h, cudaEventSynchronize(h->ev1));
+  float ms = 0.f;
+  cudaEventElapsedTime(&ms, h->ev0, h->ev1);
+  h->last_ms = ms;
+  h->last_launches = launches;
+  for (int k = 0; k < 3; ++k) { h->kms[k] = 0.0; h->kn[k] = 0; }
+  for (size_t i = 0; i < h->evkind.size(); ++i) {
+    float e = 0.f;
+    cudaEventElapsedTime(&e, h->evpool[2 * i], h->evpool[2 * i + 1]);
+    h->kms[h->evkind[i]] += e;
+    h->kn[h->evkind[i]] += 1;
+  }
+  CK(h, cudaGetLastError());
+  // times at saves: t accumulated with t += dt (src/fixed_time_stepping.jl:44,49)
+  double t = h->t;
+  int64_t slot = 0;
+  for (int64_t s = 0; s < nsteps; ++s) {
+    t += h->d.dt;
+    if (save_every > 0 && (s + 1) % save_every == 0) {
+      if (ts_out) ts_out[slot] = t;
+      ++slot;
+    }
+  }
+  h->t = t;
+  h->steps += nsteps;
+  if (nsaves > 0 && !out_is_dev) CK(h, cudaMemcpy(out, save_dev, (size_t)h->M * nsaves * plane_bytes, cudaMemcpyDeviceToHost));
+  return GPE_OK;
+}
+
+int gpe_run(gpe_handle* h, int64_t nsteps, int64_t save_every, void* out_host, double* ts_out) {
+  return run_common(h, nsteps, save_every, out_host, false, ts_out, nullptr);
+}
+
+int gpe_run_dev(gpe_handle* h, int64_t nsteps, int64_t save_every, void* out_dev, double* ts_out) {
+  return run_common(h, nsteps, save_every, out_dev, true, ts_out, nullptr);
+}
+
+int gpe_run_replay(gpe_handle* h, int64_t nsteps, int64_t save_every, const void* xi_host, void* out_host,
+                   double* ts_out) {
+  if (!h) return GPE_ERR_INVALID;
+  if (!xi_host && nsteps > 0) return fail(h, GPE_ERR_INVALID, "null xi");
+  return run_common(h, nsteps, save_every, out_host, false, ts_out, xi_host);
+}
+
+int gpe_get_state(gpe_handle* h, gpe_state* st) {
+  if (!h || !st) return h ? fail(h, GPE_ERR_INVALID, "null state") : GPE_ERR_INVALID;
+  st->t = h->t;
+  st->steps = h->steps;
+  st->seed = h->seed;
+  st->noise_mode = h->noise;
+  st->reserved = 0;
+  return GPE_OK;
+}
+
+int gpe_set_state(gpe_handle* h, const gpe_state* st) {
+  if (!h || !st) return h ? fail(h, GPE_ERR_INVALID, "null state") : GPE_ERR_INVALID;
+  if (!std::isfinite(st->t) || st->steps < 0) return fail(h, GPE_ERR_INVALID, "bad state");
+  h->t = st->t;
+  h->steps = st->steps;
+  h->seed = st->seed;
+  return GPE_OK;
+}
+
+int gpe_norm(gpe_handle* h, double* out) {
+  if (!h) return GPE_ERR_INVALID;
+  if (!out) return fail(h, GPE_ERR_INVALID, "null output");
+  PassArgs a = base_args(h);
+  CK(h, cudaMemsetAsync(h->red, 0, 4 * sizeof(double), h->stream));
+  LK(h, gpe::launch_norm(h->dtype, h->M, a, h->red, h->stream));
+  double tmp[4];
+  CK(h, cudaMemcpyAsync(tmp, h->red, 4 * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+  CK(h, cudaStreamSynchronize(h->stream));
+  for (int m = 0; m < h->M; ++m) out[m] = tmp[m] * h->dV;
+  return GPE_OK;
+}
+
+int gpe_energy(gpe_handle* h, double* out) {
+  if (!h) return GPE_ERR_INVALID;
+  (void)out;
+  return fail(h, GPE_ERR_UNSUPPORTED, "gpe_energy is not available in this build");
+}
+
+int gpe_set_timing(gpe_handle* h, int on) {
+  if (!h) return GPE_ERR_INVALID;
+  h->timing = on ? 1 : 0;
+  return GPE_OK;
+}
+
+int gpe_kernel_times(const gpe_handle* h, double* ms, int64_t* n) {
+  if (!h || !ms || !n) return GPE_ERR_INVALID;
+  for (int k = 0; k < 3; ++k) { ms[k] = h->kms[k]; n[k] = h->kn[k]; }
+  return GPE_OK;
+}
+
+double gpe_last_run_ms(const gpe_handle* h) { return h ? h->last_ms : 0.0; }
+int64_t gpe_last_run_launches(const gpe_handle* h) { return h ? h->last_launches : 0; }
+
+}  // extern "C"

@@ -1,0 +1,6 @@
+// Instantiates the line passes for double fields with 2 component(s); one
+// translation unit per (precision, M) so the build compiles them in parallel.
+#include "passes.cuh"
+namespace gpe {
+GPE_INSTANTIATE(double, 2)
+}  // namespace gpe

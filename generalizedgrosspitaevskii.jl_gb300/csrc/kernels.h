@@ -1,0 +1,70 @@
+// kernels.h -- argument block shared by the host driver and the pass kernels.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace gpe {
+
+enum TableKind { TAB_NONE = 0, TAB_SCALAR = 1, TAB_DIAG = 2, TAB_MATRIX = 3 };
+enum NoiseMode { NOISE_OFF = 0, NOISE_PHILOX = 1, NOISE_REPLAY = 2 };
+
+// One launch of a line pass.  Plain data only: it is copied to the kernel's
+// parameter space by value.
+struct PassArgs {
+  // geometry: n[0] = x (fastest); P = n0*n1*n2 spatial points; B trajectories
+  int32_t n0, n1, n2;
+  int64_t P, B;
+  // fields (M planes of B*P complex numbers in the pass precision)
+  void* u[2];
+  // optional copy of the real-space state after the first half step of the pass
+  void* save[2];
+  // k-space table exp(-i dt D)/P (col pass / 1D) and real-space table exp(-i dt/2 V)
+  const void* ktab;
+  int32_t kkind;
+  const void* vtab;
+  int32_t vkind;
+  // twiddles w_N^k, k < N, for the transformed line length
+  const void* tw;
+  // nonlinearity G_j = sum_l g[j][l] |u_l|^2 + c[j] (complex); FP64 values and their
+  // FP32 roundings, so the FP32 passes never convert per point
+  int32_t nl_on[2];
+  double g[2][2][2];
+  double c[2][2];
+  float gf[2][2][2];
+  float cf[2][2];
+  // pump F_m = a_m(t) p_m(r): profile (real or complex, pass precision), FP64 amplitudes
+  const void* pprof[2];
+  int32_t pprof_cplx;
+  const double2* pamp[2];
+  int64_t pamp_n[2];
+  // noise: -i sqrt(dt/2) eta_m (FP64, host-formed) [* eta profile] * xi
+  int32_t noise;
+  uint32_t seed_lo, seed_hi;
+  double nfac[2][2];
+  float nfacf[2][2];
+  const void* etaprof[2];
+  const void* xi;     // replay: [half - xi_h0][m][b][p]
+  int64_t xi_h0;
+  double dt;
+  float dthf;  // dt/2 rounded to FP32
+  // row pass program: [iFFT] [half hA] [save] [half hB] [FFT]; h < 0 skips a half
+  int32_t do_ifft, do_fft;
+  int64_t hA, hB;
+  // 1D resident program: nsteps full steps from step0, save every save_every steps
+  // into save[m] + slot*save_stride
+  int64_t nsteps, step0, save_every, save_stride;
+  // column pass: lines of length N with stride ld; a tile is CC consecutive x
+  // columns at outer index o (offset o*ostride) of trajectory b
+  int64_t ld, ostride, nouter;
+  int32_t col_fwd, col_inv;
+};
+
+// Launchers: return 0 or a cudaError_t value.  logn = log2 of the line length.
+int launch_row(int dtype, int M, int logn, const PassArgs& a, int64_t nlines, cudaStream_t s);
+int launch_col(int dtype, int M, int logn, const PassArgs& a, cudaStream_t s);
+int launch_line1d(int dtype, int M, int logn, const PassArgs& a, cudaStream_t s);
+int launch_nl_only(int dtype, int M, const PassArgs& a, cudaStream_t s);
+// FP64 reductions: out[m] += sum |u_m|^2 (device double array of M entries)
+int launch_norm(int dtype, int M, const PassArgs& a, double* out, cudaStream_t s);
+
+}  // namespace gpe

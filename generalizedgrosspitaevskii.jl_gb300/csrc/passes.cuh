@@ -1,0 +1,549 @@
+// passes.cuh -- the fused line passes of one Strang step.
+//
+// A reference step (src/strang_splitting.jl:86-90) is
+//   half(t+dt/2, dt/2) ; FFT ; * exp(-i dt D(k)) ; iFFT ; half(t+dt, dt/2)
+// with the real-space half step of src/kernels.jl:37-54.  Here a 2D step is two
+// passes over HBM, each reading and writing the field once:
+//   row pass    : [iFFT_x] [half A] [save] [half B] [FFT_x]   (lines along x)
+//   column pass : FFT_y  * table(k)  iFFT_y                    (tiles of CC columns)
+// Between steps the state stays x-transformed, so the trailing half of step k and
+// the leading half of step k+1 share one row pass.  In 1D a line is the whole
+// field, so one resident kernel runs many steps without touching HBM.
+#pragma once
+#include "fft.cuh"
+#include "kernels.h"
+#include "philox.cuh"
+
+namespace gpe {
+
+__host__ __device__ constexpr int cmin(int a, int b) { return a < b ? a : b; }
+__host__ __device__ constexpr int cmax(int a, int b) { return a > b ? a : b; }
+__host__ __device__ constexpr int pow2floor(int v) { return v <= 1 ? 1 : 2 * pow2floor(v / 2); }
+
+// Tiling of a line of 2^LOGN points for precision Real and M components.
+template <typename Real, int M, int LOGN>
+struct LineCfg {
+  using C = typename CT<Real>::T;
+  static constexpr int N = 1 << LOGN;
+  static constexpr int EMAX = (sizeof(Real) == 8 && M == 2) ? 8 : 16;  // points per thread
+  static constexpr int E = cmin(EMAX, N / 2);
+  static constexpr int T = N / E;  // threads per line
+  static constexpr int ROWT = 256;
+  static constexpr int L = T >= ROWT ? 1 : ROWT / T;  // lines per row-pass block
+  static constexpr int CCMAX = 128 / (int)sizeof(C);  // columns per tile: one 128-byte row
+  static constexpr int TPB = (M == 2) ? 512 : 1024;
+  static constexpr int SMEM_LIMIT = 200 * 1024;
+  static constexpr int CC = cmax(1, cmin(cmin(CCMAX, cmax(1, TPB / T)), pow2floor(SMEM_LIMIT / (N * (int)sizeof(C)))));
+  static constexpr int ROW_THREADS = L * T;
+  static constexpr int COL_THREADS = CC * T;
+  static constexpr size_t ROW_SMEM = (size_t)L * N * sizeof(C);
+  static constexpr size_t COL_SMEM = (size_t)CC * N * sizeof(C);
+};
+
+template <typename Real> __device__ __forceinline__ void sc(Real x, Real* s, Real* c);
+template <> __device__ __forceinline__ void sc<double>(double x, double* s, double* c) { sincos(x, s, c); }
+template <> __device__ __forceinline__ void sc<float>(float x, float* s, float* c) { sincosf(x, s, c); }
+__device__ __forceinline__ double rexp(double x) { return exp(x); }
+__device__ __forceinline__ float rexp(float x) { return expf(x); }
+
+// Typed views of the coefficient block.
+template <typename Real> struct Coef;
+template <> struct Coef<double> {
+  __device__ static __forceinline__ double g(const PassArgs& a, int j, int l, int r) { return a.g[j][l][r]; }
+  __device__ static __forceinline__ double c(const PassArgs& a, int j, int r) { return a.c[j][r]; }
+  __device__ static __forceinline__ double nf(const PassArgs& a, int j, int r) { return a.nfac[j][r]; }
+  __device__ static __forceinline__ double dth(const PassArgs& a) { return 0.5 * a.dt; }
+};
+template <> struct Coef<float> {
+  __device__ static __forceinline__ float g(const PassArgs& a, int j, int l, int r) { return a.gf[j][l][r]; }
+  __device__ static __forceinline__ float c(const PassArgs& a, int j, int r) { return a.cf[j][r]; }
+  __device__ static __forceinline__ float nf(const PassArgs& a, int j, int r) { return a.nfacf[j][r]; }
+  __device__ static __forceinline__ float dth(const PassArgs& a) { return a.dthf; }
+};
+
+// Pump coefficient (dt/4) * a(t_h) for half-step boundary h, formed in FP64.
+template <typename C>
+__device__ __forceinline__ C pump_coef(const PassArgs& a, int m, int64_t h) {
+  const int64_t n = a.pamp_n[m];
+  const double2 amp = a.pamp[m][n == 1 ? 0 : (h < n ? h : n - 1)];
+  const double f = 0.25 * a.dt;
+  return cmake<C>(f * amp.x, f * amp.y);
+}
+
+// Real-space half step h (delta = dt/2) at spatial point p of trajectory b, on the
+// M values u (src/kernels.jl:37-54):
+//   u <- cis(-delta G(u)) V (u + delta/2 F_now) + delta/2 F_next - i sqrt(delta) eta xi
+// G is evaluated on u before the pump is added (src/kernels.jl:40,44).
+// pn/px: pump coefficients (dt/4)a(t_h), (dt/4)a(t_{h+1}), hoisted by the caller.
+template <typename Real, int M>
+__device__ __forceinline__ void half_step(typename CT<Real>::T (&u)[M], const PassArgs& a,
+                                          int64_t p, int64_t b, int64_t h,
+                                          const typename CT<Real>::T (&pn)[M],
+                                          const typename CT<Real>::T (&px)[M]) {
+  using C = typename CT<Real>::T;
+  using K = Coef<Real>;
+  const Real dth = K::dth(a);
+  Real dens[M];
+#pragma unroll
+  for (int l = 0; l < M; ++l) dens[l] = u[l].x * u[l].x + u[l].y * u[l].y;
+  C E[M];
+  bool hasE[M];
+#pragma unroll
+  for (int j = 0; j < M; ++j) {
+    hasE[j] = a.nl_on[j] != 0;
+    if (hasE[j]) {
+      Real gr = K::c(a, j, 0), gi = K::c(a, j, 1);
+#pragma unroll
+      for (int l = 0; l < M; ++l) {
+        gr += K::g(a, j, l, 0) * dens[l];
+        gi += K::g(a, j, l, 1) * dens[l];
+      }
+      Real s, c;
+      sc<Real>(dth * gr, &s, &c);
+      const Real mag = (gi != (Real)0) ? rexp(dth * gi) : (Real)1;
+      E[j].x = mag * c;
+      E[j].y = -mag * s;
+    }
+  }
+  if (a.vkind == TAB_SCALAR) {
+    const C v = __ldg((const C*)a.vtab + p);
+#pragma unroll
+    for (int j = 0; j < M; ++j) { E[j] = hasE[j] ? cmul(E[j], v) : v; hasE[j] = true; }
+  } else if (a.vkind == TAB_DIAG) {
+#pragma unroll
+    for (int j = 0; j < M; ++j) {
+      const C v = __ldg((const C*)a.vtab + (int64_t)j * a.P + p);
+      E[j] = hasE[j] ? cmul(E[j], v) : v;
+      hasE[j] = true;
+    }
+  }
+  C prof[M];
+#pragma unroll
+  for (int j = 0; j < M; ++j) {
+    if (a.pprof[j]) {
+      if (a.pprof_cplx) prof[j] = __ldg((const C*)a.pprof[j] + p);
+      else { prof[j].x = __ldg((const Real*)a.pprof[j] + p); prof[j].y = (Real)0; }
+      u[j] = cadd(u[j], cmul(pn[j], prof[j]));
+    }
+  }
+  if (a.vkind == TAB_MATRIX && M == 2) {
+    // matrix potential with no nonlinearity: mat-vec with the per-point 2x2 table
+    const C* vt = (const C*)a.vtab;
+    const C t00 = __ldg(vt + p), t01 = __ldg(vt + a.P + p);
+    const C t10 = __ldg(vt + 2 * a.P + p), t11 = __ldg(vt + 3 * a.P + p);
+    const C y0 = cadd(cmul(t00, u[0]), cmul(t01, u[M - 1]));
+    const C y1 = cadd(cmul(t10, u[0]), cmul(t11, u[M - 1]));
+    u[0] = y0;
+    u[M - 1] = y1;
+  } else {
+#pragma unroll
+    for (int j = 0; j < M; ++j)
+      if (hasE[j]) u[j] = cmul(E[j], u[j]);
+  }
+#pragma unroll
+  for (int j = 0; j < M; ++j)
+    if (a.pprof[j]) u[j] = cadd(u[j], cmul(px[j], prof[j]));
+  if (a.noise != NOISE_OFF) {
+    C xi[M];
+    if (a.noise == NOISE_PHILOX) {
+      const uint4 r = Philox4x32::gen(noise_counter(p, b, h), a.seed_lo, a.seed_hi);
+      xi[0] = BoxMuller<Real>::get(r.x, r.y);
+      if constexpr (M == 2) xi[M - 1] = BoxMuller<Real>::get(r.z, r.w);
+    } else {
+      const C* xb = (const C*)a.xi;
+#pragma unroll
+      for (int j = 0; j < M; ++j) xi[j] = xb[((h - a.xi_h0) * M + j) * a.B * a.P + b * a.P + p];
+    }
+#pragma unroll
+    for (int j = 0; j < M; ++j) {
+      C nf;
+      nf.x = K::nf(a, j, 0);
+      nf.y = K::nf(a, j, 1);
+      if (a.etaprof[j]) nf = cscale(nf, __ldg((const Real*)a.etaprof[j] + p));
+      u[j] = cadd(u[j], cmul(nf, xi[j]));
+    }
+  }
+}
+
+template <typename Real, int M>
+__device__ __forceinline__ void load_pump(const PassArgs& a, int64_t h, typename CT<Real>::T (&pn)[M],
+                                          typename CT<Real>::T (&px)[M]) {
+  using C = typename CT<Real>::T;
+#pragma unroll
+  for (int j = 0; j < M; ++j) {
+    if (a.pprof[j] && h >= 0) {
+      pn[j] = pump_coef<C>(a, j, h);
+      px[j] = pump_coef<C>(a, j, h + 1);
+    } else {
+      pn[j] = cmake<C>(0.0, 0.0);
+      px[j] = pn[j];
+    }
+  }
+}
+
+// k-space multiply of the M values at table index kp (src/strang_splitting.jl:73-74)
+template <typename Real, int M>
+__device__ __forceinline__ void kmul(typename CT<Real>::T (&v)[M], const PassArgs& a, int64_t kp) {
+  using C = typename CT<Real>::T;
+  const C* kt = (const C*)a.ktab;
+  if (a.kkind == TAB_SCALAR) {
+    const C k = __ldg(kt + kp);
+#pragma unroll
+    for (int m = 0; m < M; ++m) v[m] = cmul(k, v[m]);
+  } else if (a.kkind == TAB_DIAG) {
+#pragma unroll
+    for (int m = 0; m < M; ++m) v[m] = cmul(__ldg(kt + (int64_t)m * a.P + kp), v[m]);
+  } else if (a.kkind == TAB_MATRIX) {
+    if constexpr (M == 2) {
+      const C t00 = __ldg(kt + kp), t01 = __ldg(kt + a.P + kp);
+      const C t10 = __ldg(kt + 2 * a.P + kp), t11 = __ldg(kt + 3 * a.P + kp);
+      const C y0 = cadd(cmul(t00, v[0]), cmul(t01, v[1]));
+      const C y1 = cadd(cmul(t10, v[0]), cmul(t11, v[1]));
+      v[0] = y0;
+      v[1] = y1;
+    } else {
+      v[0] = cmul(__ldg(kt + kp), v[0]);
+    }
+  }
+}
+
+// ------------------------------------------------------------------ row pass
+template <typename Real, int LOGN, int M>
+__global__ void __launch_bounds__(LineCfg<Real, M, LOGN>::ROW_THREADS)
+row_kernel(const PassArgs a, const int64_t nlines) {
+  using Cfg = LineCfg<Real, M, LOGN>;
+  using C = typename CT<Real>::T;
+  constexpr int N = Cfg::N, E = Cfg::E, T = Cfg::T, L = Cfg::L;
+  extern __shared__ __align__(16) unsigned char smraw[];
+  C* sm = reinterpret_cast<C*>(smraw);
+  const int t = threadIdx.x % T, l = threadIdx.x / T;
+  int64_t line = (int64_t)blockIdx.x * L + l;
+  const bool active = line < nlines;
+  if (!active) line = nlines - 1;  // idle lines of the last block compute a copy, store nothing
+  const RowLayout<C> lay{sm + l * N};
+  const C* tw = (const C*)a.tw;
+  const int64_t lpb = a.P / N;
+  const int64_t b = line / lpb;
+  const int64_t p0 = (line - b * lpb) * N + t;
+  const int64_t g0 = b * a.P + p0;
+  C x[M][E];
+#pragma unroll
+  for (int m = 0; m < M; ++m)
+#pragma unroll
+    for (int i = 0; i < E; ++i) x[m][i] = ((const C*)a.u[m])[g0 + T * i];
+  if (a.do_ifft) {
+#pragma unroll
+    for (int m = 0; m < M; ++m) fft_line<C, N, E, +1>(x[m], t, lay, tw);
+  }
+  if (a.hA >= 0 || a.hB >= 0 || a.save[0]) {
+    C pnA[M], pxA[M], pnB[M], pxB[M];
+    load_pump<Real, M>(a, a.hA, pnA, pxA);
+    load_pump<Real, M>(a, a.hB, pnB, pxB);
+#pragma unroll
+    for (int i = 0; i < E; ++i) {
+      C v[M];
+#pragma unroll
+      for (int m = 0; m < M; ++m) v[m] = x[m][i];
+      const int64_t p = p0 + T * i;
+      if (a.hA >= 0) half_step<Real, M>(v, a, p, b, a.hA, pnA, pxA);
+      if (a.save[0] && active) {
+#pragma unroll
+        for (int m = 0; m < M; ++m) ((C*)a.save[m])[g0 + T * i] = v[m];
+      }
+      if (a.hB >= 0) half_step<Real, M>(v, a, p, b, a.hB, pnB, pxB);
+#pragma unroll
+      for (int m = 0; m < M; ++m) x[m][i] = v[m];
+    }
+  }
+  if (a.do_fft) {
+#pragma unroll
+    for (int m = 0; m < M; ++m) fft_line<C, N, E, -1>(x[m], t, lay, tw);
+  }
+  if (active) {
+#pragma unroll
+    for (int m = 0; m < M; ++m)
+#pragma unroll
+      for (int i = 0; i < E; ++i) ((C*)a.u[m])[g0 + T * i] = x[m][i];
+  }
+}
+
+// ------------------------------------------------------------------ column pass
+template <typename Real, int LOGN, int M>
+__global__ void __launch_bounds__(LineCfg<Real, M, LOGN>::COL_THREADS)
+col_kernel(const PassArgs a) {
+  using Cfg = LineCfg<Real, M, LOGN>;
+  using C = typename CT<Real>::T;
+  constexpr int N = Cfg::N, E = Cfg::E, T = Cfg::T, CC = Cfg::CC;
+  extern __shared__ __align__(16) unsigned char smraw[];
+  C* sm = reinterpret_cast<C*>(smraw);
+  const int c = threadIdx.x % CC, t = threadIdx.x / CC;
+  int64_t tile = blockIdx.x;
+  const int64_t ntx = a.n0 / CC;
+  const int64_t xt = tile % ntx;
+  tile /= ntx;
+  const int64_t o = tile % a.nouter;
+  const int64_t b = tile / a.nouter;
+  const int64_t sp0 = o * a.ostride + xt * CC + c + (int64_t)t * a.ld;
+  const int64_t g0 = b * a.P + sp0;
+  const int64_t step = (int64_t)T * a.ld;
+  const ColLayout<C, CC> lay{sm + c};
+  const C* tw = (const C*)a.tw;
+  C x[M][E];
+#pragma unroll
+  for (int m = 0; m < M; ++m)
+#pragma unroll
+    for (int i = 0; i < E; ++i) x[m][i] = ((const C*)a.u[m])[g0 + step * i];
+  if (a.col_fwd) {
+#pragma unroll
+    for (int m = 0; m < M; ++m) fft_line<C, N, E, -1>(x[m], t, lay, tw);
+  }
+  if (a.ktab) {
+#pragma unroll
+    for (int i = 0; i < E; ++i) {
+      C v[M];
+#pragma unroll
+      for (int m = 0; m < M; ++m) v[m] = x[m][i];
+      kmul<Real, M>(v, a, sp0 + step * i);
+#pragma unroll
+      for (int m = 0; m < M; ++m) x[m][i] = v[m];
+    }
+  }
+  if (a.col_inv) {
+#pragma unroll
+    for (int m = 0; m < M; ++m) fft_line<C, N, E, +1>(x[m], t, lay, tw);
+  }
+#pragma unroll
+  for (int m = 0; m < M; ++m)
+#pragma unroll
+    for (int i = 0; i < E; ++i) ((C*)a.u[m])[g0 + step * i] = x[m][i];
+}
+
+// ------------------------------------------------------------------ 1D resident
+// nlines = B trajectories of one line each; runs a.nsteps full steps in registers.
+template <typename Real, int LOGN, int M>
+__global__ void __launch_bounds__(LineCfg<Real, M, LOGN>::ROW_THREADS)
+line1d_kernel(const PassArgs a, const int64_t nlines) {
+  using Cfg = LineCfg<Real, M, LOGN>;
+  using C = typename CT<Real>::T;
+  constexpr int N = Cfg::N, E = Cfg::E, T = Cfg::T, L = Cfg::L;
+  extern __shared__ __align__(16) unsigned char smraw[];
+  C* sm = reinterpret_cast<C*>(smraw);
+  const int t = threadIdx.x % T, l = threadIdx.x / T;
+  int64_t line = (int64_t)blockIdx.x * L + l;
+  const bool active = line < nlines;
+  if (!active) line = nlines - 1;
+  const RowLayout<C> lay{sm + l * N};
+  const C* tw = (const C*)a.tw;
+  const int64_t b = line;
+  const int64_t g0 = b * a.P + t;
+  C x[M][E];
+#pragma unroll
+  for (int m = 0; m < M; ++m)
+#pragma unroll
+    for (int i = 0; i < E; ++i) x[m][i] = ((const C*)a.u[m])[g0 + T * i];
+  for (int64_t s = 0; s < a.nsteps; ++s) {
+    const int64_t k = a.step0 + s;
+    C pn[M], px[M];
+    load_pump<Real, M>(a, 2 * k, pn, px);
+#pragma unroll
+    for (int i = 0; i < E; ++i) {
+      C v[M];
+#pragma unroll
+      for (int m = 0; m < M; ++m) v[m] = x[m][i];
+      half_step<Real, M>(v, a, t + T * i, b, 2 * k, pn, px);
+#pragma unroll
+      for (int m = 0; m < M; ++m) x[m][i] = v[m];
+    }
+    if (a.ktab) {
+#pragma unroll
+      for (int m = 0; m < M; ++m) fft_line<C, N, E, -1>(x[m], t, lay, tw);
+#pragma unroll
+      for (int i = 0; i < E; ++i) {
+        C v[M];
+#pragma unroll
+        for (int m = 0; m < M; ++m) v[m] = x[m][i];
+        kmul<Real, M>(v, a, t + T * i);
+#pragma unroll
+        for (int m = 0; m < M; ++m) x[m][i] = v[m];
+      }
+#pragma unroll
+      for (int m = 0; m < M; ++m) fft_line<C, N, E, +1>(x[m], t, lay, tw);
+    }
+    load_pump<Real, M>(a, 2 * k + 1, pn, px);
+#pragma unroll
+    for (int i = 0; i < E; ++i) {
+      C v[M];
+#pragma unroll
+      for (int m = 0; m < M; ++m) v[m] = x[m][i];
+      half_step<Real, M>(v, a, t + T * i, b, 2 * k + 1, pn, px);
+#pragma unroll
+      for (int m = 0; m < M; ++m) x[m][i] = v[m];
+    }
+    if (a.save_every > 0 && ((s + 1) % a.save_every) == 0 && active) {
+      const int64_t slot = (s + 1) / a.save_every - 1;
+#pragma unroll
+      for (int m = 0; m < M; ++m)
+#pragma unroll
+        for (int i = 0; i < E; ++i) ((C*)a.save[m])[slot * a.save_stride + g0 + T * i] = x[m][i];
+    }
+  }
+  if (active) {
+#pragma unroll
+    for (int m = 0; m < M; ++m)
+#pragma unroll
+      for (int i = 0; i < E; ++i) ((C*)a.u[m])[g0 + T * i] = x[m][i];
+  }
+}
+
+// ------------------------------------------------------------------ no dispersion
+// Without a dispersion the step is pointwise: one thread per point runs all steps.
+template <typename Real, int M>
+__global__ void __launch_bounds__(256) nl_only_kernel(const PassArgs a) {
+  using C = typename CT<Real>::T;
+  const int64_t total = a.P * a.B;
+  for (int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; q < total; q += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t b = q / a.P, p = q - b * a.P;
+    C v[M];
+#pragma unroll
+    for (int m = 0; m < M; ++m) v[m] = ((const C*)a.u[m])[q];
+    for (int64_t s = 0; s < a.nsteps; ++s) {
+      const int64_t k = a.step0 + s;
+      C pn[M], px[M];
+      load_pump<Real, M>(a, 2 * k, pn, px);
+      half_step<Real, M>(v, a, p, b, 2 * k, pn, px);
+      load_pump<Real, M>(a, 2 * k + 1, pn, px);
+      half_step<Real, M>(v, a, p, b, 2 * k + 1, pn, px);
+      if (a.save_every > 0 && ((s + 1) % a.save_every) == 0) {
+        const int64_t slot = (s + 1) / a.save_every - 1;
+#pragma unroll
+        for (int m = 0; m < M; ++m) ((C*)a.save[m])[slot * a.save_stride + q] = v[m];
+      }
+    }
+#pragma unroll
+    for (int m = 0; m < M; ++m) ((C*)a.u[m])[q] = v[m];
+  }
+}
+
+// ------------------------------------------------------------------ FP64 norm
+template <typename Real, int M>
+__global__ void __launch_bounds__(256) norm_kernel(const PassArgs a, double* out) {
+  using C = typename CT<Real>::T;
+  __shared__ double red[M][8];
+  const int64_t total = a.P * a.B;
+  double acc[M];
+#pragma unroll
+  for (int m = 0; m < M; ++m) acc[m] = 0.0;
+  for (int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; q < total; q += (int64_t)gridDim.x * blockDim.x) {
+#pragma unroll
+    for (int m = 0; m < M; ++m) {
+      const C v = ((const C*)a.u[m])[q];
+      acc[m] += (double)v.x * (double)v.x + (double)v.y * (double)v.y;
+    }
+  }
+#pragma unroll
+  for (int m = 0; m < M; ++m) {
+    double v = acc[m];
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    if ((threadIdx.x & 31) == 0) red[m][threadIdx.x >> 5] = v;
+  }
+  __syncthreads();
+  if (threadIdx.x < 32) {
+#pragma unroll
+    for (int m = 0; m < M; ++m) {
+      double v = (threadIdx.x < (blockDim.x >> 5)) ? red[m][threadIdx.x] : 0.0;
+      for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+      if (threadIdx.x == 0) atomicAdd(out + m, v);
+    }
+  }
+}
+
+// ------------------------------------------------------------------ launchers
+template <typename K>
+static inline int set_smem(K k, size_t bytes) {
+  if (bytes > 48 * 1024) return (int)cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+  return 0;
+}
+
+template <typename Real, int M, int LOGN>
+int launch_row_n(const PassArgs& a, int64_t nlines, cudaStream_t s) {
+  using Cfg = LineCfg<Real, M, LOGN>;
+  auto k = row_kernel<Real, LOGN, M>;
+  int e = set_smem(k, Cfg::ROW_SMEM);
+  if (e) return e;
+  const int64_t blocks = (nlines + Cfg::L - 1) / Cfg::L;
+  k<<<(unsigned)blocks, Cfg::ROW_THREADS, Cfg::ROW_SMEM, s>>>(a, nlines);
+  return (int)cudaGetLastError();
+}
+template <typename Real, int M, int LOGN>
+int launch_col_n(const PassArgs& a, cudaStream_t s) {
+  using Cfg = LineCfg<Real, M, LOGN>;
+  if (a.n0 % Cfg::CC) return (int)cudaErrorInvalidValue;
+  auto k = col_kernel<Real, LOGN, M>;
+  int e = set_smem(k, Cfg::COL_SMEM);
+  if (e) return e;
+  const int64_t blocks = (int64_t)(a.n0 / Cfg::CC) * a.nouter * a.B;
+  k<<<(unsigned)blocks, Cfg::COL_THREADS, Cfg::COL_SMEM, s>>>(a);
+  return (int)cudaGetLastError();
+}
+template <typename Real, int M, int LOGN>
+int launch_line1d_n(const PassArgs& a, cudaStream_t s) {
+  using Cfg = LineCfg<Real, M, LOGN>;
+  auto k = line1d_kernel<Real, LOGN, M>;
+  int e = set_smem(k, Cfg::ROW_SMEM);
+  if (e) return e;
+  const int64_t blocks = (a.B + Cfg::L - 1) / Cfg::L;
+  k<<<(unsigned)blocks, Cfg::ROW_THREADS, Cfg::ROW_SMEM, s>>>(a, a.B);
+  return (int)cudaGetLastError();
+}
+
+#define GPE_LOGN_SWITCH(FN, ...)                \
+  switch (logn) {                               \
+    case 4: return FN<Real, M, 4>(__VA_ARGS__);   \
+    case 5: return FN<Real, M, 5>(__VA_ARGS__);   \
+    case 6: return FN<Real, M, 6>(__VA_ARGS__);   \
+    case 7: return FN<Real, M, 7>(__VA_ARGS__);   \
+    case 8: return FN<Real, M, 8>(__VA_ARGS__);   \
+    case 9: return FN<Real, M, 9>(__VA_ARGS__);   \
+    case 10: return FN<Real, M, 10>(__VA_ARGS__); \
+    case 11: return FN<Real, M, 11>(__VA_ARGS__); \
+    case 12: return FN<Real, M, 12>(__VA_ARGS__); \
+    default: return (int)cudaErrorInvalidValue;   \
+  }
+
+template <typename Real, int M>
+int launch_row_t(int logn, const PassArgs& a, int64_t nlines, cudaStream_t s) {
+  GPE_LOGN_SWITCH(launch_row_n, a, nlines, s)
+}
+template <typename Real, int M>
+int launch_col_t(int logn, const PassArgs& a, cudaStream_t s) {
+  GPE_LOGN_SWITCH(launch_col_n, a, s)
+}
+template <typename Real, int M>
+int launch_line1d_t(int logn, const PassArgs& a, cudaStream_t s) {
+  GPE_LOGN_SWITCH(launch_line1d_n, a, s)
+}
+template <typename Real, int M>
+int launch_nl_only_t(const PassArgs& a, cudaStream_t s) {
+  const int64_t total = a.P * a.B;
+  int64_t blocks = (total + 255) / 256;
+  if (blocks > 152 * 64) blocks = 152 * 64;
+  nl_only_kernel<Real, M><<<(unsigned)blocks, 256, 0, s>>>(a);
+  return (int)cudaGetLastError();
+}
+template <typename Real, int M>
+int launch_norm_t(const PassArgs& a, double* out, cudaStream_t s) {
+  const int64_t total = a.P * a.B;
+  int64_t blocks = (total + 255) / 256;
+  if (blocks > 152 * 8) blocks = 152 * 8;
+  norm_kernel<Real, M><<<(unsigned)blocks, 256, 0, s>>>(a, out);
+  return (int)cudaGetLastError();
+}
+
+#define GPE_INSTANTIATE(REAL, MM)                                                            \
+  template int launch_row_t<REAL, MM>(int, const PassArgs&, int64_t, cudaStream_t);         \
+  template int launch_col_t<REAL, MM>(int, const PassArgs&, cudaStream_t);                  \
+  template int launch_line1d_t<REAL, MM>(int, const PassArgs&, cudaStream_t);               \
+  template int launch_nl_only_t<REAL, MM>(const PassArgs&, cudaStream_t);                   \
+  template int launch_norm_t<REAL, MM>(const PassArgs&, double*, cudaStream_t);
+
+}  // namespace gpe

@@ -1,0 +1,184 @@
+/*
+ * gpe.h -- C ABI of libgpe, the GB300 (sm_103a) StrangSplitting backend for
+ * GeneralizedGrossPitaevskii.jl.
+ *
+ * The library advances
+ *     i du = [D(-i grad) u + V(r) u + G(u) u + i F(r,t)] dt + eta dW
+ * on a periodic uniform grid with the reference's Strang splitting
+ * (src/strang_splitting.jl:86-90, src/kernels.jl:37-54).  It is the compute
+ * backend for the reference's
+ *     solve(prob, StrangSplitting(), tspan; dt, nsaves, save_start)
+ * (src/fixed_time_stepping.jl:56-81): the host side (a Julia shim, or the Python
+ * mirror shipped with this library) resolves dt (src/fixed_time_stepping.jl:14-24),
+ * samples the user closures on the grids and passes the results here as plain
+ * FP64 arrays.
+ *
+ * Conventions
+ *  - Axis 0 is x and is the fastest varying (Julia column-major order): a field is
+ *    stored as C array [batch][z][y][x] of interleaved (re, im) complex numbers.
+ *    Components are separate arrays (the reference's tuple of arrays).
+ *  - Field precision is GPE_C128 (FP64) or GPE_C64 (FP32).  Every table, time and
+ *    coefficient crosses this ABI in FP64.
+ *  - Every call returns 0 on success or a negative GPE_ERR_* code; gpe_last_error()
+ *    gives a readable message.  No C++ exception crosses the ABI.
+ *  - One handle owns one CUDA stream and its device buffers; a handle is not
+ *    thread safe, distinct handles may be used concurrently.  Calls are synchronous
+ *    unless stated otherwise.
+ */
+#ifndef GPE_H
+#define GPE_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define GPE_ABI_VERSION 1
+
+/* status codes */
+#define GPE_OK 0
+#define GPE_ERR_INVALID (-1)     /* bad argument, shape or state */
+#define GPE_ERR_UNSUPPORTED (-2) /* closure family / size this backend does not do */
+#define GPE_ERR_CUDA (-3)        /* a CUDA runtime call failed */
+#define GPE_ERR_NONFINITE (-4)   /* NaN/Inf found in an input or the state */
+#define GPE_ERR_TIMEOUT (-5)     /* a bounded device wait expired */
+#define GPE_ERR_NOMEM (-6)       /* device allocation failed */
+
+/* field precision */
+#define GPE_C128 0 /* ComplexF64 fields, FP64 arithmetic */
+#define GPE_C64 1  /* ComplexF32 fields, FP32 arithmetic, FP64 tables/time built on host */
+
+/* table kinds: what the user closure returned per grid point */
+#define GPE_TABLE_NONE 0
+#define GPE_TABLE_SCALAR 1 /* one complex number per point, same for every component */
+#define GPE_TABLE_DIAG 2   /* M complex numbers per point (SVector) */
+#define GPE_TABLE_MATRIX 3 /* M x M complex matrix per point (SMatrix), row-major a*M+b */
+
+/* noise modes */
+#define GPE_NOISE_OFF 0
+#define GPE_NOISE_PHILOX 1 /* in-kernel Philox4x32-10 + Box-Muller, E|xi|^2 = 1 */
+#define GPE_NOISE_REPLAY 2 /* xi supplied by the host for every half step */
+
+typedef struct gpe_handle gpe_handle;
+
+typedef struct gpe_desc {
+  int32_t abi_version; /* GPE_ABI_VERSION */
+  int32_t ndim;        /* spatial dimensions: 1, 2 or 3 */
+  int64_t n[3];        /* grid points per axis, n[0] = x; unused axes = 1 */
+  double lengths[3];   /* domain size per axis (x in [0, L)) */
+  int64_t batch;       /* trailing (trajectory) dims flattened, >= 1 */
+  int32_t ncomp;       /* components M: 1 or 2 */
+  int32_t dtype;       /* GPE_C128 or GPE_C64 */
+  double dt;           /* the resolved step (src/fixed_time_stepping.jl:19-21) */
+  double t0;           /* tspan[1] */
+  int32_t device;      /* CUDA device ordinal; -1 = the calling thread's current device */
+  int32_t flags;       /* reserved, 0 */
+} gpe_desc;
+
+/* Solver state apart from the fields: enough to resume bit-identically. */
+typedef struct gpe_state {
+  double t;          /* time accumulated with t += dt (src/fixed_time_stepping.jl:44) */
+  int64_t steps;     /* full steps taken since t0 */
+  uint64_t seed;     /* Philox key */
+  int32_t noise_mode;
+  int32_t reserved;
+} gpe_state;
+
+/* ---- lifetime ------------------------------------------------------------ */
+/* Replaces init(prob, StrangSplitting(), tspan; dt, ...) (src/strang_splitting.jl:32-67):
+ * allocates the device state for the grid, batch and precision in *desc. */
+int gpe_create(const gpe_desc* desc, gpe_handle** out);
+int gpe_destroy(gpe_handle* h);
+/* Message for the last failed call on h (or the last gpe_create failure if h is NULL). */
+const char* gpe_last_error(const gpe_handle* h);
+/* Version / build information string. */
+const char* gpe_version(void);
+
+/* ---- fields -------------------------------------------------------------- */
+/* Upload component comp (u0[comp], src/strang_splitting.jl:48) from host memory:
+ * batch*P complex numbers of the handle's precision, layout [batch][z][y][x]. */
+int gpe_set_field(gpe_handle* h, int comp, const void* host);
+int gpe_get_field(gpe_handle* h, int comp, void* host);
+/* Same with device pointers the caller owns (e.g. a torch tensor's data_ptr()). */
+int gpe_set_field_dev(gpe_handle* h, int comp, const void* dev);
+int gpe_get_field_dev(gpe_handle* h, int comp, void* dev);
+
+/* ---- linear operators ---------------------------------------------------- */
+/* Dispersion samples D(k) on reciprocal_grid (src/problem.jl:135-139), FP64 complex
+ * interleaved, spatial points only: kind SCALAR -> P, DIAG -> M*P ([m][p]),
+ * MATRIX -> M*M*P ([a*M+b][p]).  The library forms exp(-i dt D) on the host in FP64
+ * (src/misc.jl:12-20; closed-form 2x2 exponential for MATRIX). */
+int gpe_set_dispersion(gpe_handle* h, const double* D, int kind);
+/* The finished table exp(-i dt D(k)) instead of D (same layouts), e.g. built by the
+ * caller with the reference's own get_exponential. */
+int gpe_set_ktable(gpe_handle* h, const double* table, int kind);
+/* Potential samples V(r) on direct_grid; the library forms exp(-i dt/2 V)
+ * (src/strang_splitting.jl:54).  MATRIX potentials need a MATRIX nonlinearity or none. */
+int gpe_set_potential(gpe_handle* h, const double* V, int kind);
+int gpe_set_vtable(gpe_handle* h, const double* table, int kind);
+
+/* ---- local terms --------------------------------------------------------- */
+/* Diagonal nonlinearity family G_j(u) = sum_l g[j*M+l] |u_l|^2 + c[j] with complex
+ * (interleaved) g (M*M) and c (M); c may be NULL.  Covers every nonlinearity of the
+ * reference's tests and examples (e.g. test/kerr_propagation.jl:24,
+ * examples/exciton_polariton.jl:50). */
+int gpe_set_nonlinearity(gpe_handle* h, const double* g, const double* c);
+/* Separable pump F_comp(r, t) = a(t) * p(r).  profile: P real FP64 values (or P
+ * interleaved complex when profile_complex != 0); amp: n_amp complex FP64 values of
+ * a(t) at the reference's pump sampling times: amp[0] = a(t0), amp[2k+1] =
+ * a(t_k + dt/2), amp[2k+2] = a(t_k + dt), t_k = end time of step k accumulated with
+ * t += dt (src/strang_splitting.jl:56-58,78-84, src/misc.jl:39-42).  n_amp == 1 means a
+ * constant amplitude.  profile == NULL removes the pump of that component. */
+int gpe_set_pump(gpe_handle* h, int comp, const double* profile, int profile_complex,
+                 const double* amp, int64_t n_amp);
+/* Position noise -i sqrt(dt/2) eta_m xi_m added after every real-space half step
+ * (src/kernels.jl:42,49).  eta: M complex amplitudes; eta_profile: NULL or M*P real
+ * factors ([m][p]).  mode GPE_NOISE_PHILOX draws xi in-kernel from (seed, half step,
+ * component, point, trajectory); GPE_NOISE_REPLAY takes xi from gpe_run_replay. */
+int gpe_set_noise(gpe_handle* h, int mode, uint64_t seed, const double* eta,
+                  const double* eta_profile);
+
+/* ---- stepping ------------------------------------------------------------ */
+/* Advance nsteps full Strang steps (src/fixed_time_stepping.jl:38-50).  After every
+ * save_every steps (0 = never) the state is stored into out_host as save slot s:
+ * component m, slot s is at out_host + (m*nsaves + s) * batch*P complex numbers, with
+ * nsaves = nsteps / save_every; ts_out[s] (may be NULL) receives the accumulated time.
+ * out_host may be NULL when save_every == 0. */
+int gpe_run(gpe_handle* h, int64_t nsteps, int64_t save_every, void* out_host,
+            double* ts_out);
+/* As gpe_run with out_dev a device buffer of the same layout the caller owns. */
+int gpe_run_dev(gpe_handle* h, int64_t nsteps, int64_t save_every, void* out_dev,
+                double* ts_out);
+/* As gpe_run in GPE_NOISE_REPLAY mode: xi_host holds 2*nsteps half steps of
+ * M*batch*P complex numbers (handle precision), layout [half][m][batch][p]. */
+int gpe_run_replay(gpe_handle* h, int64_t nsteps, int64_t save_every, const void* xi_host,
+                   void* out_host, double* ts_out);
+
+/* ---- checkpoint / diagnostics ------------------------------------------- */
+int gpe_get_state(gpe_handle* h, gpe_state* st);
+int gpe_set_state(gpe_handle* h, const gpe_state* st);
+/* out[m] = sum over batch and grid of |u_m|^2 dV, accumulated in FP64 on the device. */
+int gpe_norm(gpe_handle* h, double* out);
+/* out[0] = kinetic sum_k u~^H D(k) u~ dV/P (real part; needs gpe_set_dispersion),
+ * out[1] = interaction sum_r sum_j (1/2) Re(g_jl) |u_j|^2 |u_l|^2 dV,
+ * out[2] = potential sum_r u^H V u dV (needs gpe_set_potential), FP64. */
+int gpe_energy(gpe_handle* h, double* out);
+
+/* Per-launch timing for benchmarks: when on, gpe_run* brackets every kernel launch
+ * with CUDA events on the handle's stream.  gpe_kernel_times then gives, for the last
+ * run, ms[k] = summed device time and n[k] = launches of kernel kind k:
+ * 0 = row pass (x lines), 1 = column pass (y lines), 2 = resident 1D / pointwise. */
+int gpe_set_timing(gpe_handle* h, int on);
+int gpe_kernel_times(const gpe_handle* h, double* ms, int64_t* n);
+
+/* Wall time of the device work of the last gpe_run* call, in milliseconds. */
+double gpe_last_run_ms(const gpe_handle* h);
+/* Number of kernels launched by the last gpe_run* call. */
+int64_t gpe_last_run_launches(const gpe_handle* h);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* GPE_H */
