@@ -25,23 +25,42 @@ template <typename Real, int M, int LOGN>
 struct LineCfg {
   using C = typename CT<Real>::T;
   static constexpr int N = 1 << LOGN;
-  static constexpr int EMAX = (sizeof(Real) == 8 && M == 2) ? 8 : 16;  // points per thread
+  // points per thread: column pass (E) and row pass (ER, which also carries the
+  // pointwise half steps and so keeps fewer points live)
+  static constexpr int EMAX = (sizeof(Real) == 8 && M == 2) ? 8 : 16;
   static constexpr int E = cmin(EMAX, N / 2);
-  static constexpr int T = N / E;  // threads per line
+  static constexpr int T = N / E;  // threads per line, column pass
+  static constexpr int ERMAX = (M == 2) ? 8 : 16;
+  static constexpr int ER = cmin(ERMAX, N / 2);
+  static constexpr int TR = N / ER;  // threads per line, row pass
   static constexpr int ROWT = 256;
-  static constexpr int L = T >= ROWT ? 1 : ROWT / T;  // lines per row-pass block
+  static constexpr int L = TR >= ROWT ? 1 : ROWT / TR;  // lines per row-pass block
   static constexpr int CCMAX = 128 / (int)sizeof(C);  // columns per tile: one 128-byte row
   static constexpr int TPB = (M == 2) ? 512 : 1024;
   static constexpr int SMEM_LIMIT = 200 * 1024;
   static constexpr int CC = cmax(1, cmin(cmin(CCMAX, cmax(1, TPB / T)), pow2floor(SMEM_LIMIT / (N * (int)sizeof(C)))));
-  static constexpr int ROW_THREADS = L * T;
+  static constexpr int ROW_THREADS = L * TR;
   static constexpr int COL_THREADS = CC * T;
   static constexpr size_t ROW_SMEM = (size_t)L * N * sizeof(C);
   static constexpr size_t COL_SMEM = (size_t)CC * N * sizeof(C);
 };
 
 template <typename Real> __device__ __forceinline__ void sc(Real x, Real* s, Real* c);
-template <> __device__ __forceinline__ void sc<double>(double x, double* s, double* c) { sincos(x, s, c); }
+// FP64 sin/cos of the nonlinear phase.  FP64 runs at 1/64 of the FP32 rate on GB300, so
+// small angles (the usual case: |dt/2 * G| << 1) use the Taylor series of sin and cos
+// to x^13 / x^12 (truncation error below x^14/14! < 3e-24 for |x| <= 1/8), about a
+// third of the cost of the general routine, which handles the rest.
+template <> __device__ __forceinline__ void sc<double>(double x, double* s, double* c) {
+  if (fabs(x) <= 0.125) {
+    const double x2 = x * x;
+    *c = 1.0 + x2 * (-1.0 / 2 + x2 * (1.0 / 24 + x2 * (-1.0 / 720 + x2 * (1.0 / 40320 + x2 * (-1.0 / 3628800 +
+         x2 * (1.0 / 479001600))))));
+    *s = x * (1.0 + x2 * (-1.0 / 6 + x2 * (1.0 / 120 + x2 * (-1.0 / 5040 + x2 * (1.0 / 362880 + x2 * (-1.0 / 39916800 +
+         x2 * (1.0 / 6227020800.0)))))));
+  } else {
+    sincos(x, s, c);
+  }
+}
 template <> __device__ __forceinline__ void sc<float>(float x, float* s, float* c) { sincosf(x, s, c); }
 __device__ __forceinline__ double rexp(double x) { return exp(x); }
 __device__ __forceinline__ float rexp(float x) { return expf(x); }
@@ -213,7 +232,7 @@ __global__ void __launch_bounds__(LineCfg<Real, M, LOGN>::ROW_THREADS)
 row_kernel(const PassArgs a, const int64_t nlines) {
   using Cfg = LineCfg<Real, M, LOGN>;
   using C = typename CT<Real>::T;
-  constexpr int N = Cfg::N, E = Cfg::E, T = Cfg::T, L = Cfg::L;
+  constexpr int N = Cfg::N, E = Cfg::ER, T = Cfg::TR, L = Cfg::L;
   extern __shared__ __align__(16) unsigned char smraw[];
   C* sm = reinterpret_cast<C*>(smraw);
   const int t = threadIdx.x % T, l = threadIdx.x / T;
@@ -235,24 +254,31 @@ row_kernel(const PassArgs a, const int64_t nlines) {
 #pragma unroll
     for (int m = 0; m < M; ++m) fft_line<C, N, E, +1>(x[m], t, lay, tw);
   }
-  if (a.hA >= 0 || a.hB >= 0 || a.save[0]) {
-    C pnA[M], pxA[M], pnB[M], pxB[M];
-    load_pump<Real, M>(a, a.hA, pnA, pxA);
-    load_pump<Real, M>(a, a.hB, pnB, pxB);
+  // Both half steps run through ONE instance of half_step (a two-trip loop that is
+  // not unrolled): a half step then rounds identically whether it opens a run (entry
+  // pass) or sits between two steps, so a checkpointed and resumed run reproduces
+  // an uninterrupted one bit for bit.
+#pragma unroll 1
+  for (int half = 0; half < 2; ++half) {
+    const int64_t h = half ? a.hB : a.hA;
+    if (h >= 0) {
+      C pn[M], px[M];
+      load_pump<Real, M>(a, h, pn, px);
 #pragma unroll
-    for (int i = 0; i < E; ++i) {
-      C v[M];
+      for (int i = 0; i < E; ++i) {
+        C v[M];
 #pragma unroll
-      for (int m = 0; m < M; ++m) v[m] = x[m][i];
-      const int64_t p = p0 + T * i;
-      if (a.hA >= 0) half_step<Real, M>(v, a, p, b, a.hA, pnA, pxA);
-      if (a.save[0] && active) {
+        for (int m = 0; m < M; ++m) v[m] = x[m][i];
+        half_step<Real, M>(v, a, p0 + T * i, b, h, pn, px);
 #pragma unroll
-        for (int m = 0; m < M; ++m) ((C*)a.save[m])[g0 + T * i] = v[m];
+        for (int m = 0; m < M; ++m) x[m][i] = v[m];
       }
-      if (a.hB >= 0) half_step<Real, M>(v, a, p, b, a.hB, pnB, pxB);
+    }
+    if (half == 0 && a.save[0] && active) {
 #pragma unroll
-      for (int m = 0; m < M; ++m) x[m][i] = v[m];
+      for (int m = 0; m < M; ++m)
+#pragma unroll
+        for (int i = 0; i < E; ++i) ((C*)a.save[m])[g0 + T * i] = x[m][i];
     }
   }
   if (a.do_fft) {
@@ -325,7 +351,7 @@ __global__ void __launch_bounds__(LineCfg<Real, M, LOGN>::ROW_THREADS)
 line1d_kernel(const PassArgs a, const int64_t nlines) {
   using Cfg = LineCfg<Real, M, LOGN>;
   using C = typename CT<Real>::T;
-  constexpr int N = Cfg::N, E = Cfg::E, T = Cfg::T, L = Cfg::L;
+  constexpr int N = Cfg::N, E = Cfg::ER, T = Cfg::TR, L = Cfg::L;
   extern __shared__ __align__(16) unsigned char smraw[];
   C* sm = reinterpret_cast<C*>(smraw);
   const int t = threadIdx.x % T, l = threadIdx.x / T;

@@ -504,3 +504,34 @@ class PhiloxNoise:
         bm = box_muller_f32 if self.fp32 else box_muller_f64
         xs = [bm(w[0], w[1]), bm(w[2], w[3])][: self.M]
         return np.stack(xs).astype(np.complex128).reshape((self.M,) + self.batch_shape + self.spatial)
+
+
+class Fp32Iterator(OracleIterator):
+    """The reference's arithmetic for ComplexF32 fields: FFTs in single precision,
+    FP64 tables (dt is FP64, src/misc.jl:16) multiplied into the FP32 field with the
+    product rounded back to FP32 when stored (src/kernels.jl:51-53).  Used to bound
+    what an FP32 implementation can reach on a given problem."""
+
+    def __init__(self, *a, **k):
+        super().__init__(*a, **k)
+        self.u = self.u.astype(np.complex64)
+
+    def _diffusion_step(self):
+        import scipy.fft as sfft
+        if self.exp_D is None:
+            return
+        ft = sfft.fftn(self.u.astype(np.complex64), axes=self.fft_axes)
+        ft = self._apply(self.exp_D, self.ekind, ft.astype(np.complex128)).astype(np.complex64)
+        self.u = sfft.ifftn(ft, axes=self.fft_axes).astype(np.complex64)
+
+    def _potential_pump_step(self, t, dt_half):
+        self.u = self.u.astype(np.complex128)
+        super()._potential_pump_step(t, dt_half)
+        self.u = self.u.astype(np.complex64)
+
+
+def solve_fp32(prob: OracleProblem, tspan, dt: float, nsaves: int, save_start: bool = True,
+               xi_source: Optional[Callable] = None):
+    it = Fp32Iterator(prob, tspan, dt, nsaves, save_start, xi_source)
+    it.u = it.u.astype(np.complex64)
+    return it.solve()

@@ -74,23 +74,3 @@ def polariton2d(N=128, L=256.0, A=5.0, ramp=200.0, w=50.0, dtype=np.complex128):
                           pump_amp=lambda t: np.array([amp(t), 0.0]))
     return gpu, orc
 
-
-def fp32_fft_pipeline_error(orc, tspan, dt, nsaves, g):
-    """Rel L2 (all saves) of the same scalar Kerr run done with a standard FP32 FFT
-    (scipy/pocketfft in single precision), the arithmetic of the reference's
-    ComplexF32 path.  It bounds what any FP32 implementation can reach on
-    ill-conditioned (self-focusing) cases."""
-    import scipy.fft as sf
-    it = O.OracleIterator(orc, tspan, dt, nsaves)
-    ts, ref = O.solve(orc, tspan, dt, nsaves)
-    E = it.exp_D.astype(np.complex64)
-    dth = np.float32(it.dt / 2)
-    u = orc.u0[0].astype(np.complex64)
-    out = [u.copy()]
-    for _ in range(nsaves):
-        for _ in range(it.steps_per_save):
-            u = (np.exp(-1j * dth * np.float32(g) * (np.abs(u) ** 2)).astype(np.complex64) * u).astype(np.complex64)
-            u = sf.ifft2((E * sf.fft2(u)).astype(np.complex64)).astype(np.complex64)
-            u = (np.exp(-1j * dth * np.float32(g) * (np.abs(u) ** 2)).astype(np.complex64) * u).astype(np.complex64)
-        out.append(u.copy())
-    return O.rel_l2(np.array(out).astype(np.complex128), ref[0])

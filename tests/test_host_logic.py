@@ -1,0 +1,112 @@
+"""Host-side logic of the mirror of the reference's surface (no GPU needed): grids,
+dt resolution, pump sampling times, closure classification, Philox restatement."""
+import math
+
+import numpy as np
+import pytest
+
+from oracle import gpe_oracle as O
+
+
+def test_grids_match_reference_convention(gpe):
+    """src/problem.jl:129-139: x_j = j L/N; k = fftfreq(N, 2 pi N / L)."""
+    from gpe_gb300 import problem as P
+    for L, N in [(8.0, 128), (256.0, 512), (10.0, 64), (3.0, 16)]:
+        assert np.array_equal(P.direct_grid_axis(L, N), O.direct_grid(L, N))
+        assert np.allclose(P.reciprocal_grid_axis(L, N), np.fft.fftfreq(N, L / N) * 2 * math.pi, rtol=1e-15, atol=1e-13)
+        assert np.array_equal(P.reciprocal_grid_axis(L, N), O.reciprocal_grid(L, N))
+
+
+def test_dt_resolution_and_pump_times_agree_with_oracle(gpe):
+    for dt, tspan, ns in [(0.01, (0, 0.4), 64), (0.05, (0, 200), 100), (0.3, (0, 7.7), 13), (4, (0, 200), 1)]:
+        a = gpe.resolve_fixed_timestepping(dt, tspan, ns)
+        b = O.resolve_fixed_timestepping(dt, tspan, ns)
+        assert a[0] == b[0] and a[2] == b[2]
+        n = a[2] * ns
+        assert np.array_equal(gpe.pump_sample_times(float(tspan[0]), a[0], n), O.pump_times(float(tspan[0]), a[0], n))
+
+
+def test_nonlinearity_classification(gpe):
+    from gpe_gb300.problem import classify_nonlinearity
+    g, c = classify_nonlinearity(lambda u, p: -6.0 * np.abs(u[0]) ** 2, 1, None)
+    assert np.allclose(g, [[-6.0]]) and np.allclose(c, [0])
+    # SVector and SMatrix{1,1} forms of the same closure
+    g2, _ = classify_nonlinearity(lambda u, p: [-6.0 * np.abs(u[0]) ** 2], 1, None)
+    g3, _ = classify_nonlinearity(lambda u, p: [[-6.0 * np.abs(u[0]) ** 2]], 1, None)
+    assert np.allclose(g2, g) and np.allclose(g3, g)
+    g, c = classify_nonlinearity(lambda u, p: [0 * u[0], p * np.abs(u[1]) ** 2], 2, 0.003)
+    assert np.allclose(g, [[0, 0], [0, 0.003]])
+    g, c = classify_nonlinearity(lambda u, p: (0.01 - 0.2j) * (np.abs(u[0]) ** 2 - 1 / 0.5), 1, None)
+    assert np.allclose(g, [[0.01 - 0.2j]]) and np.allclose(c, [-(0.01 - 0.2j) * 2])
+    with pytest.raises(NotImplementedError):
+        classify_nonlinearity(lambda u, p: np.abs(u[0]) ** 4, 1, None)
+    with pytest.raises(NotImplementedError):
+        classify_nonlinearity(lambda u, p: [[np.abs(u[0]) ** 2, 1.0 + 0 * u[0]], [1.0 + 0 * u[0], np.abs(u[1]) ** 2]], 2, None)
+
+
+def test_pump_classification(gpe):
+    from gpe_gb300.problem import classify_pump, direct_grid_axis
+    L, N = 16.0, 32
+    axes = (direct_grid_axis(L, N), direct_grid_axis(L, N))
+    times = gpe.pump_sample_times(0.0, 0.1, 20)
+    amp = lambda t: 2.0 * min(t / 1.0, 1.0) * np.exp(0.3j * t)
+    prof = lambda r: np.exp(-((r[0] - 8) ** 2 + (r[1] - 8) ** 2) / 9)
+    profiles, amps = classify_pump(lambda r, p, t: [amp(t) * prof(r), 0], axes, None, 2, times)
+    assert profiles[1] is None
+    X, Y = np.meshgrid(*axes, indexing="ij")
+    for i, t in enumerate(times):
+        F = amps[0, i] * profiles[0]
+        assert np.allclose(F, (amp(t) * prof((X, Y))).ravel(order="F"), rtol=1e-12, atol=1e-14)
+    with pytest.raises(NotImplementedError):
+        classify_pump(lambda r, p, t: np.exp(-((r[0] - t) ** 2)), axes, None, 1, times)
+
+
+def test_noise_classification(gpe):
+    from gpe_gb300.problem import classify_noise, direct_grid_axis
+    axes = (direct_grid_axis(10.0, 16),)
+    eta, prof = classify_noise(lambda u, r, p: 0.5, axes, None, 1, (16,))
+    assert np.allclose(eta, [0.5]) and prof is None
+    eta, prof = classify_noise(lambda u, r, p: [0.5, 0.25j], axes, None, 2, (16,))
+    assert np.allclose(eta, [0.5, 0.25j]) and prof is None
+    eta, prof = classify_noise(lambda u, r, p: 0.5 * np.exp(-r[0] ** 2), axes, None, 1, (16,))
+    assert prof is not None and np.allclose(eta[0] * prof[0], 0.5 * np.exp(-axes[0] ** 2))
+    with pytest.raises(NotImplementedError):
+        classify_noise(lambda u, r, p: 0.1 * np.abs(u[0]), axes, None, 1, (16,))
+
+
+def test_table_sampling_kinds(gpe):
+    from gpe_gb300 import _lib as L
+    from gpe_gb300.problem import sample_table, reciprocal_grid_axis
+    ax = (reciprocal_grid_axis(8.0, 16), reciprocal_grid_axis(4.0, 32))
+    v, k = sample_table(lambda k, p: (k[0] ** 2 + k[1] ** 2) / 2, ax, None, 1)
+    assert k == L.GPE_TABLE_SCALAR and v.shape == (1, 512)
+    KX, KY = np.meshgrid(*ax, indexing="ij")
+    assert np.array_equal(v[0], ((KX ** 2 + KY ** 2) / 2).ravel(order="F"))
+    v, k = sample_table(lambda k, p: [[k[0], 1.0], [1.0, -0.1j]], ax, None, 2)
+    assert k == L.GPE_TABLE_MATRIX and v.shape == (4, 512) and np.all(v[1] == 1.0)
+    v, k = sample_table(lambda k, p: [k[0], k[1]], ax, None, 2)
+    assert k == L.GPE_TABLE_DIAG
+    v, k = sample_table(lambda k, p: [[(k[0] ** 2 + k[1] ** 2) / 2]], ax, None, 1)
+    assert k == L.GPE_TABLE_SCALAR
+
+
+def test_philox_known_answers():
+    """Philox4x32-10 known-answer vectors (Random123 kat_vectors)."""
+    kats = [((0, 0, 0, 0), (0, 0), (0x6627E8D5, 0xE169C58D, 0xBC57AC4C, 0x9B00DBD8)),
+            ((0xFFFFFFFF,) * 4, (0xFFFFFFFF,) * 2, (0x408F276D, 0x41C83B0E, 0xA20BC7C6, 0x6D5451FD)),
+            ((0x243F6A88, 0x85A308D3, 0x13198A2E, 0x03707344), (0xA4093822, 0x299F31D0),
+             (0xD16CFE09, 0x94FDCCEB, 0x5001E420, 0x24126EA1))]
+    for ctr, key, want in kats:
+        got = O.philox4x32_10(*[np.array([c], np.uint64) for c in ctr], *key)
+        assert tuple(int(g[0]) for g in got) == want
+
+
+def test_philox_noise_statistics():
+    xi = O.PhiloxNoise(42, 2, (4,), (64, 64))(3)
+    assert xi.shape == (2, 4, 64, 64)
+    assert abs(np.mean(np.abs(xi) ** 2) - 1) < 0.02
+    assert abs(np.mean(xi)) < 0.02
+    assert abs(np.mean(xi.real ** 2) - 0.5) < 0.02 and abs(np.mean(xi.real * xi.imag)) < 0.02
+    # independent streams per half step and per component
+    assert np.abs(np.mean(xi[0] * np.conj(xi[1]))) < 0.02
+    assert not np.allclose(O.PhiloxNoise(42, 1, (), (16,))(0), O.PhiloxNoise(42, 1, (), (16,))(1))
