@@ -22,6 +22,7 @@ GPE_ERR_TIMEOUT = -5
 GPE_ERR_NOMEM = -6
 GPE_C128 = 0
 GPE_C64 = 1
+GPE_FLAG_FP64_NATIVE = 1
 GPE_TABLE_NONE, GPE_TABLE_SCALAR, GPE_TABLE_DIAG, GPE_TABLE_MATRIX = 0, 1, 2, 3
 GPE_NOISE_OFF, GPE_NOISE_PHILOX, GPE_NOISE_REPLAY = 0, 1, 2
 

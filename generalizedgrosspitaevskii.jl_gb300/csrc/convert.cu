@@ -1,0 +1,36 @@
+// convert.cu -- FP64 <-> double-word conversion of complex arrays on the device.
+#include "dw.cuh"
+#include "kernels.h"
+
+namespace gpe {
+
+__global__ void f64_to_dw_kernel(const double2* __restrict__ src, dwc* __restrict__ dst, int64_t n) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    const double2 v = src[i];
+    dst[i] = mk(dw_from(v.x), dw_from(v.y));
+  }
+}
+
+__global__ void dw_to_f64_kernel(const dwc* __restrict__ src, double2* __restrict__ dst, int64_t n) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    const dwc v = src[i];
+    dst[i] = make_double2(dw_to_double(re(v)), dw_to_double(im(v)));
+  }
+}
+
+static unsigned grid_for(int64_t n) {
+  int64_t b = (n + 255) / 256;
+  return (unsigned)(b > 152 * 32 ? 152 * 32 : (b < 1 ? 1 : b));
+}
+
+int launch_f64_to_dw(const void* src, void* dst, int64_t n, cudaStream_t s) {
+  f64_to_dw_kernel<<<grid_for(n), 256, 0, s>>>((const double2*)src, (dwc*)dst, n);
+  return (int)cudaGetLastError();
+}
+
+int launch_dw_to_f64(const void* src, void* dst, int64_t n, cudaStream_t s) {
+  dw_to_f64_kernel<<<grid_for(n), 256, 0, s>>>((const dwc*)src, (double2*)dst, n);
+  return (int)cudaGetLastError();
+}
+
+}  // namespace gpe

@@ -26,11 +26,29 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <type_traits>
+
+#include "dw.cuh"
+
 namespace gpe {
 
+// Precision tags: double (native FP64), float (FP32) and DWR (double-word FP64 on the
+// FP32 pipes, see dw.cuh).  CT<R>::T is the complex storage type.
+struct DWR {};
 template <typename Real> struct CT;
 template <> struct CT<double> { using T = double2; };
 template <> struct CT<float> { using T = float2; };
+template <> struct CT<DWR> { using T = dwc; };
+
+// read-only cached loads of complex table entries
+__device__ __forceinline__ double2 ldgc(const double2* p) { return __ldg(p); }
+__device__ __forceinline__ float2 ldgc(const float2* p) { return __ldg(p); }
+__device__ __forceinline__ dwc ldgc(const dwc* p) {
+  const float4 v = __ldg(reinterpret_cast<const float4*>(p));
+  dwc z;
+  z.xh = v.x; z.xl = v.y; z.yh = v.z; z.yl = v.w;
+  return z;
+}
 
 template <typename C> __device__ __forceinline__ C cadd(C a, C b) { C r; r.x = a.x + b.x; r.y = a.y + b.y; return r; }
 template <typename C> __device__ __forceinline__ C csub(C a, C b) { C r; r.x = a.x - b.x; r.y = a.y - b.y; return r; }
@@ -76,18 +94,41 @@ __host__ __device__ constexpr int bitrev(int v, int bits) {
 template <int DIR, int n, int i, typename C>
 __device__ __forceinline__ C twc(C d) {
   constexpr int k = (i * 16 / n) & 15;
-  if constexpr (k == 0) {
-    return d;
-  } else if constexpr (k == 4) {  // w = DIR * i
-    C r; r.x = -DIR * d.y; r.y = DIR * d.x; return r;
-  } else if constexpr (k == 8) {
-    C r; r.x = -d.x; r.y = -d.y; return r;
-  } else if constexpr (k == 12) {  // w = -DIR * i
-    C r; r.x = DIR * d.y; r.y = -DIR * d.x; return r;
+  if constexpr (std::is_same<C, dwc>::value) {
+    if constexpr (k == 0) {
+      return d;
+    } else if constexpr (k == 4) {  // w = DIR * i: (x, y) -> (-DIR y, DIR x)
+      dwc r;
+      r.xh = -DIR * d.yh; r.xl = -DIR * d.yl; r.yh = DIR * d.xh; r.yl = DIR * d.xl;
+      return r;
+    } else if constexpr (k == 8) {
+      dwc r;
+      r.xh = -d.xh; r.xl = -d.xl; r.yh = -d.yh; r.yl = -d.yl;
+      return r;
+    } else if constexpr (k == 12) {
+      dwc r;
+      r.xh = DIR * d.yh; r.xl = DIR * d.yl; r.yh = -DIR * d.xh; r.yl = -DIR * d.xl;
+      return r;
+    } else {
+      dwc w;
+      w.xh = dwh(cos16(k)); w.xl = dwl(cos16(k));
+      w.yh = dwh(DIR * sin16(k)); w.yl = dwl(DIR * sin16(k));
+      return cmul(d, w);
+    }
   } else {
-    using R = decltype(d.x);
-    const R c = (R)cos16(k), s = (R)(DIR * sin16(k));
-    C r; r.x = d.x * c - d.y * s; r.y = d.x * s + d.y * c; return r;
+    if constexpr (k == 0) {
+      return d;
+    } else if constexpr (k == 4) {  // w = DIR * i
+      C r; r.x = -DIR * d.y; r.y = DIR * d.x; return r;
+    } else if constexpr (k == 8) {
+      C r; r.x = -d.x; r.y = -d.y; return r;
+    } else if constexpr (k == 12) {  // w = -DIR * i
+      C r; r.x = DIR * d.y; r.y = -DIR * d.x; return r;
+    } else {
+      using R = decltype(d.x);
+      const R c = (R)cos16(k), s = (R)(DIR * sin16(k));
+      C r; r.x = d.x * c - d.y * s; r.y = d.x * s + d.y * c; return r;
+    }
   }
 }
 
@@ -177,7 +218,7 @@ __device__ __forceinline__ void fft_stage(C (&x)[E], int t, const Lay& lay, cons
       constexpr int TS = N / (NS * R);
 #pragma unroll
       for (int r = 1; r < R; ++r) {
-        const C w = __ldg(tw + k * r * TS);
+        const C w = ldgc(tw + k * r * TS);
         v[r] = (DIR < 0) ? cmul(v[r], w) : cmulc(v[r], w);
       }
     }

@@ -31,9 +31,10 @@ template <typename Real, int M> int launch_line1d_t(int, const PassArgs&, cudaSt
 template <typename Real, int M> int launch_nl_only_t(const PassArgs&, cudaStream_t);
 template <typename Real, int M> int launch_norm_t(const PassArgs&, double*, cudaStream_t);
 
-#define GPE_DISPATCH(FN, ...)                                          \
-  if (dtype == GPE_C128) return M == 1 ? FN<double, 1>(__VA_ARGS__)   \
-                                       : FN<double, 2>(__VA_ARGS__);  \
+// dtype here is the pass precision (PREC_F64, PREC_F32, PREC_DW)
+#define GPE_DISPATCH(FN, ...)                                                                  \
+  if (dtype == PREC_F64) return M == 1 ? FN<double, 1>(__VA_ARGS__) : FN<double, 2>(__VA_ARGS__); \
+  if (dtype == PREC_DW) return M == 1 ? FN<DWR, 1>(__VA_ARGS__) : FN<DWR, 2>(__VA_ARGS__);        \
   return M == 1 ? FN<float, 1>(__VA_ARGS__) : FN<float, 2>(__VA_ARGS__);
 
 int launch_row(int dtype, int M, int logn, const PassArgs& a, int64_t nl, cudaStream_t s) { GPE_DISPATCH(launch_row_t, logn, a, nl, s) }
@@ -49,7 +50,8 @@ struct gpe_handle {
   gpe_desc d{};
   int dev = 0;
   int M = 1, dtype = GPE_C128, ndim = 2;
-  size_t rsz = 8, csz = 16;  // bytes per real / complex
+  int prec = gpe::PREC_DW;   // pass precision: FP64 fields default to double-word passes
+  size_t rsz = 8, csz = 16;  // device bytes per real / complex number
   int64_t n[3] = {1, 1, 1};
   int logn[3] = {0, 0, 0};
   int64_t P = 1, B = 1;
@@ -69,8 +71,8 @@ struct gpe_handle {
   void* pprof[2] = {nullptr, nullptr};
   int pprof_cplx = 0;
   std::vector<cd> pprof_host[2];
-  double2* pamp[2] = {nullptr, nullptr};
-  int64_t pamp_n[2] = {0, 0};
+  void* pcoef[2] = {nullptr, nullptr};  // (dt/4) a(t_h) per half-step boundary, pass precision
+  int64_t pcoef_n[2] = {0, 0};
   void* etaprof[2] = {nullptr, nullptr};
   int noise = GPE_NOISE_OFF;
   uint64_t seed = 0;
@@ -127,11 +129,23 @@ static int fail(gpe_handle* h, int code, const char* fmt, ...) {
 static bool is_pow2(int64_t v) { return v > 0 && (v & (v - 1)) == 0; }
 static int ilog2i(int64_t v) { int r = 0; while ((1ll << r) < v) ++r; return r; }
 
-// Upload n complex FP64 values converted to the handle precision.
+// FP64 -> double word: hi = fl32(v), lo = fl32(v - hi)
+static inline void split_dw(double v, float* hl) {
+  const float hi = (float)v;
+  hl[0] = hi;
+  hl[1] = (float)(v - (double)hi);
+}
+
+// Upload n complex FP64 values in the handle's pass precision (double2, float2, or
+// the double-word layout {re.hi, re.lo, im.hi, im.lo}).
 static int upload_complex(gpe_handle* h, void** dst, const cd* src, size_t n) {
   if (!*dst) CK(h, cudaMalloc(dst, n * h->csz));
-  if (h->dtype == GPE_C128) {
+  if (h->prec == gpe::PREC_F64) {
     CK(h, cudaMemcpy(*dst, src, n * 16, cudaMemcpyHostToDevice));
+  } else if (h->prec == gpe::PREC_DW) {
+    std::vector<float> tmp(4 * n);
+    for (size_t i = 0; i < n; ++i) { split_dw(src[i].real(), &tmp[4 * i]); split_dw(src[i].imag(), &tmp[4 * i + 2]); }
+    CK(h, cudaMemcpy(*dst, tmp.data(), n * 16, cudaMemcpyHostToDevice));
   } else {
     std::vector<float> tmp(2 * n);
     for (size_t i = 0; i < n; ++i) { tmp[2 * i] = (float)src[i].real(); tmp[2 * i + 1] = (float)src[i].imag(); }
@@ -139,10 +153,15 @@ static int upload_complex(gpe_handle* h, void** dst, const cd* src, size_t n) {
   }
   return GPE_OK;
 }
+// Upload n real FP64 values (double, float, or a {hi, lo} float pair).
 static int upload_real(gpe_handle* h, void** dst, const double* src, size_t n) {
   if (!*dst) CK(h, cudaMalloc(dst, n * h->rsz));
-  if (h->dtype == GPE_C128) {
+  if (h->prec == gpe::PREC_F64) {
     CK(h, cudaMemcpy(*dst, src, n * 8, cudaMemcpyHostToDevice));
+  } else if (h->prec == gpe::PREC_DW) {
+    std::vector<float> tmp(2 * n);
+    for (size_t i = 0; i < n; ++i) split_dw(src[i], &tmp[2 * i]);
+    CK(h, cudaMemcpy(*dst, tmp.data(), n * 8, cudaMemcpyHostToDevice));
   } else {
     std::vector<float> tmp(n);
     for (size_t i = 0; i < n; ++i) tmp[i] = (float)src[i];
@@ -240,6 +259,7 @@ int gpe_create(const gpe_desc* desc, gpe_handle** out) {
   h->M = desc->ncomp;
   h->dtype = desc->dtype;
   h->ndim = desc->ndim;
+  h->prec = desc->dtype == GPE_C64 ? gpe::PREC_F32 : ((desc->flags & GPE_FLAG_FP64_NATIVE) ? gpe::PREC_F64 : gpe::PREC_DW);
   h->rsz = desc->dtype == GPE_C128 ? 8 : 4;
   h->csz = 2 * h->rsz;
   h->B = desc->batch;
@@ -293,7 +313,7 @@ int gpe_destroy(gpe_handle* h) {
   for (int m = 0; m < 2; ++m) {
     cudaFree(h->u[m]);
     cudaFree(h->pprof[m]);
-    cudaFree(h->pamp[m]);
+    cudaFree(h->pcoef[m]);
     cudaFree(h->etaprof[m]);
   }
   for (int a = 0; a < 3; ++a) cudaFree(h->tw[a]);
@@ -329,6 +349,13 @@ int gpe_set_field(gpe_handle* h, int comp, const void* host) {
     for (size_t i = 0; i < 2 * n; ++i)
       if (!std::isfinite(f[i])) return fail(h, GPE_ERR_NONFINITE, "field %d has NaN or Inf", comp);
   }
+  if (h->prec == gpe::PREC_DW) {
+    const double* v = (const double*)host;
+    std::vector<float> tmp(4 * n);
+    for (size_t i = 0; i < 2 * n; ++i) split_dw(v[i], &tmp[2 * i]);
+    CK(h, cudaMemcpy(h->u[comp], tmp.data(), n * 16, cudaMemcpyHostToDevice));
+    return GPE_OK;
+  }
   CK(h, cudaMemcpy(h->u[comp], host, n * h->csz, cudaMemcpyHostToDevice));
   return GPE_OK;
 }
@@ -337,8 +364,16 @@ int gpe_get_field(gpe_handle* h, int comp, void* host) {
   int rc = check_comp(h, comp);
   if (rc) return rc;
   if (!host) return fail(h, GPE_ERR_INVALID, "null destination");
+  const size_t n = (size_t)h->P * h->B;
   CK(h, cudaStreamSynchronize(h->stream));
-  CK(h, cudaMemcpy(host, h->u[comp], (size_t)h->P * h->B * h->csz, cudaMemcpyDeviceToHost));
+  if (h->prec == gpe::PREC_DW) {
+    std::vector<float> tmp(4 * n);
+    CK(h, cudaMemcpy(tmp.data(), h->u[comp], n * 16, cudaMemcpyDeviceToHost));
+    double* v = (double*)host;
+    for (size_t i = 0; i < 2 * n; ++i) v[i] = (double)tmp[2 * i] + (double)tmp[2 * i + 1];
+    return GPE_OK;
+  }
+  CK(h, cudaMemcpy(host, h->u[comp], n * h->csz, cudaMemcpyDeviceToHost));
   return GPE_OK;
 }
 
@@ -346,7 +381,11 @@ int gpe_set_field_dev(gpe_handle* h, int comp, const void* dev) {
   int rc = check_comp(h, comp);
   if (rc) return rc;
   if (!dev) return fail(h, GPE_ERR_INVALID, "null field");
-  CK(h, cudaMemcpyAsync(h->u[comp], dev, (size_t)h->P * h->B * h->csz, cudaMemcpyDeviceToDevice, h->stream));
+  if (h->prec == gpe::PREC_DW) {
+    LK(h, gpe::launch_f64_to_dw(dev, h->u[comp], h->P * h->B, h->stream));
+  } else {
+    CK(h, cudaMemcpyAsync(h->u[comp], dev, (size_t)h->P * h->B * h->csz, cudaMemcpyDeviceToDevice, h->stream));
+  }
   CK(h, cudaStreamSynchronize(h->stream));
   return GPE_OK;
 }
@@ -355,7 +394,11 @@ int gpe_get_field_dev(gpe_handle* h, int comp, void* dev) {
   int rc = check_comp(h, comp);
   if (rc) return rc;
   if (!dev) return fail(h, GPE_ERR_INVALID, "null destination");
-  CK(h, cudaMemcpyAsync(dev, h->u[comp], (size_t)h->P * h->B * h->csz, cudaMemcpyDeviceToDevice, h->stream));
+  if (h->prec == gpe::PREC_DW) {
+    LK(h, gpe::launch_dw_to_f64(h->u[comp], dev, h->P * h->B, h->stream));
+  } else {
+    CK(h, cudaMemcpyAsync(dev, h->u[comp], (size_t)h->P * h->B * h->csz, cudaMemcpyDeviceToDevice, h->stream));
+  }
   CK(h, cudaStreamSynchronize(h->stream));
   return GPE_OK;
 }
@@ -480,9 +523,9 @@ int gpe_set_pump(gpe_handle* h, int comp, const double* profile, int profile_com
   if (rc) return rc;
   cudaFree(h->pprof[comp]);
   h->pprof[comp] = nullptr;
-  cudaFree(h->pamp[comp]);
-  h->pamp[comp] = nullptr;
-  h->pamp_n[comp] = 0;
+  cudaFree(h->pcoef[comp]);
+  h->pcoef[comp] = nullptr;
+  h->pcoef_n[comp] = 0;
   h->pprof_host[comp].clear();
   if (!profile) return GPE_OK;
   if (!amp || n_amp < 1) return fail(h, GPE_ERR_INVALID, "pump needs at least one amplitude");
@@ -492,9 +535,14 @@ int gpe_set_pump(gpe_handle* h, int comp, const double* profile, int profile_com
   std::vector<cd>& ph = h->pprof_host[comp];
   ph.resize(P);
   for (size_t p = 0; p < P; ++p) ph[p] = profile_complex ? cd(profile[2 * p], profile[2 * p + 1]) : cd(profile[p], 0.0);
-  CK(h, cudaMalloc((void**)&h->pamp[comp], (size_t)n_amp * sizeof(double2)));
-  CK(h, cudaMemcpy(h->pamp[comp], amp, (size_t)n_amp * sizeof(double2), cudaMemcpyHostToDevice));
-  h->pamp_n[comp] = n_amp;
+  {
+    // (dt/4) a(t_h): the delta/2 = dt/4 factor of src/kernels.jl:45-46, formed in FP64
+    std::vector<cd> coef((size_t)n_amp);
+    for (int64_t i = 0; i < n_amp; ++i) coef[(size_t)i] = 0.25 * h->d.dt * cd(amp[2 * i], amp[2 * i + 1]);
+    rc = upload_complex(h, &h->pcoef[comp], coef.data(), (size_t)n_amp);
+    if (rc) return rc;
+    h->pcoef_n[comp] = n_amp;
+  }
   // All pumped components share one profile format: complex if any profile is complex.
   int want_cplx = 0;
   for (int m = 0; m < h->M; ++m)
@@ -574,16 +622,29 @@ static PassArgs base_args(gpe_handle* h) {
   a.kkind = h->kkind;
   a.vtab = h->vtab;
   a.vkind = h->vkind;
+  float hl[2];
   for (int j = 0; j < 2; ++j) {
     a.nl_on[j] = h->nl_on[j];
+    a.nl_imag[j] = h->c[j][1] != 0.0;
     for (int l = 0; l < 2; ++l)
-      for (int r = 0; r < 2; ++r) { a.g[j][l][r] = h->g[j][l][r]; a.gf[j][l][r] = (float)h->g[j][l][r]; }
-    for (int r = 0; r < 2; ++r) { a.c[j][r] = h->c[j][r]; a.cf[j][r] = (float)h->c[j][r]; }
+      for (int r = 0; r < 2; ++r) {
+        a.g[j][l][r] = h->g[j][l][r];
+        split_dw(h->g[j][l][r], hl);
+        a.gf[j][l][r] = hl[0];
+        a.gl[j][l][r] = hl[1];
+        if (r == 1 && h->g[j][l][1] != 0.0) a.nl_imag[j] = 1;
+      }
+    for (int r = 0; r < 2; ++r) {
+      a.c[j][r] = h->c[j][r];
+      split_dw(h->c[j][r], hl);
+      a.cf[j][r] = hl[0];
+      a.cl[j][r] = hl[1];
+    }
   }
   for (int m = 0; m < h->M; ++m) {
     a.pprof[m] = h->pprof[m];
-    a.pamp[m] = h->pamp[m];
-    a.pamp_n[m] = h->pamp_n[m];
+    a.pcoef[m] = h->pcoef[m];
+    a.pcoef_n[m] = h->pcoef_n[m];
     a.etaprof[m] = h->etaprof[m];
   }
   a.pprof_cplx = h->pprof_cplx;
@@ -595,11 +656,16 @@ static PassArgs base_args(gpe_handle* h) {
   for (int m = 0; m < h->M; ++m) {
     a.nfac[m][0] = sq * h->eta[m][1];
     a.nfac[m][1] = -sq * h->eta[m][0];
-    a.nfacf[m][0] = (float)a.nfac[m][0];
-    a.nfacf[m][1] = (float)a.nfac[m][1];
+    for (int r = 0; r < 2; ++r) {
+      split_dw(a.nfac[m][r], hl);
+      a.nfacf[m][r] = hl[0];
+      a.nfacl[m][r] = hl[1];
+    }
   }
   a.dt = h->d.dt;
-  a.dthf = (float)(0.5 * h->d.dt);
+  split_dw(0.5 * h->d.dt, hl);
+  a.dthf = hl[0];
+  a.dthl = hl[1];
   a.hA = a.hB = -1;
   return a;
 }
@@ -638,10 +704,10 @@ static int enqueue_steps(gpe_handle* h, int64_t nsteps, int64_t save_every, void
     if (save_every > 0) slot_ptrs(a, 0);
     TimedLaunch tl(h, 2);
     if (!has_k) {
-      LK(h, gpe::launch_nl_only(h->dtype, h->M, a, h->stream));
+      LK(h, gpe::launch_nl_only(h->prec, h->M, a, h->stream));
     } else {
       a.tw = h->tw[0];
-      LK(h, gpe::launch_line1d(h->dtype, h->M, h->logn[0], a, h->stream));
+      LK(h, gpe::launch_line1d(h->prec, h->M, h->logn[0], a, h->stream));
     }
     *launches = 1;
     return GPE_OK;
@@ -656,7 +722,7 @@ static int enqueue_steps(gpe_handle* h, int64_t nsteps, int64_t save_every, void
   r.hB = -1;
   {
     TimedLaunch tl(h, 0);
-    LK(h, gpe::launch_row(h->dtype, h->M, h->logn[0], r, nrows, h->stream));
+    LK(h, gpe::launch_row(h->prec, h->M, h->logn[0], r, nrows, h->stream));
   }
   ++nl;
   PassArgs c = a;
@@ -669,7 +735,7 @@ static int enqueue_steps(gpe_handle* h, int64_t nsteps, int64_t save_every, void
   for (int64_t s = 0; s < nsteps; ++s) {
     {
       TimedLaunch tl(h, 1);
-      LK(h, gpe::launch_col(h->dtype, h->M, h->logn[1], c, h->stream));
+      LK(h, gpe::launch_col(h->prec, h->M, h->logn[1], c, h->stream));
     }
     const bool last = (s == nsteps - 1);
     PassArgs rr = a;
@@ -681,7 +747,7 @@ static int enqueue_steps(gpe_handle* h, int64_t nsteps, int64_t save_every, void
     if (save_every > 0 && (s + 1) % save_every == 0) slot_ptrs(rr, (s + 1) / save_every - 1);
     {
       TimedLaunch tl(h, 0);
-      LK(h, gpe::launch_row(h->dtype, h->M, h->logn[0], rr, nrows, h->stream));
+      LK(h, gpe::launch_row(h->prec, h->M, h->logn[0], rr, nrows, h->stream));
     }
     nl += 2;
   }
@@ -701,8 +767,8 @@ static int run_common(gpe_handle* h, int64_t nsteps, int64_t save_every, void* o
   const int64_t nsaves = save_every > 0 ? nsteps / save_every : 0;
   if (nsaves > 0 && !out) return fail(h, GPE_ERR_INVALID, "null save buffer");
   for (int m = 0; m < h->M; ++m)
-    if (h->pprof[m] && h->pamp_n[m] > 1 && h->pamp_n[m] < 2 * (h->steps + nsteps) + 1)
-      return fail(h, GPE_ERR_INVALID, "pump %d has %lld amplitudes, %lld steps need %lld", m, (long long)h->pamp_n[m],
+    if (h->pprof[m] && h->pcoef_n[m] > 1 && h->pcoef_n[m] < 2 * (h->steps + nsteps) + 1)
+      return fail(h, GPE_ERR_INVALID, "pump %d has %lld amplitudes, %lld steps need %lld", m, (long long)h->pcoef_n[m],
                   (long long)(h->steps + nsteps), (long long)(2 * (h->steps + nsteps) + 1));
   if (h->noise == GPE_NOISE_REPLAY && !xi_host)
     return fail(h, GPE_ERR_INVALID, "noise mode is replay: use gpe_run_replay");
@@ -801,7 +867,7 @@ int gpe_norm(gpe_handle* h, double* out) {
   if (!out) return fail(h, GPE_ERR_INVALID, "null output");
   PassArgs a = base_args(h);
   CK(h, cudaMemsetAsync(h->red, 0, 4 * sizeof(double), h->stream));
-  LK(h, gpe::launch_norm(h->dtype, h->M, a, h->red, h->stream));
+  LK(h, gpe::launch_norm(h->prec, h->M, a, h->red, h->stream));
   double tmp[4];
   CK(h, cudaMemcpyAsync(tmp, h->red, 4 * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
   CK(h, cudaStreamSynchronize(h->stream));

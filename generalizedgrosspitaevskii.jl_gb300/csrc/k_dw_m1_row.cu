@@ -1,0 +1,6 @@
+// Instantiates the row kernels for double-word FP64 fields with 1 component(s); the
+// kernels are split over many small translation units so the build runs in parallel.
+#include "passes.cuh"
+namespace gpe {
+GPE_INSTANTIATE_ROW(DWR, 1)
+}  // namespace gpe

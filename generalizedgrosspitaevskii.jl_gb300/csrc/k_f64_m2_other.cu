@@ -1,0 +1,6 @@
+// Instantiates the other kernels for native FP64 fields with 2 component(s); the
+// kernels are split over many small translation units so the build runs in parallel.
+#include "passes.cuh"
+namespace gpe {
+GPE_INSTANTIATE_OTHER(double, 2)
+}  // namespace gpe

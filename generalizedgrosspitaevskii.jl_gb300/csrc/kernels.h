@@ -5,6 +5,8 @@
 
 namespace gpe {
 
+struct DWR;  // double-word precision tag (defined in fft.cuh)
+
 enum TableKind { TAB_NONE = 0, TAB_SCALAR = 1, TAB_DIAG = 2, TAB_MATRIX = 3 };
 enum NoiseMode { NOISE_OFF = 0, NOISE_PHILOX = 1, NOISE_REPLAY = 2 };
 
@@ -25,28 +27,30 @@ struct PassArgs {
   int32_t vkind;
   // twiddles w_N^k, k < N, for the transformed line length
   const void* tw;
-  // nonlinearity G_j = sum_l g[j][l] |u_l|^2 + c[j] (complex); FP64 values and their
-  // FP32 roundings, so the FP32 passes never convert per point
-  int32_t nl_on[2];
+  // nonlinearity G_j = sum_l g[j][l] |u_l|^2 + c[j] (complex).  FP64 values, their FP32
+  // roundings (gf, cf) and the FP32 remainders (gl, cl) that make (gf + gl) the
+  // double-word form, so no pass converts per point.
+  int32_t nl_on[2], nl_imag[2];
   double g[2][2][2];
   double c[2][2];
-  float gf[2][2][2];
-  float cf[2][2];
-  // pump F_m = a_m(t) p_m(r): profile (real or complex, pass precision), FP64 amplitudes
+  float gf[2][2][2], gl[2][2][2];
+  float cf[2][2], cl[2][2];
+  // pump F_m = a_m(t) p_m(r): profile (real or complex) and the per-boundary
+  // coefficients (dt/4) a_m(t_h), both stored in the pass precision
   const void* pprof[2];
   int32_t pprof_cplx;
-  const double2* pamp[2];
-  int64_t pamp_n[2];
-  // noise: -i sqrt(dt/2) eta_m (FP64, host-formed) [* eta profile] * xi
+  const void* pcoef[2];
+  int64_t pcoef_n[2];
+  // noise: -i sqrt(dt/2) eta_m (host-formed) [* eta profile] * xi
   int32_t noise;
   uint32_t seed_lo, seed_hi;
   double nfac[2][2];
-  float nfacf[2][2];
+  float nfacf[2][2], nfacl[2][2];
   const void* etaprof[2];
   const void* xi;     // replay: [half - xi_h0][m][b][p]
   int64_t xi_h0;
   double dt;
-  float dthf;  // dt/2 rounded to FP32
+  float dthf, dthl;  // dt/2 as FP32 and its double-word remainder
   // row pass program: [iFFT] [half hA] [save] [half hB] [FFT]; h < 0 skips a half
   int32_t do_ifft, do_fft;
   int64_t hA, hB;
@@ -59,6 +63,9 @@ struct PassArgs {
   int32_t col_fwd, col_inv;
 };
 
+// Pass precisions: native FP64, FP32, double-word FP64 on the FP32 pipes.
+enum PassPrec { PREC_F64 = 0, PREC_F32 = 1, PREC_DW = 2 };
+
 // Launchers: return 0 or a cudaError_t value.  logn = log2 of the line length.
 int launch_row(int dtype, int M, int logn, const PassArgs& a, int64_t nlines, cudaStream_t s);
 int launch_col(int dtype, int M, int logn, const PassArgs& a, cudaStream_t s);
@@ -66,5 +73,8 @@ int launch_line1d(int dtype, int M, int logn, const PassArgs& a, cudaStream_t s)
 int launch_nl_only(int dtype, int M, const PassArgs& a, cudaStream_t s);
 // FP64 reductions: out[m] += sum |u_m|^2 (device double array of M entries)
 int launch_norm(int dtype, int M, const PassArgs& a, double* out, cudaStream_t s);
+// FP64 <-> double-word conversion of n complex numbers
+int launch_f64_to_dw(const void* src, void* dst, int64_t n, cudaStream_t s);
+int launch_dw_to_f64(const void* src, void* dst, int64_t n, cudaStream_t s);
 
 }  // namespace gpe

@@ -9,6 +9,9 @@
 // Between steps the state stays x-transformed, so the trailing half of step k and
 // the leading half of step k+1 share one row pass.  In 1D a line is the whole
 // field, so one resident kernel runs many steps without touching HBM.
+//
+// Three precisions share the code: double (native FP64), float (FP32) and DWR
+// (double-word FP64 on the FP32 pipes, dw.cuh).
 #pragma once
 #include "fft.cuh"
 #include "kernels.h"
@@ -27,7 +30,7 @@ struct LineCfg {
   static constexpr int N = 1 << LOGN;
   // points per thread: column pass (E) and row pass (ER, which also carries the
   // pointwise half steps and so keeps fewer points live)
-  static constexpr int EMAX = (sizeof(Real) == 8 && M == 2) ? 8 : 16;
+  static constexpr int EMAX = (sizeof(C) == 16 && M == 2) ? 8 : 16;
   static constexpr int E = cmin(EMAX, N / 2);
   static constexpr int T = N / E;  // threads per line, column pass
   static constexpr int ERMAX = (M == 2) ? 8 : 16;
@@ -45,6 +48,7 @@ struct LineCfg {
   static constexpr size_t COL_SMEM = (size_t)CC * N * sizeof(C);
 };
 
+// ------------------------------------------------------------------ scalar helpers
 template <typename Real> __device__ __forceinline__ void sc(Real x, Real* s, Real* c);
 // FP64 sin/cos of the nonlinear phase.  FP64 runs at 1/64 of the FP32 rate on GB300, so
 // small angles (the usual case: |dt/2 * G| << 1) use the Taylor series of sin and cos
@@ -65,6 +69,33 @@ template <> __device__ __forceinline__ void sc<float>(float x, float* s, float* 
 __device__ __forceinline__ double rexp(double x) { return exp(x); }
 __device__ __forceinline__ float rexp(float x) { return expf(x); }
 
+// Double-word sin/cos.  |x| <= 1/8: cos = 1 - x^2/2 + x^4/24 + tail, sin = x (1 - x^2/6 +
+// x^4/120 + tail) with the double-word leading terms and the tails (below 6e-9 and
+// 8e-10) summed in FP32, which keeps the result within a few units of 2^-48.  Larger
+// angles go through the FP64 routine.
+__device__ __forceinline__ void dw_sincos(dw x, dw& s, dw& c) {
+  if (fabsf(x.h) <= 0.125f) {
+    const dw x2 = dw_mul(x, x);
+    const float t = x2.h;
+    const float t3 = t * t * t;
+    const float tc = t3 * (-1.0f / 720 + t * (1.0f / 40320 + t * (-1.0f / 3628800 + t * (1.0f / 479001600))));
+    const float ts = t3 * (-1.0f / 5040 + t * (1.0f / 362880 + t * (-1.0f / 39916800 + t * (1.0f / 6227020800.0f))));
+    const dw q = dw_mul(x2, x2);
+    dw cc = dw_add_acc({1.0f, 0.0f}, {-0.5f * x2.h, -0.5f * x2.l});
+    cc = dw_add_acc(cc, dw_mul(q, {dwh(1.0 / 24), dwl(1.0 / 24)}));
+    c = dw_add_acc(cc, {tc, 0.0f});
+    dw ss = dw_add_acc({1.0f, 0.0f}, dw_neg(dw_mul(x2, {dwh(1.0 / 6), dwl(1.0 / 6)})));
+    ss = dw_add_acc(ss, dw_mul(q, {dwh(1.0 / 120), dwl(1.0 / 120)}));
+    ss = dw_add_acc(ss, {ts, 0.0f});
+    s = dw_mul(x, ss);
+  } else {
+    double sd, cd;
+    sincos(dw_to_double(x), &sd, &cd);
+    s = dw_from(sd);
+    c = dw_from(cd);
+  }
+}
+
 // Typed views of the coefficient block.
 template <typename Real> struct Coef;
 template <> struct Coef<double> {
@@ -80,58 +111,151 @@ template <> struct Coef<float> {
   __device__ static __forceinline__ float dth(const PassArgs& a) { return a.dthf; }
 };
 
-// Pump coefficient (dt/4) * a(t_h) for half-step boundary h, formed in FP64.
-template <typename C>
-__device__ __forceinline__ C pump_coef(const PassArgs& a, int m, int64_t h) {
-  const int64_t n = a.pamp_n[m];
-  const double2 amp = a.pamp[m][n == 1 ? 0 : (h < n ? h : n - 1)];
-  const double f = 0.25 * a.dt;
-  return cmake<C>(f * amp.x, f * amp.y);
+// real profile value at p (pump or noise profile), stored as Real / Real / dw
+template <typename Real> struct Prof;
+template <> struct Prof<double> {
+  __device__ static __forceinline__ double2 cplx(const void* base, int64_t p) { return make_double2(__ldg((const double*)base + p), 0.0); }
+};
+template <> struct Prof<float> {
+  __device__ static __forceinline__ float2 cplx(const void* base, int64_t p) { return make_float2(__ldg((const float*)base + p), 0.0f); }
+};
+template <> struct Prof<DWR> {
+  __device__ static __forceinline__ dwc cplx(const void* base, int64_t p) {
+    const float2 v = __ldg((const float2*)base + p);
+    dwc z; z.xh = v.x; z.xl = v.y; z.yh = 0.0f; z.yl = 0.0f;
+    return z;
+  }
+};
+
+// complex normal deviate in the pass precision
+template <typename Real> struct Xi;
+template <> struct Xi<double> {
+  __device__ static __forceinline__ double2 get(uint32_t w0, uint32_t w1) { return box_muller_f64(w0, w1); }
+};
+template <> struct Xi<float> {
+  __device__ static __forceinline__ float2 get(uint32_t w0, uint32_t w1) { return box_muller_f32(w0, w1); }
+};
+template <> struct Xi<DWR> {
+  __device__ static __forceinline__ dwc get(uint32_t w0, uint32_t w1) {
+    const double2 v = box_muller_f64(w0, w1);
+    return mk(dw_from(v.x), dw_from(v.y));
+  }
+};
+
+template <typename C> __device__ __forceinline__ C czero() {
+  C z;
+  memset(&z, 0, sizeof z);
+  return z;
+}
+
+// Pump coefficients (dt/4) a(t_h) and (dt/4) a(t_{h+1}) for half step h.
+template <typename Real, int M>
+__device__ __forceinline__ void load_pump(const PassArgs& a, int64_t h, typename CT<Real>::T (&pn)[M],
+                                          typename CT<Real>::T (&px)[M]) {
+  using C = typename CT<Real>::T;
+#pragma unroll
+  for (int j = 0; j < M; ++j) {
+    if (a.pprof[j] && h >= 0) {
+      const int64_t n = a.pcoef_n[j];
+      const C* pc = (const C*)a.pcoef[j];
+      pn[j] = n == 1 ? ldgc(pc) : ldgc(pc + (h < n ? h : n - 1));
+      px[j] = n == 1 ? pn[j] : ldgc(pc + (h + 1 < n ? h + 1 : n - 1));
+    } else {
+      pn[j] = czero<C>();
+      px[j] = pn[j];
+    }
+  }
+}
+
+// xi for half step h at point p of trajectory b (Philox or replayed)
+template <typename Real, int M>
+__device__ __forceinline__ void draw_xi(const PassArgs& a, int64_t p, int64_t b, int64_t h,
+                                        typename CT<Real>::T (&xi)[M]) {
+  using C = typename CT<Real>::T;
+  if (a.noise == NOISE_PHILOX) {
+    const uint4 r = Philox4x32::gen(noise_counter(p, b, h), a.seed_lo, a.seed_hi);
+    xi[0] = Xi<Real>::get(r.x, r.y);
+    if constexpr (M == 2) xi[M - 1] = Xi<Real>::get(r.z, r.w);
+  } else {
+    const C* xb = (const C*)a.xi;
+#pragma unroll
+    for (int j = 0; j < M; ++j) xi[j] = xb[((h - a.xi_h0) * M + j) * a.B * a.P + b * a.P + p];
+  }
 }
 
 // Real-space half step h (delta = dt/2) at spatial point p of trajectory b, on the
 // M values u (src/kernels.jl:37-54):
 //   u <- cis(-delta G(u)) V (u + delta/2 F_now) + delta/2 F_next - i sqrt(delta) eta xi
 // G is evaluated on u before the pump is added (src/kernels.jl:40,44).
-// pn/px: pump coefficients (dt/4)a(t_h), (dt/4)a(t_{h+1}), hoisted by the caller.
+// pn/px: pump coefficients (dt/4)a(t_h), (dt/4)a(t_{h+1}).
 template <typename Real, int M>
 __device__ __forceinline__ void half_step(typename CT<Real>::T (&u)[M], const PassArgs& a,
                                           int64_t p, int64_t b, int64_t h,
                                           const typename CT<Real>::T (&pn)[M],
                                           const typename CT<Real>::T (&px)[M]) {
   using C = typename CT<Real>::T;
-  using K = Coef<Real>;
-  const Real dth = K::dth(a);
-  Real dens[M];
-#pragma unroll
-  for (int l = 0; l < M; ++l) dens[l] = u[l].x * u[l].x + u[l].y * u[l].y;
   C E[M];
   bool hasE[M];
+  if constexpr (std::is_same<Real, DWR>::value) {
+    dw dens[M];
 #pragma unroll
-  for (int j = 0; j < M; ++j) {
-    hasE[j] = a.nl_on[j] != 0;
-    if (hasE[j]) {
-      Real gr = K::c(a, j, 0), gi = K::c(a, j, 1);
+    for (int l = 0; l < M; ++l) dens[l] = dot2<+1>(re(u[l]), re(u[l]), im(u[l]), im(u[l]));
+    const dw dth = {a.dthf, a.dthl};
 #pragma unroll
-      for (int l = 0; l < M; ++l) {
-        gr += K::g(a, j, l, 0) * dens[l];
-        gi += K::g(a, j, l, 1) * dens[l];
+    for (int j = 0; j < M; ++j) {
+      hasE[j] = a.nl_on[j] != 0;
+      if (hasE[j]) {
+        dw gr = {a.cf[j][0], a.cl[j][0]};
+#pragma unroll
+        for (int l = 0; l < M; ++l) gr = dw_add_acc(gr, dw_mul({a.gf[j][l][0], a.gl[j][l][0]}, dens[l]));
+        dw s, c;
+        dw_sincos(dw_mul(dth, gr), s, c);
+        if (a.nl_imag[j]) {
+          dw gi = {a.cf[j][1], a.cl[j][1]};
+#pragma unroll
+          for (int l = 0; l < M; ++l) gi = dw_add_acc(gi, dw_mul({a.gf[j][l][1], a.gl[j][l][1]}, dens[l]));
+          const dw mag = dw_from(exp(dw_to_double(dw_mul(dth, gi))));
+          s = dw_mul(s, mag);
+          c = dw_mul(c, mag);
+        }
+        E[j] = mk(c, dw_neg(s));
       }
-      Real s, c;
-      sc<Real>(dth * gr, &s, &c);
-      const Real mag = (gi != (Real)0) ? rexp(dth * gi) : (Real)1;
-      E[j].x = mag * c;
-      E[j].y = -mag * s;
+    }
+  } else {
+    using K = Coef<Real>;
+    const Real dth = K::dth(a);
+    Real dens[M];
+#pragma unroll
+    for (int l = 0; l < M; ++l) dens[l] = u[l].x * u[l].x + u[l].y * u[l].y;
+#pragma unroll
+    for (int j = 0; j < M; ++j) {
+      hasE[j] = a.nl_on[j] != 0;
+      if (hasE[j]) {
+        Real gr = K::c(a, j, 0), gi = K::c(a, j, 1);
+#pragma unroll
+        for (int l = 0; l < M; ++l) {
+          gr += K::g(a, j, l, 0) * dens[l];
+          gi += K::g(a, j, l, 1) * dens[l];
+        }
+        Real s, c;
+        sc<Real>(dth * gr, &s, &c);
+        const Real mag = a.nl_imag[j] ? rexp(dth * gi) : (Real)1;
+        E[j].x = mag * c;
+        E[j].y = -mag * s;
+      }
     }
   }
   if (a.vkind == TAB_SCALAR) {
-    const C v = __ldg((const C*)a.vtab + p);
+    const C v = ldgc((const C*)a.vtab + p);
 #pragma unroll
-    for (int j = 0; j < M; ++j) { E[j] = hasE[j] ? cmul(E[j], v) : v; hasE[j] = true; }
+    for (int j = 0; j < M; ++j) {
+      E[j] = hasE[j] ? cmul(E[j], v) : v;
+      hasE[j] = true;
+    }
   } else if (a.vkind == TAB_DIAG) {
 #pragma unroll
     for (int j = 0; j < M; ++j) {
-      const C v = __ldg((const C*)a.vtab + (int64_t)j * a.P + p);
+      const C v = ldgc((const C*)a.vtab + (int64_t)j * a.P + p);
       E[j] = hasE[j] ? cmul(E[j], v) : v;
       hasE[j] = true;
     }
@@ -140,16 +264,15 @@ __device__ __forceinline__ void half_step(typename CT<Real>::T (&u)[M], const Pa
 #pragma unroll
   for (int j = 0; j < M; ++j) {
     if (a.pprof[j]) {
-      if (a.pprof_cplx) prof[j] = __ldg((const C*)a.pprof[j] + p);
-      else { prof[j].x = __ldg((const Real*)a.pprof[j] + p); prof[j].y = (Real)0; }
+      prof[j] = a.pprof_cplx ? ldgc((const C*)a.pprof[j] + p) : Prof<Real>::cplx(a.pprof[j], p);
       u[j] = cadd(u[j], cmul(pn[j], prof[j]));
     }
   }
   if (a.vkind == TAB_MATRIX && M == 2) {
     // matrix potential with no nonlinearity: mat-vec with the per-point 2x2 table
     const C* vt = (const C*)a.vtab;
-    const C t00 = __ldg(vt + p), t01 = __ldg(vt + a.P + p);
-    const C t10 = __ldg(vt + 2 * a.P + p), t11 = __ldg(vt + 3 * a.P + p);
+    const C t00 = ldgc(vt + p), t01 = ldgc(vt + a.P + p);
+    const C t10 = ldgc(vt + 2 * a.P + p), t11 = ldgc(vt + 3 * a.P + p);
     const C y0 = cadd(cmul(t00, u[0]), cmul(t01, u[M - 1]));
     const C y1 = cadd(cmul(t10, u[0]), cmul(t11, u[M - 1]));
     u[0] = y0;
@@ -164,38 +287,22 @@ __device__ __forceinline__ void half_step(typename CT<Real>::T (&u)[M], const Pa
     if (a.pprof[j]) u[j] = cadd(u[j], cmul(px[j], prof[j]));
   if (a.noise != NOISE_OFF) {
     C xi[M];
-    if (a.noise == NOISE_PHILOX) {
-      const uint4 r = Philox4x32::gen(noise_counter(p, b, h), a.seed_lo, a.seed_hi);
-      xi[0] = BoxMuller<Real>::get(r.x, r.y);
-      if constexpr (M == 2) xi[M - 1] = BoxMuller<Real>::get(r.z, r.w);
-    } else {
-      const C* xb = (const C*)a.xi;
-#pragma unroll
-      for (int j = 0; j < M; ++j) xi[j] = xb[((h - a.xi_h0) * M + j) * a.B * a.P + b * a.P + p];
-    }
+    draw_xi<Real, M>(a, p, b, h, xi);
 #pragma unroll
     for (int j = 0; j < M; ++j) {
       C nf;
-      nf.x = K::nf(a, j, 0);
-      nf.y = K::nf(a, j, 1);
-      if (a.etaprof[j]) nf = cscale(nf, __ldg((const Real*)a.etaprof[j] + p));
+      if constexpr (std::is_same<Real, DWR>::value) {
+        nf = mk({a.nfacf[j][0], a.nfacl[j][0]}, {a.nfacf[j][1], a.nfacl[j][1]});
+        if (a.etaprof[j]) {
+          const float2 e = __ldg((const float2*)a.etaprof[j] + p);
+          nf = cscale(nf, dw{e.x, e.y});
+        }
+      } else {
+        nf.x = Coef<Real>::nf(a, j, 0);
+        nf.y = Coef<Real>::nf(a, j, 1);
+        if (a.etaprof[j]) nf = cscale(nf, __ldg((const Real*)a.etaprof[j] + p));
+      }
       u[j] = cadd(u[j], cmul(nf, xi[j]));
-    }
-  }
-}
-
-template <typename Real, int M>
-__device__ __forceinline__ void load_pump(const PassArgs& a, int64_t h, typename CT<Real>::T (&pn)[M],
-                                          typename CT<Real>::T (&px)[M]) {
-  using C = typename CT<Real>::T;
-#pragma unroll
-  for (int j = 0; j < M; ++j) {
-    if (a.pprof[j] && h >= 0) {
-      pn[j] = pump_coef<C>(a, j, h);
-      px[j] = pump_coef<C>(a, j, h + 1);
-    } else {
-      pn[j] = cmake<C>(0.0, 0.0);
-      px[j] = pn[j];
     }
   }
 }
@@ -206,22 +313,70 @@ __device__ __forceinline__ void kmul(typename CT<Real>::T (&v)[M], const PassArg
   using C = typename CT<Real>::T;
   const C* kt = (const C*)a.ktab;
   if (a.kkind == TAB_SCALAR) {
-    const C k = __ldg(kt + kp);
+    const C k = ldgc(kt + kp);
 #pragma unroll
     for (int m = 0; m < M; ++m) v[m] = cmul(k, v[m]);
   } else if (a.kkind == TAB_DIAG) {
 #pragma unroll
-    for (int m = 0; m < M; ++m) v[m] = cmul(__ldg(kt + (int64_t)m * a.P + kp), v[m]);
+    for (int m = 0; m < M; ++m) v[m] = cmul(ldgc(kt + (int64_t)m * a.P + kp), v[m]);
   } else if (a.kkind == TAB_MATRIX) {
     if constexpr (M == 2) {
-      const C t00 = __ldg(kt + kp), t01 = __ldg(kt + a.P + kp);
-      const C t10 = __ldg(kt + 2 * a.P + kp), t11 = __ldg(kt + 3 * a.P + kp);
+      const C t00 = ldgc(kt + kp), t01 = ldgc(kt + a.P + kp);
+      const C t10 = ldgc(kt + 2 * a.P + kp), t11 = ldgc(kt + 3 * a.P + kp);
       const C y0 = cadd(cmul(t00, v[0]), cmul(t01, v[1]));
       const C y1 = cadd(cmul(t10, v[0]), cmul(t11, v[1]));
       v[0] = y0;
       v[1] = y1;
     } else {
-      v[0] = cmul(__ldg(kt + kp), v[0]);
+      v[0] = cmul(ldgc(kt + kp), v[0]);
+    }
+  }
+}
+
+// Saved states are written in the caller's precision: a double-word state is rounded
+// to FP64 (double2) on the way out.
+template <typename Real>
+__device__ __forceinline__ void store_save(void* base, int64_t idx, const typename CT<Real>::T& v) {
+  if constexpr (std::is_same<Real, DWR>::value) {
+    ((double2*)base)[idx] = make_double2(dw_to_double(re(v)), dw_to_double(im(v)));
+  } else {
+    ((typename CT<Real>::T*)base)[idx] = v;
+  }
+}
+
+// conj in place (the inverse transform is conj o FFT o conj, so each kernel holds a
+// single forward FFT instance)
+template <typename C, int E>
+__device__ __forceinline__ void conj_all(C (&x)[E]) {
+#pragma unroll
+  for (int i = 0; i < E; ++i) {
+    if constexpr (std::is_same<C, dwc>::value) {
+      x[i].yh = -x[i].yh;
+      x[i].yl = -x[i].yl;
+    } else {
+      x[i].y = -x[i].y;
+    }
+  }
+}
+
+// Transform every component's line in place: forward (unnormalised) or inverse (the
+// 1/P is folded into the k-space table).  One FFT instance serves all components and
+// both directions: component 1 is swapped into the slot of component 0 and back.
+template <typename C, int N, int E, int M, class Lay>
+__device__ __forceinline__ void fft_components(C (&x)[M][E], bool inverse, int t, const Lay& lay,
+                                               const C* __restrict__ tw) {
+#pragma unroll 1
+  for (int m = 0; m < M; ++m) {
+    if (inverse) conj_all(x[0]);
+    fft_line<C, N, E, -1>(x[0], t, lay, tw);
+    if (inverse) conj_all(x[0]);
+    if constexpr (M == 2) {
+#pragma unroll
+      for (int i = 0; i < E; ++i) {
+        const C tmp = x[0][i];
+        x[0][i] = x[1][i];
+        x[1][i] = tmp;
+      }
     }
   }
 }
@@ -250,17 +405,18 @@ row_kernel(const PassArgs a, const int64_t nlines) {
   for (int m = 0; m < M; ++m)
 #pragma unroll
     for (int i = 0; i < E; ++i) x[m][i] = ((const C*)a.u[m])[g0 + T * i];
-  if (a.do_ifft) {
-#pragma unroll
-    for (int m = 0; m < M; ++m) fft_line<C, N, E, +1>(x[m], t, lay, tw);
-  }
-  // Both half steps run through ONE instance of half_step (a two-trip loop that is
-  // not unrolled): a half step then rounds identically whether it opens a run (entry
-  // pass) or sits between two steps, so a checkpointed and resumed run reproduces
-  // an uninterrupted one bit for bit.
+  // Phases: 0 inverse FFT_x, 1 half step A (+ save), 2 half step B, 3 forward FFT_x.
+  // The loop is not unrolled, so the kernel holds one FFT and one half-step instance:
+  // a half step rounds identically whether it opens a run (entry pass) or sits
+  // between two steps, and a checkpointed, resumed run reproduces an uninterrupted one
+  // bit for bit.
 #pragma unroll 1
-  for (int half = 0; half < 2; ++half) {
-    const int64_t h = half ? a.hB : a.hA;
+  for (int ph = 0; ph < 4; ++ph) {
+    if (ph == 0 || ph == 3) {
+      if (ph == 0 ? a.do_ifft : a.do_fft) fft_components<C, N, E, M>(x, ph == 0, t, lay, tw);
+      continue;
+    }
+    const int64_t h = ph == 2 ? a.hB : a.hA;
     if (h >= 0) {
       C pn[M], px[M];
       load_pump<Real, M>(a, h, pn, px);
@@ -274,16 +430,12 @@ row_kernel(const PassArgs a, const int64_t nlines) {
         for (int m = 0; m < M; ++m) x[m][i] = v[m];
       }
     }
-    if (half == 0 && a.save[0] && active) {
+    if (ph == 1 && a.save[0] && active) {
 #pragma unroll
       for (int m = 0; m < M; ++m)
 #pragma unroll
-        for (int i = 0; i < E; ++i) ((C*)a.save[m])[g0 + T * i] = x[m][i];
+        for (int i = 0; i < E; ++i) store_save<Real>(a.save[m], g0 + T * i, x[m][i]);
     }
-  }
-  if (a.do_fft) {
-#pragma unroll
-    for (int m = 0; m < M; ++m) fft_line<C, N, E, -1>(x[m], t, lay, tw);
   }
   if (active) {
 #pragma unroll
@@ -319,24 +471,24 @@ col_kernel(const PassArgs a) {
   for (int m = 0; m < M; ++m)
 #pragma unroll
     for (int i = 0; i < E; ++i) x[m][i] = ((const C*)a.u[m])[g0 + step * i];
-  if (a.col_fwd) {
-#pragma unroll
-    for (int m = 0; m < M; ++m) fft_line<C, N, E, -1>(x[m], t, lay, tw);
-  }
-  if (a.ktab) {
-#pragma unroll
-    for (int i = 0; i < E; ++i) {
-      C v[M];
-#pragma unroll
-      for (int m = 0; m < M; ++m) v[m] = x[m][i];
-      kmul<Real, M>(v, a, sp0 + step * i);
-#pragma unroll
-      for (int m = 0; m < M; ++m) x[m][i] = v[m];
+  // phases: 0 forward FFT_y, 1 k-space table, 2 inverse FFT_y (one FFT instance)
+#pragma unroll 1
+  for (int ph = 0; ph < 3; ++ph) {
+    if (ph != 1) {
+      if (ph == 0 ? a.col_fwd : a.col_inv) fft_components<C, N, E, M>(x, ph == 2, t, lay, tw);
+      continue;
     }
-  }
-  if (a.col_inv) {
+    if (a.ktab) {
 #pragma unroll
-    for (int m = 0; m < M; ++m) fft_line<C, N, E, +1>(x[m], t, lay, tw);
+      for (int i = 0; i < E; ++i) {
+        C v[M];
+#pragma unroll
+        for (int m = 0; m < M; ++m) v[m] = x[m][i];
+        kmul<Real, M>(v, a, sp0 + step * i);
+#pragma unroll
+        for (int m = 0; m < M; ++m) x[m][i] = v[m];
+      }
+    }
   }
 #pragma unroll
   for (int m = 0; m < M; ++m)
@@ -346,6 +498,8 @@ col_kernel(const PassArgs a) {
 
 // ------------------------------------------------------------------ 1D resident
 // nlines = B trajectories of one line each; runs a.nsteps full steps in registers.
+// Both half steps of a step share one half_step instance (a non-unrolled loop), like
+// the row pass.
 template <typename Real, int LOGN, int M>
 __global__ void __launch_bounds__(LineCfg<Real, M, LOGN>::ROW_THREADS)
 line1d_kernel(const PassArgs a, const int64_t nlines) {
@@ -369,48 +523,45 @@ line1d_kernel(const PassArgs a, const int64_t nlines) {
     for (int i = 0; i < E; ++i) x[m][i] = ((const C*)a.u[m])[g0 + T * i];
   for (int64_t s = 0; s < a.nsteps; ++s) {
     const int64_t k = a.step0 + s;
-    C pn[M], px[M];
-    load_pump<Real, M>(a, 2 * k, pn, px);
+    // phases: 0 half step 2k, 1 forward FFT, 2 k-space table, 3 inverse FFT,
+    // 4 half step 2k+1 (one FFT and one half-step instance)
+#pragma unroll 1
+    for (int ph = 0; ph < 5; ++ph) {
+      if (ph == 1 || ph == 3) {
+        if (a.ktab) fft_components<C, N, E, M>(x, ph == 3, t, lay, tw);
+      } else if (ph == 2) {
+        if (a.ktab) {
 #pragma unroll
-    for (int i = 0; i < E; ++i) {
-      C v[M];
+          for (int i = 0; i < E; ++i) {
+            C v[M];
 #pragma unroll
-      for (int m = 0; m < M; ++m) v[m] = x[m][i];
-      half_step<Real, M>(v, a, t + T * i, b, 2 * k, pn, px);
+            for (int m = 0; m < M; ++m) v[m] = x[m][i];
+            kmul<Real, M>(v, a, t + T * i);
 #pragma unroll
-      for (int m = 0; m < M; ++m) x[m][i] = v[m];
-    }
-    if (a.ktab) {
+            for (int m = 0; m < M; ++m) x[m][i] = v[m];
+          }
+        }
+      } else {
+        const int64_t h = 2 * k + (ph == 4 ? 1 : 0);
+        C pn[M], px[M];
+        load_pump<Real, M>(a, h, pn, px);
 #pragma unroll
-      for (int m = 0; m < M; ++m) fft_line<C, N, E, -1>(x[m], t, lay, tw);
+        for (int i = 0; i < E; ++i) {
+          C v[M];
 #pragma unroll
-      for (int i = 0; i < E; ++i) {
-        C v[M];
+          for (int m = 0; m < M; ++m) v[m] = x[m][i];
+          half_step<Real, M>(v, a, t + T * i, b, h, pn, px);
 #pragma unroll
-        for (int m = 0; m < M; ++m) v[m] = x[m][i];
-        kmul<Real, M>(v, a, t + T * i);
-#pragma unroll
-        for (int m = 0; m < M; ++m) x[m][i] = v[m];
+          for (int m = 0; m < M; ++m) x[m][i] = v[m];
+        }
       }
-#pragma unroll
-      for (int m = 0; m < M; ++m) fft_line<C, N, E, +1>(x[m], t, lay, tw);
-    }
-    load_pump<Real, M>(a, 2 * k + 1, pn, px);
-#pragma unroll
-    for (int i = 0; i < E; ++i) {
-      C v[M];
-#pragma unroll
-      for (int m = 0; m < M; ++m) v[m] = x[m][i];
-      half_step<Real, M>(v, a, t + T * i, b, 2 * k + 1, pn, px);
-#pragma unroll
-      for (int m = 0; m < M; ++m) x[m][i] = v[m];
     }
     if (a.save_every > 0 && ((s + 1) % a.save_every) == 0 && active) {
       const int64_t slot = (s + 1) / a.save_every - 1;
 #pragma unroll
       for (int m = 0; m < M; ++m)
 #pragma unroll
-        for (int i = 0; i < E; ++i) ((C*)a.save[m])[slot * a.save_stride + g0 + T * i] = x[m][i];
+        for (int i = 0; i < E; ++i) store_save<Real>(a.save[m], slot * a.save_stride + g0 + T * i, x[m][i]);
     }
   }
   if (active) {
@@ -433,16 +584,17 @@ __global__ void __launch_bounds__(256) nl_only_kernel(const PassArgs a) {
 #pragma unroll
     for (int m = 0; m < M; ++m) v[m] = ((const C*)a.u[m])[q];
     for (int64_t s = 0; s < a.nsteps; ++s) {
-      const int64_t k = a.step0 + s;
-      C pn[M], px[M];
-      load_pump<Real, M>(a, 2 * k, pn, px);
-      half_step<Real, M>(v, a, p, b, 2 * k, pn, px);
-      load_pump<Real, M>(a, 2 * k + 1, pn, px);
-      half_step<Real, M>(v, a, p, b, 2 * k + 1, pn, px);
+#pragma unroll 1
+      for (int half = 0; half < 2; ++half) {
+        const int64_t h = 2 * (a.step0 + s) + half;
+        C pn[M], px[M];
+        load_pump<Real, M>(a, h, pn, px);
+        half_step<Real, M>(v, a, p, b, h, pn, px);
+      }
       if (a.save_every > 0 && ((s + 1) % a.save_every) == 0) {
         const int64_t slot = (s + 1) / a.save_every - 1;
 #pragma unroll
-        for (int m = 0; m < M; ++m) ((C*)a.save[m])[slot * a.save_stride + q] = v[m];
+        for (int m = 0; m < M; ++m) store_save<Real>(a.save[m], slot * a.save_stride + q, v[m]);
       }
     }
 #pragma unroll
@@ -451,6 +603,14 @@ __global__ void __launch_bounds__(256) nl_only_kernel(const PassArgs a) {
 }
 
 // ------------------------------------------------------------------ FP64 norm
+template <typename C> __device__ __forceinline__ double abs2d(const C& v) {
+  return (double)v.x * (double)v.x + (double)v.y * (double)v.y;
+}
+template <> __device__ __forceinline__ double abs2d<dwc>(const dwc& v) {
+  const double x = dw_to_double(re(v)), y = dw_to_double(im(v));
+  return x * x + y * y;
+}
+
 template <typename Real, int M>
 __global__ void __launch_bounds__(256) norm_kernel(const PassArgs a, double* out) {
   using C = typename CT<Real>::T;
@@ -461,10 +621,7 @@ __global__ void __launch_bounds__(256) norm_kernel(const PassArgs a, double* out
   for (int m = 0; m < M; ++m) acc[m] = 0.0;
   for (int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; q < total; q += (int64_t)gridDim.x * blockDim.x) {
 #pragma unroll
-    for (int m = 0; m < M; ++m) {
-      const C v = ((const C*)a.u[m])[q];
-      acc[m] += (double)v.x * (double)v.x + (double)v.y * (double)v.y;
-    }
+    for (int m = 0; m < M; ++m) acc[m] += abs2d(((const C*)a.u[m])[q]);
   }
 #pragma unroll
   for (int m = 0; m < M; ++m) {
@@ -565,11 +722,13 @@ int launch_norm_t(const PassArgs& a, double* out, cudaStream_t s) {
   return (int)cudaGetLastError();
 }
 
-#define GPE_INSTANTIATE(REAL, MM)                                                            \
-  template int launch_row_t<REAL, MM>(int, const PassArgs&, int64_t, cudaStream_t);         \
-  template int launch_col_t<REAL, MM>(int, const PassArgs&, cudaStream_t);                  \
-  template int launch_line1d_t<REAL, MM>(int, const PassArgs&, cudaStream_t);               \
-  template int launch_nl_only_t<REAL, MM>(const PassArgs&, cudaStream_t);                   \
+#define GPE_INSTANTIATE_ROW(REAL, MM) \
+  template int launch_row_t<REAL, MM>(int, const PassArgs&, int64_t, cudaStream_t);
+#define GPE_INSTANTIATE_COL(REAL, MM) \
+  template int launch_col_t<REAL, MM>(int, const PassArgs&, cudaStream_t);
+#define GPE_INSTANTIATE_OTHER(REAL, MM)                                           \
+  template int launch_line1d_t<REAL, MM>(int, const PassArgs&, cudaStream_t);    \
+  template int launch_nl_only_t<REAL, MM>(const PassArgs&, cudaStream_t);        \
   template int launch_norm_t<REAL, MM>(const PassArgs&, double*, cudaStream_t);
 
 }  // namespace gpe

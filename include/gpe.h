@@ -47,8 +47,14 @@ extern "C" {
 #define GPE_ERR_NOMEM (-6)       /* device allocation failed */
 
 /* field precision */
-#define GPE_C128 0 /* ComplexF64 fields, FP64 arithmetic */
+#define GPE_C128 0 /* ComplexF64 fields, FP64-accurate arithmetic (see GPE_FLAG_FP64_NATIVE) */
 #define GPE_C64 1  /* ComplexF32 fields, FP32 arithmetic, FP64 tables/time built on host */
+
+/* gpe_desc.flags */
+/* GPE_C128 runs by default on the FP32 pipes in double-word arithmetic (pairs of floats,
+ * 48-bit significands, unit roundoff 2^-48): GB300 issues FP32 FMAs 62x faster than FP64
+ * ones.  With this flag the passes use native FP64 instead. */
+#define GPE_FLAG_FP64_NATIVE 1
 
 /* table kinds: what the user closure returned per grid point */
 #define GPE_TABLE_NONE 0
@@ -74,7 +80,7 @@ typedef struct gpe_desc {
   double dt;           /* the resolved step (src/fixed_time_stepping.jl:19-21) */
   double t0;           /* tspan[1] */
   int32_t device;      /* CUDA device ordinal; -1 = the calling thread's current device */
-  int32_t flags;       /* reserved, 0 */
+  int32_t flags;       /* GPE_FLAG_* bits, 0 by default */
 } gpe_desc;
 
 /* Solver state apart from the fields: enough to resume bit-identically. */

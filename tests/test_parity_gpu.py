@@ -16,14 +16,19 @@ from cases import c_order, jl, kerr2d, polariton2d
 pytestmark = pytest.mark.gpu
 
 TOL = {np.complex128: 1e-10, np.complex64: 1e-5}
+# FP64 fields run in double-word arithmetic by default ("dw") or in native FP64
+FP64_MODES = ["dw", "native"]
+PRECISIONS = [(np.complex128, "dw"), (np.complex128, "native"), (np.complex64, "dw")]
+PREC_IDS = ["c128-dw", "c128-native", "c64"]
 
 
-def run_both(gpe, oracle, gpu_kw, orc, tspan, dt, nsaves, save_start=True, xi=None, rng=None):
+def run_both(gpe, oracle, gpu_kw, orc, tspan, dt, nsaves, save_start=True, xi=None, rng=None, fp64="dw"):
     prob = gpe.GrossPitaevskiiProblem(**gpu_kw)
     kw = {}
     if xi is not None:
         kw["noise_replay"] = lambda h: np.ascontiguousarray(xi(h))
-    ts, res = gpe.solve(prob, gpe.StrangSplitting(), tspan, dt=dt, nsaves=nsaves, save_start=save_start, rng=rng, **kw)
+    ts, res = gpe.solve(prob, gpe.StrangSplitting(), tspan, dt=dt, nsaves=nsaves, save_start=save_start, rng=rng,
+                        fp64=fp64, **kw)
     ots, ores = oracle.solve(orc, tspan, dt, nsaves, save_start=save_start, xi_source=xi)
     return ts, res, ots, ores
 
@@ -51,12 +56,12 @@ def assert_close(oracle, res, ores, tol, per_save=True):
                     assert e <= tol, f"component {m} save {s}: rel L2 {e:.3e} > {tol:g}"
 
 
-@pytest.mark.parametrize("dtype", [np.complex128, np.complex64])
-def test_kerr_plain_case(gpe, oracle, lib, dtype):
+@pytest.mark.parametrize("dtype,fp64", PRECISIONS, ids=PREC_IDS)
+def test_kerr_plain_case(gpe, oracle, lib, dtype, fp64):
     """2D Kerr 128^2, L=8, g=-6, dt=0.01 on [0, 0.4] with 64 saves: dt resolves to
     0.00625 and 64 steps (src/fixed_time_stepping.jl:14-24)."""
     gpu_kw, orc = kerr2d(128, 8.0, -6.0, dtype)
-    ts, res, ots, ores = run_both(gpe, oracle, gpu_kw, orc, (0.0, 0.4), 0.01, 64)
+    ts, res, ots, ores = run_both(gpe, oracle, gpu_kw, orc, (0.0, 0.4), 0.01, 64, fp64=fp64)
     assert np.array_equal(ts, ots)
     assert len(ts) == 65 and res[0].shape == (128, 128, 65)
     if dtype == np.complex128:
@@ -68,13 +73,13 @@ def test_kerr_plain_case(gpe, oracle, lib, dtype):
         assert_close(oracle, res, ores, tol, per_save=False)
 
 
-@pytest.mark.parametrize("dtype", [np.complex128, np.complex64])
-def test_polariton_matrix_dispersion_pump_ramp(gpe, oracle, lib, dtype):
+@pytest.mark.parametrize("dtype,fp64", PRECISIONS, ids=PREC_IDS)
+def test_polariton_matrix_dispersion_pump_ramp(gpe, oracle, lib, dtype, fp64):
     """Two components, 2x2 matrix dispersion table, diagonal nonlinearity, pump with a
     linear ramp sampled at the reference's shifted pump times."""
     gpu_kw, orc = polariton2d(N=128, L=256.0, A=5.0, ramp=20.0)
     gpu_kw["u0"] = tuple(u.astype(dtype) for u in gpu_kw["u0"])
-    ts, res, ots, ores = run_both(gpe, oracle, gpu_kw, orc, (0.0, 10.0), 0.05, 10)
+    ts, res, ots, ores = run_both(gpe, oracle, gpu_kw, orc, (0.0, 10.0), 0.05, 10, fp64=fp64)
     assert np.array_equal(ts, ots)
     if dtype == np.complex128:
         assert_close(oracle, res, ores, TOL[dtype])
@@ -83,14 +88,16 @@ def test_polariton_matrix_dispersion_pump_ramp(gpe, oracle, lib, dtype):
         assert_close(oracle, res, ores, fp32_tol(oracle, orc, (0.0, 10.0), 0.05, 10), per_save=False)
 
 
-@pytest.mark.parametrize("N", [16, 32, 64, 256, 512])
-def test_kerr_sizes(gpe, oracle, lib, N):
+@pytest.mark.parametrize("fp64", FP64_MODES)
+@pytest.mark.parametrize("N", [16, 32, 64, 256, 512, 1024])
+def test_kerr_sizes(gpe, oracle, lib, N, fp64):
     gpu_kw, orc = kerr2d(N, 8.0, -2.0, np.complex128)
-    ts, res, ots, ores = run_both(gpe, oracle, gpu_kw, orc, (0.0, 0.05), 0.005, 2)
+    ts, res, ots, ores = run_both(gpe, oracle, gpu_kw, orc, (0.0, 0.05), 0.005, 2, fp64=fp64)
     assert_close(oracle, res, ores, 1e-10)
 
 
-def test_rectangular_and_batch(gpe, oracle, lib):
+@pytest.mark.parametrize("fp64", FP64_MODES)
+def test_rectangular_and_batch(gpe, oracle, lib, fp64):
     L = (8.0, 4.0)
     X, Y = oracle.mesh(oracle.grids(L, (64, 32))[0])  # C order (32, 64)
     rng = np.random.default_rng(0)
@@ -100,13 +107,14 @@ def test_rectangular_and_batch(gpe, oracle, lib):
     gkw = dict(u0=(jl(u0c),), lengths=L, dispersion=disp, nonlinearity=lambda u, p: (1.5 - 0.1j) * np.abs(u[0]) ** 2 + 0.3)
     orc = oracle.OracleProblem(u0=(u0c,), lengths=L, dispersion=disp, nonlin_g=np.array([[1.5 - 0.1j]]),
                                nonlin_c=np.array([0.3]))
-    ts, res, ots, ores = run_both(gpe, oracle, gkw, orc, (0.0, 0.3), 0.01, 3)
+    ts, res, ots, ores = run_both(gpe, oracle, gkw, orc, (0.0, 0.3), 0.01, 3, fp64=fp64)
     assert res[0].shape == (64, 32, 3, 4)
     assert_close(oracle, res, ores, 1e-10)
 
 
+@pytest.mark.parametrize("fp64", FP64_MODES)
 @pytest.mark.parametrize("kind", ["scalar", "diag"])
-def test_potential_tables(gpe, oracle, lib, kind):
+def test_potential_tables(gpe, oracle, lib, kind, fp64):
     N, L = 64, 10.0
     (X, Y), _ = (oracle.mesh(oracle.grids((L, L), (N, N))[0]), None)
     u0c = (np.exp(-((X - 5) ** 2 + (Y - 5) ** 2) / 2) + 0j)
@@ -123,12 +131,12 @@ def test_potential_tables(gpe, oracle, lib, kind):
     odisp = lambda k, p: np.stack([(k[0] ** 2 + k[1] ** 2) / 2, (k[0] ** 2 + k[1] ** 2) / 4])
     opot = pot if kind == "scalar" else (lambda r, p: np.stack([np.asarray(v) * np.ones_like(r[0]) for v in pot(r, p)]))
     orc = oracle.OracleProblem(u0=(u0c, u1c), lengths=(L, L), dispersion=odisp, potential=opot, nonlin_g=g)
-    ts, res, ots, ores = run_both(gpe, oracle, gkw, orc, (0.0, 0.2), 0.01, 4)
+    ts, res, ots, ores = run_both(gpe, oracle, gkw, orc, (0.0, 0.2), 0.01, 4, fp64=fp64)
     assert_close(oracle, res, ores, 1e-10)
 
 
-@pytest.mark.parametrize("dtype", [np.complex128, np.complex64])
-def test_noise_replay_2d(gpe, oracle, lib, dtype):
+@pytest.mark.parametrize("dtype,fp64", PRECISIONS, ids=PREC_IDS)
+def test_noise_replay_2d(gpe, oracle, lib, dtype, fp64):
     """Replay mode feeds the same xi to both sides: identical dW."""
     N, L, B = 32, 16.0, 3
     rng = np.random.default_rng(11)
@@ -144,12 +152,13 @@ def test_noise_replay_2d(gpe, oracle, lib, dtype):
                                eta=np.array([eta]))
     rn = oracle.ReplayNoise(5, (1, B, N, N))
     xi = (lambda h: rn(h).astype(np.complex64).astype(np.complex128)) if dtype == np.complex64 else rn
-    ts, res, ots, ores = run_both(gpe, oracle, gkw, orc, (0.0, 0.4), 0.02, 4, xi=xi)
+    ts, res, ots, ores = run_both(gpe, oracle, gkw, orc, (0.0, 0.4), 0.02, 4, xi=xi, fp64=fp64)
     tol = TOL[dtype] if dtype == np.complex128 else fp32_tol(oracle, orc, (0.0, 0.4), 0.02, 4, xi=xi)
     assert_close(oracle, res, ores, tol, per_save=dtype == np.complex128)
 
 
-def test_noise_philox_matches_restatement(gpe, oracle, lib):
+@pytest.mark.parametrize("fp64", FP64_MODES)
+def test_noise_philox_matches_restatement(gpe, oracle, lib, fp64):
     """Philox mode: the in-kernel draws equal the CPU restatement of Philox4x32-10 +
     Box-Muller, so FP64 results agree with the oracle to 1e-10."""
     N, L, B = 32, 16.0, 2
@@ -161,12 +170,13 @@ def test_noise_philox_matches_restatement(gpe, oracle, lib):
     seed = 0x1234_5678_9ABC
     xi = oracle.PhiloxNoise(seed, 1, (B,), (N, N))
     prob = gpe.GrossPitaevskiiProblem(**gkw)
-    ts, res = gpe.solve(prob, gpe.StrangSplitting(), (0.0, 0.2), dt=0.02, nsaves=2, rng=seed)
+    ts, res = gpe.solve(prob, gpe.StrangSplitting(), (0.0, 0.2), dt=0.02, nsaves=2, rng=seed, fp64=fp64)
     ots, ores = oracle.solve(orc, (0.0, 0.2), 0.02, 2, xi_source=xi)
     assert_close(oracle, res, ores, 1e-10)
 
 
-def test_1d_bistability_segment(gpe, oracle, lib):
+@pytest.mark.parametrize("fp64", FP64_MODES)
+def test_1d_bistability_segment(gpe, oracle, lib, fp64):
     """1D driven-dissipative line (the reference's bistability problem), a short
     segment of its ramp: resident 1D kernel vs oracle."""
     w0, g, d, kz, gam, L, N = 1483.0, 0.01, 0.3, 27.0, 0.1, 256.0, 256
@@ -182,11 +192,12 @@ def test_1d_bistability_segment(gpe, oracle, lib):
     orc = oracle.OracleProblem(u0=(np.zeros(N, np.complex128),), lengths=(L,), dispersion=disp,
                                nonlin_g=np.array([[g]]), pump_profile=prof[None].astype(np.complex128),
                                pump_amp=lambda t: np.array([np.sqrt(I(t))]))
-    ts, res, ots, ores = run_both(gpe, oracle, gkw, orc, (0.0, 300.0), 0.05, 20)
+    ts, res, ots, ores = run_both(gpe, oracle, gkw, orc, (0.0, 300.0), 0.05, 20, fp64=fp64)
     assert_close(oracle, res, ores, 1e-10)
 
 
-def test_1d_batch_noise_replay(gpe, oracle, lib):
+@pytest.mark.parametrize("fp64", FP64_MODES)
+def test_1d_batch_noise_replay(gpe, oracle, lib, fp64):
     """1D, 200 trajectories with position noise (the windowed-FT test's shape)."""
     N, L, B = 64, 20.0, 200
     hb = 0.6582
@@ -198,13 +209,41 @@ def test_1d_batch_noise_replay(gpe, oracle, lib):
     gkw = dict(u0=(jl(u0c),), lengths=(L,), dispersion=disp, position_noise_func=lambda u, r, p: eta)
     orc = oracle.OracleProblem(u0=(u0c,), lengths=(L,), dispersion=disp, eta=np.array([eta]))
     xi = oracle.ReplayNoise(9, (1, B, N))
-    ts, res, ots, ores = run_both(gpe, oracle, gkw, orc, (0.0, 40.0), 4.0, 1, save_start=False, xi=xi)
+    ts, res, ots, ores = run_both(gpe, oracle, gkw, orc, (0.0, 40.0), 4.0, 1, save_start=False, xi=xi, fp64=fp64)
     assert res[0].shape == (64, 200, 1)
     assert_close(oracle, res, ores, 1e-10)
 
 
-def test_resume_is_bit_identical(gpe, oracle, lib):
-    """Checkpoint (fields + gpe_state) and resume equals an uninterrupted run."""
+@pytest.mark.parametrize("dtype,fp64", [(np.complex128, "native"), (np.complex64, "dw")], ids=["c128-native", "c64"])
+def test_resume_is_bit_identical(gpe, oracle, lib, dtype, fp64):
+    """Checkpoint (fields + gpe_state) and resume equals an uninterrupted run.  (The
+    double-word state is rounded to FP64 when read out, so its checkpoints resume to
+    within one FP64 rounding; see test_resume_double_word.)"""
+    gpu_kw, _ = kerr2d(64, 8.0, -3.0, dtype)
+    gpu_kw["position_noise_func"] = lambda u, r, p: 0.05
+    prob = gpe.GrossPitaevskiiProblem(**gpu_kw)
+    kw = dict(fp64=fp64)
+    it = gpe.init(prob, gpe.StrangSplitting(), (0.0, 0.2), dt=0.01, nsaves=1, rng=77, **kw)
+    it.step(20)
+    full = it.get_fields()[0].copy()
+    it.close()
+    it1 = gpe.init(prob, gpe.StrangSplitting(), (0.0, 0.2), dt=0.01, nsaves=1, rng=77, **kw)
+    it1.step(8)
+    st = it1.state()
+    f = it1.get_fields()
+    it1.close()
+    it2 = gpe.init(prob, gpe.StrangSplitting(), (0.0, 0.2), dt=0.01, nsaves=1, rng=77, **kw)
+    it2.set_fields(f)
+    it2.set_state(st)
+    it2.step(12)
+    resumed = it2.get_fields()[0]
+    it2.close()
+    assert np.array_equal(full, resumed)
+
+
+def test_resume_double_word(gpe, oracle, lib):
+    """Double-word state: a resumed run agrees with an uninterrupted one to 1e-13 (the
+    checkpoint holds the FP64 rounding of the 48-bit state)."""
     gpu_kw, _ = kerr2d(64, 8.0, -3.0, np.complex128)
     gpu_kw["position_noise_func"] = lambda u, r, p: 0.05
     prob = gpe.GrossPitaevskiiProblem(**gpu_kw)
@@ -214,8 +253,7 @@ def test_resume_is_bit_identical(gpe, oracle, lib):
     it.close()
     it1 = gpe.init(prob, gpe.StrangSplitting(), (0.0, 0.2), dt=0.01, nsaves=1, rng=77)
     it1.step(8)
-    st = it1.state()
-    f = it1.get_fields()
+    st, f = it1.state(), it1.get_fields()
     it1.close()
     it2 = gpe.init(prob, gpe.StrangSplitting(), (0.0, 0.2), dt=0.01, nsaves=1, rng=77)
     it2.set_fields(f)
@@ -223,13 +261,14 @@ def test_resume_is_bit_identical(gpe, oracle, lib):
     it2.step(12)
     resumed = it2.get_fields()[0]
     it2.close()
-    assert np.array_equal(full, resumed)
+    assert oracle.rel_l2(resumed, full) <= 1e-13
 
 
-def test_norm_matches_oracle(gpe, oracle, lib):
+@pytest.mark.parametrize("fp64", FP64_MODES)
+def test_norm_matches_oracle(gpe, oracle, lib, fp64):
     gpu_kw, orc = kerr2d(64, 8.0, -3.0, np.complex128)
     prob = gpe.GrossPitaevskiiProblem(**gpu_kw)
-    it = gpe.init(prob, gpe.StrangSplitting(), (0.0, 0.1), dt=0.01, nsaves=1)
+    it = gpe.init(prob, gpe.StrangSplitting(), (0.0, 0.1), dt=0.01, nsaves=1, fp64=fp64)
     it.step(5)
     nrm = it.norm()
     u = c_order(it.get_fields()[0])
