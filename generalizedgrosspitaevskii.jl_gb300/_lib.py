@@ -6,6 +6,7 @@ fails loudly when the library is missing: there is no CPU fallback.
 from __future__ import annotations
 
 import ctypes
+import os
 from ctypes import POINTER, c_char_p, c_double, c_int, c_int32, c_int64, c_uint64, c_void_p
 from pathlib import Path
 
@@ -109,7 +110,7 @@ def load(path: Path | str | None = None):
     global _lib
     if _lib is not None and path is None:
         return _lib
-    p = Path(path) if path else LIB_PATH
+    p = Path(path) if path else Path(os.environ.get("GPE_LIB", LIB_PATH))
     if not p.exists():
         raise RuntimeError(
             f"{p} is missing: build it first (python -c 'import __graft_entry__ as g; g.build()'); "

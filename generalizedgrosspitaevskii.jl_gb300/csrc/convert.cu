@@ -4,7 +4,8 @@
 
 namespace gpe {
 
-__global__ void f64_to_dw_kernel(const double2* __restrict__ src, dwc* __restrict__ dst, int64_t n) {
+// src and dst may be the same buffer: each element is read before it is written.
+__global__ void f64_to_dw_kernel(const double2* src, dwc* dst, int64_t n) {
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
     const double2 v = src[i];
     dst[i] = mk(dw_from(v.x), dw_from(v.y));

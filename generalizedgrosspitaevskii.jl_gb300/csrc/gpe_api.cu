@@ -782,6 +782,9 @@ static int run_common(gpe_handle* h, int64_t nsteps, int64_t save_every, void* o
     int rc = ensure(h, &h->xi_buf, &h->xi_cap, xb);
     if (rc) return rc;
     CK(h, cudaMemcpy(h->xi_buf, xi_host, xb, cudaMemcpyHostToDevice));
+    // replayed draws arrive as FP64; a double-word state needs them split (in place:
+    // both layouts take 16 bytes per complex number)
+    if (h->prec == gpe::PREC_DW) LK(h, gpe::launch_f64_to_dw(h->xi_buf, h->xi_buf, (int64_t)(xb / 16), h->stream));
   }
   void* save_dev = nullptr;
   if (nsaves > 0) {

@@ -43,6 +43,10 @@ struct LineCfg {
   static constexpr int SMEM_LIMIT = 200 * 1024;
   static constexpr int CC = cmax(1, cmin(cmin(CCMAX, cmax(1, TPB / T)), pow2floor(SMEM_LIMIT / (N * (int)sizeof(C)))));
   static constexpr int ROW_THREADS = L * TR;
+#ifndef GPE_ROW_MIN_BLOCKS
+#define GPE_ROW_MIN_BLOCKS 2
+#endif
+  static constexpr int ROW_MINB = GPE_ROW_MIN_BLOCKS;
   static constexpr int COL_THREADS = CC * T;
   static constexpr size_t ROW_SMEM = (size_t)L * N * sizeof(C);
   static constexpr size_t COL_SMEM = (size_t)CC * N * sizeof(C);
@@ -381,9 +385,35 @@ __device__ __forceinline__ void fft_components(C (&x)[M][E], bool inverse, int t
   }
 }
 
+// Half step h on the E points a thread holds (points p0 + T*i).  The point loop is not
+// unrolled, so the kernel holds one copy of the half step (the double-word step is
+// several hundred instructions; eight unrolled copies overflow the instruction cache).
+// Registers cannot be indexed at run time, so each trip works on x[.][0] and rotates
+// the arrays by one; after E trips they are back in order.
+template <typename Real, int M, int E>
+__device__ __forceinline__ void half_points(typename CT<Real>::T (&x)[M][E], const PassArgs& a, int64_t p0, int T,
+                                            int64_t b, int64_t h) {
+  using C = typename CT<Real>::T;
+  C pn[M], px[M];
+  load_pump<Real, M>(a, h, pn, px);
+#pragma unroll 1
+  for (int i = 0; i < E; ++i) {
+    C v[M];
+#pragma unroll
+    for (int m = 0; m < M; ++m) v[m] = x[m][0];
+    half_step<Real, M>(v, a, p0 + (int64_t)T * i, b, h, pn, px);
+#pragma unroll
+    for (int m = 0; m < M; ++m) {
+#pragma unroll
+      for (int q = 0; q + 1 < E; ++q) x[m][q] = x[m][q + 1];
+      x[m][E - 1] = v[m];
+    }
+  }
+}
+
 // ------------------------------------------------------------------ row pass
 template <typename Real, int LOGN, int M>
-__global__ void __launch_bounds__(LineCfg<Real, M, LOGN>::ROW_THREADS)
+__global__ void __launch_bounds__(LineCfg<Real, M, LOGN>::ROW_THREADS, LineCfg<Real, M, LOGN>::ROW_MINB)
 row_kernel(const PassArgs a, const int64_t nlines) {
   using Cfg = LineCfg<Real, M, LOGN>;
   using C = typename CT<Real>::T;
@@ -417,19 +447,7 @@ row_kernel(const PassArgs a, const int64_t nlines) {
       continue;
     }
     const int64_t h = ph == 2 ? a.hB : a.hA;
-    if (h >= 0) {
-      C pn[M], px[M];
-      load_pump<Real, M>(a, h, pn, px);
-#pragma unroll
-      for (int i = 0; i < E; ++i) {
-        C v[M];
-#pragma unroll
-        for (int m = 0; m < M; ++m) v[m] = x[m][i];
-        half_step<Real, M>(v, a, p0 + T * i, b, h, pn, px);
-#pragma unroll
-        for (int m = 0; m < M; ++m) x[m][i] = v[m];
-      }
-    }
+    if (h >= 0) half_points<Real, M, E>(x, a, p0, T, b, h);
     if (ph == 1 && a.save[0] && active) {
 #pragma unroll
       for (int m = 0; m < M; ++m)
@@ -542,18 +560,7 @@ line1d_kernel(const PassArgs a, const int64_t nlines) {
           }
         }
       } else {
-        const int64_t h = 2 * k + (ph == 4 ? 1 : 0);
-        C pn[M], px[M];
-        load_pump<Real, M>(a, h, pn, px);
-#pragma unroll
-        for (int i = 0; i < E; ++i) {
-          C v[M];
-#pragma unroll
-          for (int m = 0; m < M; ++m) v[m] = x[m][i];
-          half_step<Real, M>(v, a, t + T * i, b, h, pn, px);
-#pragma unroll
-          for (int m = 0; m < M; ++m) x[m][i] = v[m];
-        }
+        half_points<Real, M, E>(x, a, t, T, b, 2 * k + (ph == 4 ? 1 : 0));
       }
     }
     if (a.save_every > 0 && ((s + 1) % a.save_every) == 0 && active) {
