@@ -100,6 +100,8 @@ SIGNATURES = {
     "gpe_kernel_times": (c_int, [H, c_void_p, c_void_p]),
     "gpe_last_run_ms": (c_double, [H]),
     "gpe_last_run_launches": (c_int64, [H]),
+    "gpe_norms_noalloc": (c_int, [c_void_p, c_int, c_int64, c_int64, c_int, c_double, c_void_p]),
+    "gpe_noalloc_last_error": (c_char_p, []),
 }
 
 _lib = None

@@ -184,6 +184,29 @@ double gpe_last_run_ms(const gpe_handle* h);
 /* Number of kernels launched by the last gpe_run* call. */
 int64_t gpe_last_run_launches(const gpe_handle* h);
 
+/* ---- allocation-free entry point ---------------------------------------- */
+/* No counterpart in the reference: an addition for callers that cannot allocate device
+ * memory (their device memory belongs to another allocator, such as a framework's
+ * caching pool or a budget fixed at start-up, or they run where cudaMalloc's implicit
+ * device synchronisation is not acceptable).
+ *
+ * out_host[m*ntraj + b] = dV * sum over the npoints values of trajectory b of
+ * |fields_dev[m]|^2, for ncomp (1 or 2) caller-owned device arrays of ntraj*npoints
+ * complex numbers (GPE_C128: double2, GPE_C64: float2), reduced in FP64.  The only
+ * scratch is a static device array of GPE_NOALLOC_MAX_NORMS doubles that the library
+ * holds on every GPU that loads it; ncomp * ntraj above that limit (or ntraj above
+ * 65535) is rejected with GPE_ERR_INVALID.  Nothing is allocated: no cudaMalloc, no
+ * cudaFree, no allocating library routine.  The first call on a device looks up the
+ * array's device address (cudaGetSymbolAddress, with that device current), so make it
+ * before any stream capture.  The call is synchronous on the legacy default stream.
+ * Every call shares the one array and overwrites the slots it uses, so calls that
+ * overlap on the GPU (from several host threads or streams) race.  Errors are
+ * described by gpe_noalloc_last_error() (per host thread). */
+#define GPE_NOALLOC_MAX_NORMS 8192
+int gpe_norms_noalloc(const void* const* fields_dev, int ncomp, int64_t npoints, int64_t ntraj,
+                      int dtype, double dV, double* out_host);
+const char* gpe_noalloc_last_error(void);
+
 #ifdef __cplusplus
 }
 #endif
