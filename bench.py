@@ -342,7 +342,57 @@ def run_gpu(args, rank, world, local_rank):
     }
     if not args.no_cpu:
         line["cpu_baseline"] = cpu_baseline()
+    if args.twa_steps > 0:
+        line["twa"] = run_twa(pkg, args.twa_steps, tune=not args.no_tune)
     print(json.dumps(line), flush=True)
+
+
+TWA_GROUPS = [(64, 342), (128, 341), (256, 341)]  # 1024 trajectories over three grids
+
+
+def run_twa(pkg, steps: int, tune: bool):
+    """Batched truncated-Wigner ensemble: 1024 trajectories of the damped-driven scalar
+    field split 342/341/341 over 64^2, 128^2 and 256^2 grids (L=64, D=|k|^2/2 - 0.1i,
+    g=0.01, F=1, eta=sqrt(gamma/(2 dV)), Philox noise, FP32 fields with FP64-built tables),
+    advanced by one CUDA graph.  Against: the plain per-trajectory form (one trajectory per
+    handle, two-pass path, run one after another) timed on a sample and scaled."""
+    T = sys.modules.get("gpe_gb300.twa") or __import__("gpe_gb300.twa", fromlist=["Ensemble"])
+    A = __import__("gpe_gb300.autotune", fromlist=["tune"])
+    prm = T.DampedDrivenParams()
+    chunk = 50
+    choices = {}
+    its = []
+    for N, B in TWA_GROUPS:
+        resident = True
+        if tune:
+            k = A.key(N, 1, "c64", B, A.gpu_name())
+            resident, chunk_n, _ = A.tune(lambda r, N=N, B=B: T.make_group(N, B, prm, 400, seed=N, resident=r), k,
+                                          trial_steps=200)
+            choices[f"{N}x{N}"] = {"resident": resident, "steps_per_graph": chunk_n}
+        its.append(T.make_group(N, B, prm, steps + 2 * chunk, seed=N, resident=resident))
+    ens = T.Ensemble(its)
+    ens.run(chunk, chunk)  # capture + warm-up
+    ens.run(steps, chunk)
+    ms = ens.last_run_ms()
+    launches = ens.last_run_launches()
+    ens.close()
+    for it in its:
+        it.close()
+    ntraj = sum(B for _, B in TWA_GROUPS)
+    value = ntraj * steps / (ms * 1e-3)
+    # plain per-trajectory form on a sample: 3 trajectories x 100 steps per grid size
+    t_plain = 0.0
+    for N, B in TWA_GROUPS:
+        rate = T.plain_per_trajectory_rate(N, prm, 3, 100, seed=N)
+        t_plain += B * steps / rate
+    plain_value = ntraj * steps / t_plain
+    return {"metric": "traj-steps/s", "value": value, "unit": "traj-steps/s", "steps": steps,
+            "ms": ms, "gpu_launches": int(launches), "trajectories": ntraj,
+            "groups": [{"grid": [N, N], "trajectories": B} for N, B in TWA_GROUPS],
+            "dtype": "f32 (tables built in FP64)", "steps_per_graph": chunk, "autotune": choices or None,
+            "plain_per_trajectory": {"value": plain_value, "unit": "traj-steps/s",
+                                     "sample": "3 trajectories x 100 steps per grid, one handle each, two-pass path"},
+            "speedup_vs_plain_per_trajectory": value / plain_value}
 
 
 def main():
@@ -356,6 +406,9 @@ def main():
     ap.add_argument("--fp64", default="dw", choices=["dw", "native"],
                     help="ComplexF64 arithmetic: double-word on the FP32 pipes (default) or native FP64")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--twa-steps", type=int, default=2000,
+                    help="steps of the batched truncated-Wigner ensemble measurement (0 skips it)")
+    ap.add_argument("--no-tune", action="store_true", help="skip the ensemble autotuner")
     args = ap.parse_args()
     if args.warmup < 3:
         ap.error("--warmup must be >= 3")

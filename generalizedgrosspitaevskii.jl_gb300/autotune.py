@@ -1,0 +1,89 @@
+"""A small autotuner for ensemble groups.
+
+For a group (grid size, components, precision, trajectories) it times the candidate
+configurations on the actual problem for a few chunks of steps and keeps the fastest:
+
+* path: the resident plane kernel (whole trajectory in shared memory, when the grid fits)
+  or the two-pass HBM path;
+* steps_per_graph: the chunk length captured in the CUDA graph (launch amortisation vs
+  graph size).
+
+Results are cached in a JSON file keyed by the group shape and the GPU name
+(``$GPE_AUTOTUNE_CACHE`` or ``~/.cache/gpe_gb300/autotune.json``).
+"""
+from __future__ import annotations
+
+import json
+import os
+from pathlib import Path
+from typing import Callable, Dict, Iterable, Optional, Tuple
+
+CANDIDATE_CHUNKS = (10, 50, 200)
+
+
+def cache_path() -> Path:
+    p = os.environ.get("GPE_AUTOTUNE_CACHE")
+    return Path(p) if p else Path.home() / ".cache" / "gpe_gb300" / "autotune.json"
+
+
+def _load() -> Dict[str, dict]:
+    p = cache_path()
+    try:
+        return json.loads(p.read_text())
+    except (OSError, ValueError):
+        return {}
+
+
+def _store(db: Dict[str, dict]):
+    p = cache_path()
+    try:
+        p.parent.mkdir(parents=True, exist_ok=True)
+        p.write_text(json.dumps(db, indent=1, sort_keys=True))
+    except OSError:
+        pass  # a read-only home only loses the cache
+
+
+def gpu_name() -> str:
+    try:
+        import subprocess
+        out = subprocess.run(["nvidia-smi", "--query-gpu=name", "--format=csv,noheader", "-i", "0"],
+                             capture_output=True, text=True, timeout=10).stdout.strip()
+        return out or "unknown"
+    except Exception:
+        return "unknown"
+
+
+def key(N: int, M: int, dtype: str, ntraj: int, gpu: str) -> str:
+    return f"{gpu}|N{N}|M{M}|{dtype}|B{ntraj}"
+
+
+def tune(make_iterator: Callable[[bool], object], k: str, chunks: Iterable[int] = CANDIDATE_CHUNKS,
+         trial_steps: int = 200, force: bool = False) -> Tuple[bool, int, dict]:
+    """Pick (resident, steps_per_graph) for one group.  make_iterator(resident) builds a
+    fresh iterator for the group.  Returns (resident, steps_per_graph, timings)."""
+    db = _load()
+    if not force and k in db:
+        r = db[k]
+        return bool(r["resident"]), int(r["steps_per_graph"]), r.get("timings", {})
+    from .twa import Ensemble
+    timings = {}
+    best = None
+    for resident in (True, False):
+        for chunk in chunks:
+            if trial_steps % chunk:
+                continue
+            it = make_iterator(resident)
+            ens = Ensemble([it])
+            try:
+                ens.run(chunk, chunk)  # capture + warm-up
+                ens.run(trial_steps, chunk)
+                ms = ens.last_run_ms()
+            finally:
+                ens.close()
+                it.close()
+            timings[f"resident={resident},chunk={chunk}"] = ms
+            if best is None or ms < best[0]:
+                best = (ms, resident, chunk)
+    db[k] = {"resident": best[1], "steps_per_graph": best[2], "timings": timings}
+    _store(db)
+    return best[1], best[2], timings

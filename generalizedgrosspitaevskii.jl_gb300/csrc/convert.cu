@@ -1,4 +1,5 @@
-// convert.cu -- FP64 <-> double-word conversion of complex arrays on the device.
+// convert.cu -- small device utilities: FP64 <-> double-word conversion of complex
+// arrays, and the step-counter advance that ends a captured chunk of steps.
 #include "dw.cuh"
 #include "kernels.h"
 
@@ -17,6 +18,15 @@ __global__ void dw_to_f64_kernel(const dwc* __restrict__ src, double2* __restric
     const dwc v = src[i];
     dst[i] = make_double2(dw_to_double(re(v)), dw_to_double(im(v)));
   }
+}
+
+__global__ void advance_kernel(int64_t* k, int64_t n) {
+  if (threadIdx.x == 0 && blockIdx.x == 0) *k += n;
+}
+
+int launch_advance(int64_t* k, int64_t n, cudaStream_t s) {
+  advance_kernel<<<1, 32, 0, s>>>(k, n);
+  return (int)cudaGetLastError();
 }
 
 static unsigned grid_for(int64_t n) {

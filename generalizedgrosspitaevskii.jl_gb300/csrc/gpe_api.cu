@@ -29,6 +29,8 @@ template <typename Real, int M> int launch_row_t(int, const PassArgs&, int64_t, 
 template <typename Real, int M> int launch_col_t(int, const PassArgs&, cudaStream_t);
 template <typename Real, int M> int launch_line1d_t(int, const PassArgs&, cudaStream_t);
 template <typename Real, int M> int launch_nl_only_t(const PassArgs&, cudaStream_t);
+template <typename Real, int M> int launch_plane_t(int, const PassArgs&, cudaStream_t);
+template <typename Real, int M> bool plane_fits_t(int);
 template <typename Real, int M> int launch_norm_t(const PassArgs&, double*, cudaStream_t);
 
 // dtype here is the pass precision (PREC_F64, PREC_F32, PREC_DW)
@@ -42,6 +44,8 @@ int launch_col(int dtype, int M, int logn, const PassArgs& a, cudaStream_t s) { 
 int launch_line1d(int dtype, int M, int logn, const PassArgs& a, cudaStream_t s) { GPE_DISPATCH(launch_line1d_t, logn, a, s) }
 int launch_nl_only(int dtype, int M, const PassArgs& a, cudaStream_t s) { GPE_DISPATCH(launch_nl_only_t, a, s) }
 int launch_norm(int dtype, int M, const PassArgs& a, double* out, cudaStream_t s) { GPE_DISPATCH(launch_norm_t, a, out, s) }
+int launch_plane(int dtype, int M, int logn, const PassArgs& a, cudaStream_t s) { GPE_DISPATCH(launch_plane_t, logn, a, s) }
+bool plane_fits(int dtype, int M, int logn) { GPE_DISPATCH(plane_fits_t, logn) }
 }  // namespace gpe
 
 using gpe::PassArgs;
@@ -91,10 +95,18 @@ struct gpe_handle {
   int64_t last_launches = 0;
   // per-launch timing (gpe_set_timing)
   int timing = 0;
+  int capturing = 0;  // inside a stream capture: no timing events
   std::vector<cudaEvent_t> evpool;
   std::vector<int> evkind;  // kernel kind of each recorded pair
   double kms[3] = {0, 0, 0};
   int64_t kn[3] = {0, 0, 0};
+  // graph replay (gpe_set_graph): a captured chunk of gsteps steps whose kernels read
+  // the chunk's first step index from kdev
+  int64_t gsteps = 0;
+  int64_t* kdev = nullptr;
+  int64_t kval = 0;
+  cudaGraphExec_t gexec = nullptr;
+  int64_t glaunches = 0;
   std::string err;
 };
 
@@ -593,7 +605,7 @@ struct TimedLaunch {
   int kind;
   size_t idx = 0;
   TimedLaunch(gpe_handle* hh, int k) : h(hh), kind(k) {
-    if (!h->timing) return;
+    if (!h->timing || h->capturing) return;
     idx = h->evkind.size();
     while (h->evpool.size() < 2 * (idx + 1)) {
       cudaEvent_t e;
@@ -604,7 +616,7 @@ struct TimedLaunch {
     cudaEventRecord(h->evpool[2 * idx], h->stream);
   }
   ~TimedLaunch() {
-    if (h->timing) cudaEventRecord(h->evpool[2 * idx + 1], h->stream);
+    if (h->timing && !h->capturing) cudaEventRecord(h->evpool[2 * idx + 1], h->stream);
   }
 };
 
@@ -683,9 +695,11 @@ static int ensure(gpe_handle* h, void** buf, size_t* cap, size_t bytes) {
 // Enqueue nsteps steps; saves go to save_dev (layout [m][slot][b][p]) with nsaves_total
 // slots per component.  Returns the number of launches in *launches.
 static int enqueue_steps(gpe_handle* h, int64_t nsteps, int64_t save_every, void* save_dev, int64_t nsaves_total,
-                         const void* xi_dev, int64_t* launches) {
+                         const void* xi_dev, int64_t* launches, bool relative = false) {
   PassArgs a = base_args(h);
-  const int64_t k0 = h->steps;
+  // relative: step indices count from the value in h->kdev (graph capture)
+  const int64_t k0 = relative ? 0 : h->steps;
+  if (relative) a.kbase = h->kdev;
   a.xi = xi_dev;
   a.xi_h0 = 2 * k0;  // replayed xi are indexed from this run's first half step
   const int64_t plane = h->P * h->B;
@@ -709,6 +723,21 @@ static int enqueue_steps(gpe_handle* h, int64_t nsteps, int64_t save_every, void
       a.tw = h->tw[0];
       LK(h, gpe::launch_line1d(h->prec, h->M, h->logn[0], a, h->stream));
     }
+    *launches = 1;
+    return GPE_OK;
+  }
+  // 2D square grids whose whole field fits in shared memory: one resident launch
+  if (h->ndim == 2 && h->n[0] == h->n[1] && !(h->d.flags & GPE_FLAG_NO_RESIDENT) &&
+      gpe::plane_fits(h->prec, h->M, h->logn[0])) {
+    a.nsteps = nsteps;
+    a.step0 = k0;
+    a.save_every = save_every;
+    a.save_stride = plane;
+    if (save_every > 0) slot_ptrs(a, 0);
+    a.tw = h->tw[0];
+    a.tw2 = h->tw[1];
+    TimedLaunch tl(h, 2);
+    LK(h, gpe::launch_plane(h->prec, h->M, h->logn[0], a, h->stream));
     *launches = 1;
     return GPE_OK;
   }
@@ -755,6 +784,46 @@ static int enqueue_steps(gpe_handle* h, int64_t nsteps, int64_t save_every, void
   return GPE_OK;
 }
 
+// Capture gsteps steps (plus the step-counter advance) into a graph once.
+static int capture_chunk(gpe_handle* h, cudaStream_t st, int64_t* launches) {
+  h->capturing = 1;
+  int64_t nl = 0;
+  const int rc = enqueue_steps(h, h->gsteps, 0, nullptr, 0, nullptr, &nl, true);
+  h->capturing = 0;
+  if (rc) return rc;
+  LK(h, gpe::launch_advance(h->kdev, h->gsteps, st));
+  *launches = nl + 1;
+  return GPE_OK;
+}
+
+static int ensure_graph(gpe_handle* h) {
+  if (!h->kdev) CK(h, cudaMalloc((void**)&h->kdev, sizeof(int64_t)));
+  if (h->gexec) return GPE_OK;
+  cudaGraph_t g = nullptr;
+  CK(h, cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
+  int64_t nl = 0;
+  const int rc = capture_chunk(h, h->stream, &nl);
+  const cudaError_t ec = cudaStreamEndCapture(h->stream, &g);
+  if (rc) {
+    if (g) cudaGraphDestroy(g);
+    return rc;
+  }
+  if (ec != cudaSuccess) return fail(h, GPE_ERR_CUDA, "graph capture failed: %s", cudaGetErrorString(ec));
+  const cudaError_t ei = cudaGraphInstantiate(&h->gexec, g, 0);
+  cudaGraphDestroy(g);
+  if (ei != cudaSuccess) return fail(h, GPE_ERR_CUDA, "graph instantiate failed: %s", cudaGetErrorString(ei));
+  h->glaunches = nl;
+  return GPE_OK;
+}
+
+static int replay_graph(gpe_handle* h, int64_t nsteps, int64_t* launches) {
+  h->kval = h->steps;
+  CK(h, cudaMemcpyAsync(h->kdev, &h->kval, sizeof(int64_t), cudaMemcpyHostToDevice, h->stream));
+  for (int64_t r = 0; r < nsteps / h->gsteps; ++r) CK(h, cudaGraphLaunch(h->gexec, h->stream));
+  *launches = h->glaunches * (nsteps / h->gsteps);
+  return GPE_OK;
+}
+
 static int run_common(gpe_handle* h, int64_t nsteps, int64_t save_every, void* out, bool out_is_dev, double* ts_out,
                       const void* xi_host) {
   if (!h) return GPE_ERR_INVALID;
@@ -797,10 +866,20 @@ static int run_common(gpe_handle* h, int64_t nsteps, int64_t save_every, void* o
     }
   }
   h->evkind.clear();
+  const bool graph = h->gsteps > 0 && save_every == 0 && !xi_host && nsteps % h->gsteps == 0;
+  if (graph) {
+    int rc = ensure_graph(h);
+    if (rc) return rc;
+  }
   CK(h, cudaEventRecord(h->ev0, h->stream));
   int64_t launches = 0;
-  int rc = enqueue_steps(h, nsteps, save_every, save_dev, nsaves, xi_host ? h->xi_buf : nullptr, &launches);
-  if (rc) return rc;
+  if (graph) {
+    int rc = replay_graph(h, nsteps, &launches);
+    if (rc) return rc;
+  } else {
+    int rc = enqueue_steps(h, nsteps, save_every, save_dev, nsaves, xi_host ? h->xi_buf : nullptr, &launches);
+    if (rc) return rc;
+  }
   CK(h, cudaEventRecord(h->ev1, h->stream));
   CK(h, cudaEventSynchronize(h->ev1));
   float ms = 0.f;
@@ -884,6 +963,51 @@ int gpe_energy(gpe_handle* h, double* out) {
   return fail(h, GPE_ERR_UNSUPPORTED, "gpe_energy is not available in this build");
 }
 
+int gpe_set_graph(gpe_handle* h, int64_t steps_per_graph) {
+  if (!h) return GPE_ERR_INVALID;
+  if (steps_per_graph < 0) return fail(h, GPE_ERR_INVALID, "steps_per_graph must be >= 0");
+  if (h->gexec) {
+    cudaGraphExecDestroy(h->gexec);
+    h->gexec = nullptr;
+  }
+  h->gsteps = steps_per_graph;
+  return GPE_OK;
+}
+
+// Enqueue without waiting: no saves, no replay.  Host bookkeeping (t, steps) advances now.
+int gpe_run_async(gpe_handle* h, int64_t nsteps) {
+  if (!h) return GPE_ERR_INVALID;
+  CK(h, cudaSetDevice(h->dev));
+  if (nsteps < 0) return fail(h, GPE_ERR_INVALID, "nsteps must be >= 0");
+  if (h->noise == GPE_NOISE_REPLAY) return fail(h, GPE_ERR_INVALID, "replayed noise needs gpe_run_replay");
+  for (int m = 0; m < h->M; ++m)
+    if (h->pprof[m] && h->pcoef_n[m] > 1 && h->pcoef_n[m] < 2 * (h->steps + nsteps) + 1)
+      return fail(h, GPE_ERR_INVALID, "pump %d has too few amplitudes for %lld more steps", m, (long long)nsteps);
+  if (nsteps == 0) return GPE_OK;
+  int64_t launches = 0;
+  if (h->gsteps > 0 && nsteps % h->gsteps == 0) {
+    int rc = ensure_graph(h);
+    if (rc) return rc;
+    rc = replay_graph(h, nsteps, &launches);
+    if (rc) return rc;
+  } else {
+    int rc = enqueue_steps(h, nsteps, 0, nullptr, 0, nullptr, &launches);
+    if (rc) return rc;
+  }
+  for (int64_t s = 0; s < nsteps; ++s) h->t += h->d.dt;
+  h->steps += nsteps;
+  h->last_launches = launches;
+  return GPE_OK;
+}
+
+int gpe_wait(gpe_handle* h) {
+  if (!h) return GPE_ERR_INVALID;
+  CK(h, cudaSetDevice(h->dev));
+  CK(h, cudaStreamSynchronize(h->stream));
+  CK(h, cudaGetLastError());
+  return GPE_OK;
+}
+
 int gpe_set_timing(gpe_handle* h, int on) {
   if (!h) return GPE_ERR_INVALID;
   h->timing = on ? 1 : 0;
@@ -898,5 +1022,140 @@ int gpe_kernel_times(const gpe_handle* h, double* ms, int64_t* n) {
 
 double gpe_last_run_ms(const gpe_handle* h) { return h ? h->last_ms : 0.0; }
 int64_t gpe_last_run_launches(const gpe_handle* h) { return h ? h->last_launches : 0; }
+
+// ---- ensembles: several handles (grid-size groups) advanced by one CUDA graph ----
+}  // extern "C"
+
+struct gpe_ensemble {
+  std::vector<gpe_handle*> hs;
+  int64_t gsteps = 0;
+  cudaGraphExec_t gexec = nullptr;
+  cudaEvent_t fork = nullptr, ev0 = nullptr, ev1 = nullptr;
+  std::vector<cudaEvent_t> joins;
+  int64_t launches_per_graph = 0;
+  double last_ms = 0.0;
+  int64_t last_launches = 0;
+  std::string err;
+};
+
+static int efail(gpe_ensemble* e, int code, const char* msg) {
+  if (e) e->err = msg;
+  else g_create_error = msg;
+  return code;
+}
+
+extern "C" {
+
+int gpe_ensemble_create(gpe_handle* const* handles, int n, gpe_ensemble** out) {
+  if (!handles || n < 1 || !out) return efail(nullptr, GPE_ERR_INVALID, "ensemble needs at least one handle");
+  *out = nullptr;
+  for (int i = 0; i < n; ++i) {
+    if (!handles[i]) return efail(nullptr, GPE_ERR_INVALID, "null handle in ensemble");
+    if (handles[i]->dev != handles[0]->dev) return efail(nullptr, GPE_ERR_INVALID, "ensemble handles must share a device");
+    if (handles[i]->noise == GPE_NOISE_REPLAY) return efail(nullptr, GPE_ERR_INVALID, "ensembles do not replay noise");
+  }
+  gpe_ensemble* e = new gpe_ensemble();
+  e->hs.assign(handles, handles + n);
+  cudaSetDevice(handles[0]->dev);
+  cudaEventCreateWithFlags(&e->fork, cudaEventDisableTiming);
+  cudaEventCreate(&e->ev0);
+  cudaEventCreate(&e->ev1);
+  e->joins.resize((size_t)n);
+  for (auto& j : e->joins) cudaEventCreateWithFlags(&j, cudaEventDisableTiming);
+  *out = e;
+  return GPE_OK;
+}
+
+int gpe_ensemble_destroy(gpe_ensemble* e) {
+  if (!e) return GPE_OK;
+  if (e->gexec) cudaGraphExecDestroy(e->gexec);
+  cudaEventDestroy(e->fork);
+  cudaEventDestroy(e->ev0);
+  cudaEventDestroy(e->ev1);
+  for (auto j : e->joins) cudaEventDestroy(j);
+  delete e;
+  return GPE_OK;
+}
+
+const char* gpe_ensemble_last_error(const gpe_ensemble* e) { return e ? e->err.c_str() : g_create_error.c_str(); }
+
+// One graph: fork from the first handle's stream to every handle's stream, each handle
+// enqueues steps_per_graph steps (its resident launch or its pass chain) and advances its
+// own step counter, then everything joins back.  The graph is replayed nsteps /
+// steps_per_graph times.
+int gpe_ensemble_run(gpe_ensemble* e, int64_t nsteps, int64_t steps_per_graph) {
+  if (!e) return GPE_ERR_INVALID;
+  if (nsteps < 0 || steps_per_graph < 1 || nsteps % steps_per_graph)
+    return efail(e, GPE_ERR_INVALID, "nsteps must be a non-negative multiple of steps_per_graph >= 1");
+  gpe_handle* h0 = e->hs[0];
+  cudaSetDevice(h0->dev);
+  for (gpe_handle* h : e->hs)
+    for (int m = 0; m < h->M; ++m)
+      if (h->pprof[m] && h->pcoef_n[m] > 1 && h->pcoef_n[m] < 2 * (h->steps + nsteps) + 1)
+        return efail(e, GPE_ERR_INVALID, "a pump has too few amplitudes for this run");
+  if (e->gexec && e->gsteps != steps_per_graph) {
+    cudaGraphExecDestroy(e->gexec);
+    e->gexec = nullptr;
+  }
+  if (!e->gexec) {
+    for (gpe_handle* h : e->hs) {
+      if (!h->kdev && cudaMalloc((void**)&h->kdev, sizeof(int64_t)) != cudaSuccess)
+        return efail(e, GPE_ERR_NOMEM, "cudaMalloc of a step counter failed");
+      h->gsteps = steps_per_graph;
+    }
+    cudaGraph_t g = nullptr;
+    if (cudaStreamBeginCapture(h0->stream, cudaStreamCaptureModeThreadLocal) != cudaSuccess)
+      return efail(e, GPE_ERR_CUDA, "cudaStreamBeginCapture failed");
+    cudaEventRecord(e->fork, h0->stream);
+    int rc = GPE_OK;
+    int64_t total = 0;
+    for (size_t i = 0; i < e->hs.size() && rc == GPE_OK; ++i) {
+      gpe_handle* h = e->hs[i];
+      if (i > 0) cudaStreamWaitEvent(h->stream, e->fork, 0);
+      int64_t nl = 0;
+      rc = capture_chunk(h, h->stream, &nl);
+      total += nl;
+      if (i > 0) {
+        cudaEventRecord(e->joins[i], h->stream);
+        cudaStreamWaitEvent(h0->stream, e->joins[i], 0);
+      }
+    }
+    const cudaError_t ec = cudaStreamEndCapture(h0->stream, &g);
+    if (rc != GPE_OK || ec != cudaSuccess) {
+      if (g) cudaGraphDestroy(g);
+      for (gpe_handle* h : e->hs) h->gsteps = 0;
+      return efail(e, rc ? rc : GPE_ERR_CUDA, rc ? "capture of a group failed" : cudaGetErrorString(ec));
+    }
+    const cudaError_t ei = cudaGraphInstantiate(&e->gexec, g, 0);
+    cudaGraphDestroy(g);
+    for (gpe_handle* h : e->hs) h->gsteps = 0;
+    if (ei != cudaSuccess) return efail(e, GPE_ERR_CUDA, cudaGetErrorString(ei));
+    e->gsteps = steps_per_graph;
+    e->launches_per_graph = total;
+  }
+  for (gpe_handle* h : e->hs) {
+    h->kval = h->steps;
+    if (cudaMemcpyAsync(h->kdev, &h->kval, sizeof(int64_t), cudaMemcpyHostToDevice, h0->stream) != cudaSuccess)
+      return efail(e, GPE_ERR_CUDA, "step counter upload failed");
+  }
+  cudaEventRecord(e->ev0, h0->stream);
+  for (int64_t r = 0; r < nsteps / steps_per_graph; ++r)
+    if (cudaGraphLaunch(e->gexec, h0->stream) != cudaSuccess) return efail(e, GPE_ERR_CUDA, "cudaGraphLaunch failed");
+  cudaEventRecord(e->ev1, h0->stream);
+  const cudaError_t es = cudaEventSynchronize(e->ev1);
+  if (es != cudaSuccess) return efail(e, GPE_ERR_CUDA, cudaGetErrorString(es));
+  float ms = 0.f;
+  cudaEventElapsedTime(&ms, e->ev0, e->ev1);
+  e->last_ms = ms;
+  e->last_launches = e->launches_per_graph * (nsteps / steps_per_graph);
+  for (gpe_handle* h : e->hs) {
+    for (int64_t s = 0; s < nsteps; ++s) h->t += h->d.dt;
+    h->steps += nsteps;
+  }
+  return GPE_OK;
+}
+
+double gpe_ensemble_last_run_ms(const gpe_ensemble* e) { return e ? e->last_ms : 0.0; }
+int64_t gpe_ensemble_last_run_launches(const gpe_ensemble* e) { return e ? e->last_launches : 0; }
 
 }  // extern "C"

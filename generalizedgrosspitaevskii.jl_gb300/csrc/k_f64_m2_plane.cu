@@ -1,0 +1,5 @@
+// Instantiates the resident plane kernels for native FP64 fields with 2 component(s).
+#include "passes.cuh"
+namespace gpe {
+GPE_INSTANTIATE_PLANE(double, 2)
+}  // namespace gpe

@@ -25,8 +25,10 @@ struct PassArgs {
   int32_t kkind;
   const void* vtab;
   int32_t vkind;
-  // twiddles w_N^k, k < N, for the transformed line length
+  // twiddles w_N^k, k < N, for the transformed line length (tw2: y lines of the
+  // resident plane kernel)
   const void* tw;
+  const void* tw2;
   // nonlinearity G_j = sum_l g[j][l] |u_l|^2 + c[j] (complex).  FP64 values, their FP32
   // roundings (gf, cf) and the FP32 remainders (gl, cl) that make (gf + gl) the
   // double-word form, so no pass converts per point.
@@ -54,6 +56,9 @@ struct PassArgs {
   // row pass program: [iFFT] [half hA] [save] [half hB] [FFT]; h < 0 skips a half
   int32_t do_ifft, do_fft;
   int64_t hA, hB;
+  // graph replay: when set, step indices (step0, hA, hB) are relative to the step count
+  // stored here on the device, so a captured chunk of steps replays at any position
+  const int64_t* kbase;
   // 1D resident program: nsteps full steps from step0, save every save_every steps
   // into save[m] + slot*save_stride
   int64_t nsteps, step0, save_every, save_stride;
@@ -71,8 +76,13 @@ int launch_row(int dtype, int M, int logn, const PassArgs& a, int64_t nlines, cu
 int launch_col(int dtype, int M, int logn, const PassArgs& a, cudaStream_t s);
 int launch_line1d(int dtype, int M, int logn, const PassArgs& a, cudaStream_t s);
 int launch_nl_only(int dtype, int M, const PassArgs& a, cudaStream_t s);
+// whole-trajectory resident 2D kernel (square grids of side 2^logn that fit in shared memory)
+int launch_plane(int dtype, int M, int logn, const PassArgs& a, cudaStream_t s);
+bool plane_fits(int dtype, int M, int logn);
 // FP64 reductions: out[m] += sum |u_m|^2 (device double array of M entries)
 int launch_norm(int dtype, int M, const PassArgs& a, double* out, cudaStream_t s);
+// *k += n on the device (end of a captured chunk of n steps)
+int launch_advance(int64_t* k, int64_t n, cudaStream_t s);
 // FP64 <-> double-word conversion of n complex numbers
 int launch_f64_to_dw(const void* src, void* dst, int64_t n, cudaStream_t s);
 int launch_dw_to_f64(const void* src, void* dst, int64_t n, cudaStream_t s);

@@ -446,8 +446,8 @@ row_kernel(const PassArgs a, const int64_t nlines) {
       if (ph == 0 ? a.do_ifft : a.do_fft) fft_components<C, N, E, M>(x, ph == 0, t, lay, tw);
       continue;
     }
-    const int64_t h = ph == 2 ? a.hB : a.hA;
-    if (h >= 0) half_points<Real, M, E>(x, a, p0, T, b, h);
+    const int64_t hr = ph == 2 ? a.hB : a.hA;
+    if (hr >= 0) half_points<Real, M, E>(x, a, p0, T, b, hr + (a.kbase ? 2 * *a.kbase : 0));
     if (ph == 1 && a.save[0] && active) {
 #pragma unroll
       for (int m = 0; m < M; ++m)
@@ -539,8 +539,9 @@ line1d_kernel(const PassArgs a, const int64_t nlines) {
   for (int m = 0; m < M; ++m)
 #pragma unroll
     for (int i = 0; i < E; ++i) x[m][i] = ((const C*)a.u[m])[g0 + T * i];
+  const int64_t step0 = a.step0 + (a.kbase ? *a.kbase : 0);
   for (int64_t s = 0; s < a.nsteps; ++s) {
-    const int64_t k = a.step0 + s;
+    const int64_t k = step0 + s;
     // phases: 0 half step 2k, 1 forward FFT, 2 k-space table, 3 inverse FFT,
     // 4 half step 2k+1 (one FFT and one half-step instance)
 #pragma unroll 1
@@ -579,6 +580,142 @@ line1d_kernel(const PassArgs a, const int64_t nlines) {
   }
 }
 
+template <typename K>
+static inline int set_smem(K k, size_t bytes);
+
+// ------------------------------------------------------------------ resident plane
+// A whole 2D trajectory (M planes of N x N points) lives in shared memory for all
+// nsteps steps; one CTA per trajectory.  Each step is one column round-set
+// (FFT_y * table * iFFT_y) and one row round-set ([iFFT_x] [half A] [save] [half B]
+// [FFT_x]), the same operations, code and order as the HBM column and row passes, so
+// the result equals theirs.  A line's FFT exchanges run in place in the line's own
+// shared-memory slots (its points are in registers meanwhile).
+template <typename Real, int M, int LOGN>
+struct PlaneCfg {
+  using C = typename CT<Real>::T;
+  static constexpr int N = 1 << LOGN;
+  static constexpr int E = cmin(sizeof(C) == 16 ? 8 : 8, N / 2);
+  static constexpr int T = N / E;            // threads per line
+  static constexpr int NT = cmin(512, N * T);  // threads per CTA
+  static constexpr int LPR = NT / T;         // lines per round
+  static constexpr int ROUNDS = N / LPR;
+  static constexpr size_t SMEM = (size_t)M * N * N * sizeof(C);
+  static constexpr bool FITS = SMEM <= 200 * 1024;
+};
+
+template <int STRIDE, typename C>
+struct StridedLayout {  // point n of a column at n * STRIDE
+  C* base;
+  template <int NS, int R>
+  __device__ __forceinline__ int addr(int idx) const { return idx * STRIDE; }
+};
+
+template <typename Real, int LOGN, int M>
+__global__ void __launch_bounds__(PlaneCfg<Real, M, LOGN>::NT)
+plane_kernel(const PassArgs a) {
+  using Cfg = PlaneCfg<Real, M, LOGN>;
+  using C = typename CT<Real>::T;
+  constexpr int N = Cfg::N, E = Cfg::E, T = Cfg::T, NT = Cfg::NT, LPR = Cfg::LPR, ROUNDS = Cfg::ROUNDS;
+  constexpr int P = N * N;
+  extern __shared__ __align__(16) unsigned char smraw[];
+  C* f = reinterpret_cast<C*>(smraw);  // f[m * P + p]
+  const int64_t b = blockIdx.x;
+  const int tid = threadIdx.x;
+  const C* twx = (const C*)a.tw;
+  const C* twy = (const C*)a.tw2;
+  for (int m = 0; m < M; ++m)
+    for (int p = tid; p < P; p += NT) f[m * P + p] = ((const C*)a.u[m])[b * P + p];
+  __syncthreads();
+  const int t = tid % T, lr = tid / T;       // row rounds: line lr of the round
+  const int cc = tid % LPR, ct = tid / LPR;  // column rounds: column cc, thread ct
+  const int64_t step0 = a.step0 + (a.kbase ? *a.kbase : 0);
+  for (int64_t s = 0; s <= a.nsteps; ++s) {
+    const int64_t k = step0 + s;
+    // ---- column round-set (absent before the first step)
+    if (s > 0 && a.ktab) {
+#pragma unroll 1
+      for (int r = 0; r < ROUNDS; ++r) {
+        const int c = r * LPR + cc;
+        const StridedLayout<N, C> lay{f + c};
+        C x[M][E];
+#pragma unroll
+        for (int m = 0; m < M; ++m)
+#pragma unroll
+          for (int i = 0; i < E; ++i) x[m][i] = f[m * P + (ct + T * i) * N + c];
+        __syncthreads();  // the column's slots become FFT exchange space
+        fft_components<C, N, E, M>(x, false, ct, lay, twy);
+#pragma unroll 1
+        for (int i = 0; i < E; ++i) {
+          C v[M];
+#pragma unroll
+          for (int m = 0; m < M; ++m) v[m] = x[m][0];
+          kmul<Real, M>(v, a, (int64_t)(ct + T * i) * N + c);
+#pragma unroll
+          for (int m = 0; m < M; ++m) {
+#pragma unroll
+            for (int q = 0; q + 1 < E; ++q) x[m][q] = x[m][q + 1];
+            x[m][E - 1] = v[m];
+          }
+        }
+        fft_components<C, N, E, M>(x, true, ct, lay, twy);
+        __syncthreads();
+#pragma unroll
+        for (int m = 0; m < M; ++m)
+#pragma unroll
+          for (int i = 0; i < E; ++i) f[m * P + (ct + T * i) * N + c] = x[m][i];
+        __syncthreads();
+      }
+    }
+    // ---- row round-set: end of step k-1 (s > 0) and start of step k (s < nsteps)
+    const bool first = (s == 0), last = (s == a.nsteps);
+    const bool save = !first && a.save_every > 0 && (s % a.save_every) == 0;
+#pragma unroll 1
+    for (int r = 0; r < ROUNDS; ++r) {
+      const int y = r * LPR + lr;
+      const RowLayout<C> lay{f + y * N};
+      C x[M][E];
+#pragma unroll
+      for (int m = 0; m < M; ++m)
+#pragma unroll
+        for (int i = 0; i < E; ++i) x[m][i] = f[m * P + y * N + t + T * i];
+      __syncthreads();  // the line's slots become FFT exchange space
+      if (!first && a.ktab) fft_components<C, N, E, M>(x, true, t, lay, twx);
+      if (!first) half_points<Real, M, E>(x, a, y * N + t, T, b, 2 * k - 1);
+      if (save) {
+        const int64_t slot = s / a.save_every - 1;
+#pragma unroll
+        for (int m = 0; m < M; ++m)
+#pragma unroll
+          for (int i = 0; i < E; ++i) store_save<Real>(a.save[m], slot * a.save_stride + b * P + y * N + t + T * i, x[m][i]);
+      }
+      if (!last) half_points<Real, M, E>(x, a, y * N + t, T, b, 2 * k);
+      if (!last && a.ktab) fft_components<C, N, E, M>(x, false, t, lay, twx);
+      __syncthreads();
+#pragma unroll
+      for (int m = 0; m < M; ++m)
+#pragma unroll
+        for (int i = 0; i < E; ++i) f[m * P + y * N + t + T * i] = x[m][i];
+      __syncthreads();
+    }
+  }
+  for (int m = 0; m < M; ++m)
+    for (int p = tid; p < P; p += NT) ((C*)a.u[m])[b * P + p] = f[m * P + p];
+}
+
+template <typename Real, int M, int LOGN>
+int launch_plane_n(const PassArgs& a, cudaStream_t s) {
+  using Cfg = PlaneCfg<Real, M, LOGN>;
+  if constexpr (!Cfg::FITS) {
+    return (int)cudaErrorInvalidValue;
+  } else {
+    auto k = plane_kernel<Real, LOGN, M>;
+    int e = set_smem(k, Cfg::SMEM);
+    if (e) return e;
+    k<<<(unsigned)a.B, Cfg::NT, Cfg::SMEM, s>>>(a);
+    return (int)cudaGetLastError();
+  }
+}
+
 // ------------------------------------------------------------------ no dispersion
 // Without a dispersion the step is pointwise: one thread per point runs all steps.
 template <typename Real, int M>
@@ -590,10 +727,11 @@ __global__ void __launch_bounds__(256) nl_only_kernel(const PassArgs a) {
     C v[M];
 #pragma unroll
     for (int m = 0; m < M; ++m) v[m] = ((const C*)a.u[m])[q];
+    const int64_t step0 = a.step0 + (a.kbase ? *a.kbase : 0);
     for (int64_t s = 0; s < a.nsteps; ++s) {
 #pragma unroll 1
       for (int half = 0; half < 2; ++half) {
-        const int64_t h = 2 * (a.step0 + s) + half;
+        const int64_t h = 2 * (step0 + s) + half;
         C pn[M], px[M];
         load_pump<Real, M>(a, h, pn, px);
         half_step<Real, M>(v, a, p, b, h, pn, px);
@@ -713,6 +851,27 @@ int launch_line1d_t(int logn, const PassArgs& a, cudaStream_t s) {
   GPE_LOGN_SWITCH(launch_line1d_n, a, s)
 }
 template <typename Real, int M>
+int launch_plane_t(int logn, const PassArgs& a, cudaStream_t s) {
+  switch (logn) {
+    case 4: return launch_plane_n<Real, M, 4>(a, s);
+    case 5: return launch_plane_n<Real, M, 5>(a, s);
+    case 6: return launch_plane_n<Real, M, 6>(a, s);
+    case 7: return launch_plane_n<Real, M, 7>(a, s);
+    default: return (int)cudaErrorInvalidValue;
+  }
+}
+// whether a 2^logn x 2^logn field of M components fits the resident kernel
+template <typename Real, int M>
+bool plane_fits_t(int logn) {
+  switch (logn) {
+    case 4: return PlaneCfg<Real, M, 4>::FITS;
+    case 5: return PlaneCfg<Real, M, 5>::FITS;
+    case 6: return PlaneCfg<Real, M, 6>::FITS;
+    case 7: return PlaneCfg<Real, M, 7>::FITS;
+    default: return false;
+  }
+}
+template <typename Real, int M>
 int launch_nl_only_t(const PassArgs& a, cudaStream_t s) {
   const int64_t total = a.P * a.B;
   int64_t blocks = (total + 255) / 256;
@@ -733,6 +892,9 @@ int launch_norm_t(const PassArgs& a, double* out, cudaStream_t s) {
   template int launch_row_t<REAL, MM>(int, const PassArgs&, int64_t, cudaStream_t);
 #define GPE_INSTANTIATE_COL(REAL, MM) \
   template int launch_col_t<REAL, MM>(int, const PassArgs&, cudaStream_t);
+#define GPE_INSTANTIATE_PLANE(REAL, MM)                                      \
+  template int launch_plane_t<REAL, MM>(int, const PassArgs&, cudaStream_t);  \
+  template bool plane_fits_t<REAL, MM>(int);
 #define GPE_INSTANTIATE_OTHER(REAL, MM)                                           \
   template int launch_line1d_t<REAL, MM>(int, const PassArgs&, cudaStream_t);    \
   template int launch_nl_only_t<REAL, MM>(const PassArgs&, cudaStream_t);        \

@@ -66,7 +66,7 @@ class StrangSplittingIterator:
 
     def __init__(self, prob: GrossPitaevskiiProblem, tspan, *, dt, nsaves, save_start=True, rng=None,
                  noise_replay: Optional[Callable] = None, total_steps: Optional[int] = None,
-                 device: int = -1, fp64: str = "dw"):
+                 device: int = -1, fp64: str = "dw", resident: bool = True):
         self.lib = L.load()
         self.prob = prob
         self.nsaves = int(nsaves)
@@ -95,7 +95,7 @@ class StrangSplittingIterator:
         d.device = device
         if fp64 not in ("dw", "native"):
             raise ValueError("fp64 must be 'dw' (double-word on the FP32 pipes) or 'native'")
-        d.flags = L.GPE_FLAG_FP64_NATIVE if fp64 == "native" else 0
+        d.flags = (L.GPE_FLAG_FP64_NATIVE if fp64 == "native" else 0) | (0 if resident else L.GPE_FLAG_NO_RESIDENT)
         h = ctypes.c_void_p()
         rc = self.lib.gpe_create(ctypes.byref(d), ctypes.byref(h))
         L.check(self.lib, None, rc)
@@ -229,17 +229,19 @@ class StrangSplittingIterator:
 
 
 def init(prob: GrossPitaevskiiProblem, alg: StrangSplitting, tspan, *, dt, nsaves, show_progress=False,
-         progress=None, save_start=True, workgroup_size=(), rng=None, noise_replay=None, fp64="dw", device=-1):
+         progress=None, save_start=True, workgroup_size=(), rng=None, noise_replay=None, fp64="dw", device=-1,
+         resident=True):
     """init(prob, StrangSplitting(), tspan; dt, nsaves, ...) (src/strang_splitting.jl:32-67).
     show_progress / progress / workgroup_size are accepted for signature parity and
     have no effect: the backend picks its own launch shapes.  Extra keywords: ``rng``
     (Philox seed or numpy Generator), ``noise_replay`` (callable h -> xi for replayed
     noise), ``fp64`` ("dw": ComplexF64 fields advanced in double-word arithmetic on the
-    FP32 pipes, the default; "native": FP64 instructions), ``device`` (CUDA ordinal)."""
+    FP32 pipes, the default; "native": FP64 instructions), ``device`` (CUDA ordinal),
+    ``resident`` (False forces the two-pass HBM path for small square 2D grids)."""
     if not isinstance(alg, StrangSplitting):
         raise TypeError("the only algorithm is StrangSplitting()")
     return StrangSplittingIterator(prob, tspan, dt=dt, nsaves=nsaves, save_start=save_start, rng=rng,
-                                   noise_replay=noise_replay, fp64=fp64, device=device)
+                                   noise_replay=noise_replay, fp64=fp64, device=device, resident=resident)
 
 
 def solve(prob: GrossPitaevskiiProblem, alg: StrangSplitting, tspan, **kwargs):

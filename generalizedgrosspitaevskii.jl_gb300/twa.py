@@ -1,0 +1,117 @@
+"""Truncated-Wigner ensembles over grids of different sizes, advanced by one CUDA graph.
+
+The reference batches stochastic trajectories along the trailing dims of u0, all on one
+grid (docs/src/stochastic_simulations.md:36-48, examples/truncated_wigner.jl:86-100).
+Here each grid size is one group (one libgpe handle whose batch holds that group's
+trajectories) and ``Ensemble`` advances every group together with a single captured CUDA
+graph (``gpe_ensemble_run``): square grids that fit in one CTA's shared memory run as one
+resident launch per chunk of steps, larger grids as their two-pass chain, each group on
+its own stream inside the graph.  ``autotune`` picks, per group, the path and the chunk
+length.
+"""
+from __future__ import annotations
+
+import ctypes
+import math
+import time
+from dataclasses import dataclass
+from typing import List, Optional, Sequence
+
+import numpy as np
+
+from . import _lib as L
+from .problem import GrossPitaevskiiProblem
+from .strang import StrangSplitting, StrangSplittingIterator
+
+
+@dataclass
+class DampedDrivenParams:
+    """i du = [|k|^2/2 - i gamma/2 + g |u|^2 + i F] u dt + sqrt(gamma / (2 dV)) dW:
+    the damped-driven scalar field of the truncated-Wigner example
+    (examples/truncated_wigner.jl:32-42,96), with the decay in the dispersion."""
+    L: float = 64.0
+    gamma: float = 0.2
+    g: float = 0.01
+    F: float = 1.0
+    dt: float = 0.02
+
+
+def wigner_problem(N: int, ntraj: int, prm: DampedDrivenParams, seed: int, dtype=np.complex64):
+    """One group: ntraj trajectories on an N x N grid starting from the coherent state
+    1 plus Wigner vacuum noise xi / sqrt(2 dV) (examples/truncated_wigner.jl:89)."""
+    dV = (prm.L / N) ** 2
+    rng = np.random.default_rng(seed)
+    xi = (rng.standard_normal((N, N, ntraj)) + 1j * rng.standard_normal((N, N, ntraj))) * math.sqrt(0.5)
+    u0 = (1.0 + xi / math.sqrt(2 * dV)).astype(dtype)
+    eta = math.sqrt(prm.gamma / (2 * dV))
+    return GrossPitaevskiiProblem(
+        (np.asfortranarray(u0),), (prm.L, prm.L),
+        dispersion=lambda k, p: (k[0] ** 2 + k[1] ** 2) / 2 - 0.5j * prm.gamma,
+        nonlinearity=lambda u, p: prm.g * np.abs(u[0]) ** 2,
+        pump=lambda r, p, t: prm.F + 0 * r[0],
+        position_noise_func=lambda u, r, p: eta)
+
+
+class Ensemble:
+    """Groups advanced together by one CUDA graph (``gpe_ensemble_run``)."""
+
+    def __init__(self, iterators: Sequence[StrangSplittingIterator]):
+        self.its = list(iterators)
+        self.lib = L.load()
+        arr = (ctypes.c_void_p * len(self.its))(*[it.h.value for it in self.its])
+        e = ctypes.c_void_p()
+        rc = self.lib.gpe_ensemble_create(arr, len(self.its), ctypes.byref(e))
+        if rc != L.GPE_OK:
+            raise L.GPEError(rc, self.lib.gpe_ensemble_last_error(None).decode())
+        self.e = e
+
+    def run(self, nsteps: int, steps_per_graph: int):
+        rc = self.lib.gpe_ensemble_run(self.e, int(nsteps), int(steps_per_graph))
+        if rc != L.GPE_OK:
+            raise L.GPEError(rc, self.lib.gpe_ensemble_last_error(self.e).decode())
+
+    def last_run_ms(self) -> float:
+        return float(self.lib.gpe_ensemble_last_run_ms(self.e))
+
+    def last_run_launches(self) -> int:
+        return int(self.lib.gpe_ensemble_last_run_launches(self.e))
+
+    def close(self):
+        if getattr(self, "e", None) is not None and self.e.value:
+            self.lib.gpe_ensemble_destroy(self.e)
+            self.e = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def make_group(N: int, ntraj: int, prm: DampedDrivenParams, nsteps: int, seed: int, dtype=np.complex64,
+               resident: bool = True, noise_seed: Optional[int] = None) -> StrangSplittingIterator:
+    prob = wigner_problem(N, ntraj, prm, seed, dtype)
+    return StrangSplittingIterator(prob, (0.0, nsteps * prm.dt), dt=prm.dt, nsaves=1, rng=noise_seed or seed + 1,
+                                   resident=resident)
+
+
+def density_moments(it: StrangSplittingIterator):
+    """Per-site ensemble mean and variance of |u|^2 over the group's trajectories (FP64)."""
+    u = it.get_fields()[0]  # (N, N, ntraj)
+    n = np.abs(u.astype(np.complex128)) ** 2
+    return n.mean(axis=-1), n.var(axis=-1)
+
+
+def plain_per_trajectory_rate(N: int, prm: DampedDrivenParams, ntraj: int, nsteps: int, seed: int = 0,
+                              dtype=np.complex64) -> float:
+    """traj-steps/s of the plain per-trajectory form: one trajectory per handle on the
+    two-pass path, trajectories run one after another (the form the batched resident
+    ensemble is measured against)."""
+    total_ms = 0.0
+    for j in range(ntraj):
+        it = make_group(N, 1, prm, nsteps + 2, seed + 7 * j, dtype, resident=False)
+        it.step(2)  # warm-up
+        it.step(nsteps)
+        total_ms += it.last_run_ms()
+        it.close()
+    return ntraj * nsteps / (total_ms * 1e-3)

@@ -55,6 +55,10 @@ extern "C" {
  * 48-bit significands, unit roundoff 2^-48): GB300 issues FP32 FMAs 62x faster than FP64
  * ones.  With this flag the passes use native FP64 instead. */
 #define GPE_FLAG_FP64_NATIVE 1
+/* Square 2D fields small enough for one CTA's shared memory (FP32 up to 128x128 with one
+ * component, 16-byte types up to 64x64) run every step of a gpe_run call in one resident
+ * launch, one CTA per trajectory.  This flag forces the two-pass HBM path instead. */
+#define GPE_FLAG_NO_RESIDENT 2
 
 /* table kinds: what the user closure returned per grid point */
 #define GPE_TABLE_NONE 0
@@ -172,10 +176,35 @@ int gpe_norm(gpe_handle* h, double* out);
  * out[2] = potential sum_r u^H V u dV (needs gpe_set_potential), FP64. */
 int gpe_energy(gpe_handle* h, double* out);
 
+/* ---- graphs, asynchronous runs, ensembles -------------------------------- */
+/* Graph mode: runs of a multiple of steps_per_graph steps (no saves, no replay) replay a
+ * CUDA graph captured once from steps_per_graph steps; the kernels read the step index
+ * from a device counter, so one graph serves every position.  0 turns it off. */
+int gpe_set_graph(gpe_handle* h, int64_t steps_per_graph);
+/* Enqueue nsteps steps on the handle's stream and return (no saves, no replayed noise);
+ * gpe_wait blocks until they are done. */
+int gpe_run_async(gpe_handle* h, int64_t nsteps);
+int gpe_wait(gpe_handle* h);
+/* Several handles (e.g. trajectory groups on grids of different sizes) advanced together
+ * by ONE captured CUDA graph: each handle's chunk of steps_per_graph steps runs on its own
+ * stream inside the graph (small square grids as one resident launch, larger ones as
+ * their pass chain), forked from and joined to the first handle's stream.  The handles
+ * stay usable on their own; gpe_ensemble_run waits for completion.  The extension of the
+ * reference's batching over trailing dims (docs/src/stochastic_simulations.md:36-48) to
+ * grids of different sizes. */
+typedef struct gpe_ensemble gpe_ensemble;
+int gpe_ensemble_create(gpe_handle* const* handles, int n, gpe_ensemble** out);
+int gpe_ensemble_run(gpe_ensemble* e, int64_t nsteps, int64_t steps_per_graph);
+int gpe_ensemble_destroy(gpe_ensemble* e);
+const char* gpe_ensemble_last_error(const gpe_ensemble* e);
+double gpe_ensemble_last_run_ms(const gpe_ensemble* e);
+int64_t gpe_ensemble_last_run_launches(const gpe_ensemble* e);
+
 /* Per-launch timing for benchmarks: when on, gpe_run* brackets every kernel launch
  * with CUDA events on the handle's stream.  gpe_kernel_times then gives, for the last
  * run, ms[k] = summed device time and n[k] = launches of kernel kind k:
- * 0 = row pass (x lines), 1 = column pass (y lines), 2 = resident 1D / pointwise. */
+ * 0 = row pass (x lines), 1 = column pass (y lines), 2 = resident (1D lines, 2D planes,
+ * pointwise-only problems). */
 int gpe_set_timing(gpe_handle* h, int on);
 int gpe_kernel_times(const gpe_handle* h, double* ms, int64_t* n);
 

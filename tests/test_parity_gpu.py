@@ -22,9 +22,10 @@ PRECISIONS = [(np.complex128, "dw"), (np.complex128, "native"), (np.complex64, "
 PREC_IDS = ["c128-dw", "c128-native", "c64"]
 
 
-def run_both(gpe, oracle, gpu_kw, orc, tspan, dt, nsaves, save_start=True, xi=None, rng=None, fp64="dw"):
+def run_both(gpe, oracle, gpu_kw, orc, tspan, dt, nsaves, save_start=True, xi=None, rng=None, fp64="dw",
+             resident=True):
     prob = gpe.GrossPitaevskiiProblem(**gpu_kw)
-    kw = {}
+    kw = {"resident": resident}
     if xi is not None:
         kw["noise_replay"] = lambda h: np.ascontiguousarray(xi(h))
     ts, res = gpe.solve(prob, gpe.StrangSplitting(), tspan, dt=dt, nsaves=nsaves, save_start=save_start, rng=rng,
@@ -88,11 +89,15 @@ def test_polariton_matrix_dispersion_pump_ramp(gpe, oracle, lib, dtype, fp64):
         assert_close(oracle, res, ores, fp32_tol(oracle, orc, (0.0, 10.0), 0.05, 10), per_save=False)
 
 
+@pytest.mark.parametrize("resident", [True, False], ids=["resident", "two-pass"])
 @pytest.mark.parametrize("fp64", FP64_MODES)
 @pytest.mark.parametrize("N", [16, 32, 64, 256, 512, 1024])
-def test_kerr_sizes(gpe, oracle, lib, N, fp64):
+def test_kerr_sizes(gpe, oracle, lib, N, fp64, resident):
+    """Square grids up to 64^2 run in the resident plane kernel unless resident=False."""
+    if resident is False and N > 64:
+        pytest.skip("larger grids always take the two-pass path")
     gpu_kw, orc = kerr2d(N, 8.0, -2.0, np.complex128)
-    ts, res, ots, ores = run_both(gpe, oracle, gpu_kw, orc, (0.0, 0.05), 0.005, 2, fp64=fp64)
+    ts, res, ots, ores = run_both(gpe, oracle, gpu_kw, orc, (0.0, 0.05), 0.005, 2, fp64=fp64, resident=resident)
     assert_close(oracle, res, ores, 1e-10)
 
 
@@ -275,3 +280,32 @@ def test_norm_matches_oracle(gpe, oracle, lib, fp64):
     it.close()
     ref = oracle.norm(u, (8.0, 8.0), 2)
     assert abs(nrm[0] - ref) <= 1e-12 * ref
+
+
+@pytest.mark.parametrize("N,dtype,M", [(64, np.complex64, 1), (128, np.complex64, 1), (64, np.complex64, 2),
+                                       (64, np.complex128, 1), (32, np.complex128, 2)])
+def test_resident_plane_matches_two_pass(gpe, oracle, lib, N, dtype, M):
+    """The resident plane kernel (whole trajectory in shared memory) and the two-pass HBM
+    path agree: same half steps, pump, Philox noise and saves; only the FFT radix split
+    differs (8 vs 16 points per thread), so they agree to rounding."""
+    L = 16.0
+    rng = np.random.default_rng(4)
+    B = 3
+    u0 = [jl(1.0 + 0.1 * (rng.standard_normal((B, N, N)) + 1j * rng.standard_normal((B, N, N)))).astype(dtype)
+          for _ in range(M)]
+    disp = (lambda k, p: (k[0] ** 2 + k[1] ** 2) / 2 - 0.1j) if M == 1 else \
+        (lambda k, p: [[(k[0] ** 2 + k[1] ** 2) / 2 - 0.1j, 0.3], [0.3, (k[0] ** 2 + k[1] ** 2) / 4 - 0.05j]])
+    nl = (lambda u, p: 0.01 * np.abs(u[0]) ** 2) if M == 1 else \
+        (lambda u, p: [0.01 * np.abs(u[0]) ** 2, 0.02 * np.abs(u[1]) ** 2 + 0.01 * np.abs(u[0]) ** 2])
+    pump = (lambda r, p, t: 1.0 + 0 * r[0]) if M == 1 else (lambda r, p, t: [min(t, 1.0) + 0 * r[0], 0])
+    kw = dict(u0=tuple(u0), lengths=(L, L), dispersion=disp, nonlinearity=nl, pump=pump,
+              position_noise_func=lambda u, r, p: 0.2)
+    prob = gpe.GrossPitaevskiiProblem(**kw)
+    out = {}
+    for resident in (True, False):
+        ts, res = gpe.solve(prob, gpe.StrangSplitting(), (0.0, 0.4), dt=0.02, nsaves=4, rng=123, resident=resident)
+        out[resident] = res
+    tol = 2e-5 if dtype == np.complex64 else 1e-12
+    for m in range(M):
+        a, b = out[True][m].astype(np.complex128), out[False][m].astype(np.complex128)
+        assert oracle.rel_l2(a, b) <= tol

@@ -1,0 +1,104 @@
+"""Truncated-Wigner ensembles: groups on grids of different sizes advanced by one CUDA
+graph (gpe_ensemble_run), checked against plain stepping, against the FP64 oracle per
+trajectory (replayed noise) and statistically (independent noise)."""
+import math
+
+import numpy as np
+import pytest
+
+from cases import c_order, jl
+
+pytestmark = pytest.mark.gpu
+
+
+def twa(gpe):
+    return __import__("gpe_gb300.twa", fromlist=["Ensemble"])
+
+
+def test_ensemble_graph_equals_plain_stepping(gpe, lib):
+    """Graph replay (device step counter) reproduces un-captured stepping bit for bit,
+    for resident (32^2, 64^2, 128^2 FP32) and two-pass (256^2) groups in one graph."""
+    T = twa(gpe)
+    prm = T.DampedDrivenParams()
+    sizes = [(32, 6), (64, 4), (128, 2), (256, 2)]
+    nsteps = 40
+    graph_its = [T.make_group(N, B, prm, nsteps, seed=N) for N, B in sizes]
+    ens = T.Ensemble(graph_its)
+    ens.run(nsteps, 10)
+    assert ens.last_run_launches() > 0
+    ens.close()
+    for (N, B), git in zip(sizes, graph_its):
+        it = T.make_group(N, B, prm, nsteps, seed=N)
+        it.step(nsteps)
+        a, b = git.get_fields()[0], it.get_fields()[0]
+        assert np.array_equal(a, b), f"N={N}"
+        assert git.state().steps == nsteps
+        it.close()
+        git.close()
+
+
+def test_resident_and_two_pass_groups_agree(gpe, oracle, lib):
+    T = twa(gpe)
+    prm = T.DampedDrivenParams()
+    for N in (64, 128):
+        a = T.make_group(N, 3, prm, 60, seed=5, resident=True)
+        b = T.make_group(N, 3, prm, 60, seed=5, resident=False)
+        a.step(60)
+        b.step(60)
+        fa, fb = a.get_fields()[0].astype(np.complex128), b.get_fields()[0].astype(np.complex128)
+        assert oracle.rel_l2(fa, fb) <= 2e-5, N
+        a.close()
+        b.close()
+
+
+def test_twa_group_per_trajectory_replay_parity(gpe, oracle, lib):
+    """FP32 group with replayed noise against the FP64 oracle on the same u0 and xi."""
+    T = twa(gpe)
+    prm = T.DampedDrivenParams()
+    N, B, nsteps = 32, 4, 50
+    prob = T.wigner_problem(N, B, prm, seed=3, dtype=np.complex64)
+    rn = oracle.ReplayNoise(17, (1, B, N, N))
+    xi32 = lambda h: rn(h).astype(np.complex64).astype(np.complex128)
+    ts, res = gpe.solve(prob, gpe.StrangSplitting(), (0.0, nsteps * prm.dt), dt=prm.dt, nsaves=5,
+                        noise_replay=lambda h: np.ascontiguousarray(xi32(h)))
+    dV = (prm.L / N) ** 2
+    u0c = c_order(prob.u0[0]).astype(np.complex128)
+    orc = oracle.OracleProblem(u0=(u0c,), lengths=(prm.L, prm.L),
+                               dispersion=lambda k, p: (k[0] ** 2 + k[1] ** 2) / 2 - 0.5j * prm.gamma,
+                               nonlin_g=np.array([[prm.g]]), pump_profile=np.ones((1, N, N), np.complex128),
+                               pump_amp=lambda t: np.array([prm.F]), eta=np.array([math.sqrt(prm.gamma / (2 * dV))]))
+    ots, ores = oracle.solve(orc, (0.0, nsteps * prm.dt), prm.dt, 5, xi_source=xi32)
+    got = c_order(res[0]).astype(np.complex128)
+    for b in range(B):
+        e = oracle.rel_l2(got[:, b], ores[0][:, b])
+        assert e <= 1e-5, (b, e)
+
+
+def test_twa_density_statistics_match_fp64_ensemble(gpe, oracle, lib):
+    """Philox ensemble (GPU, FP32) vs an independent FP64 oracle ensemble (numpy noise):
+    the mean density and its variance agree within their standard errors."""
+    T = twa(gpe)
+    prm = T.DampedDrivenParams()
+    N, B, nsteps = 32, 512, 100
+    it = T.make_group(N, B, prm, nsteps, seed=11)
+    it.step(nsteps)
+    n_gpu = np.abs(it.get_fields()[0].astype(np.complex128)) ** 2  # (N, N, B)
+    it.close()
+    dV = (prm.L / N) ** 2
+    rng = np.random.default_rng(99)
+    xi0 = (rng.standard_normal((B, N, N)) + 1j * rng.standard_normal((B, N, N))) * math.sqrt(0.5)
+    u0c = 1.0 + xi0 / math.sqrt(2 * dV)
+    orc = oracle.OracleProblem(u0=(u0c,), lengths=(prm.L, prm.L),
+                               dispersion=lambda k, p: (k[0] ** 2 + k[1] ** 2) / 2 - 0.5j * prm.gamma,
+                               nonlin_g=np.array([[prm.g]]), pump_profile=np.ones((1, N, N), np.complex128),
+                               pump_amp=lambda t: np.array([prm.F]), eta=np.array([math.sqrt(prm.gamma / (2 * dV))]))
+    nrng = np.random.default_rng(7)
+    ts, ores = oracle.solve(orc, (0.0, nsteps * prm.dt), prm.dt, 1, save_start=False,
+                            xi_source=lambda h: oracle.complex_normal(nrng, (1, B, N, N)))
+    n_cpu = np.abs(ores[0, -1]) ** 2  # (B, N, N)
+    # trajectory-level means (spatial average per trajectory) are independent samples
+    mg, mc = n_gpu.mean(axis=(0, 1)), n_cpu.mean(axis=(1, 2))
+    se = math.sqrt(mg.var() / B + mc.var() / B)
+    assert abs(mg.mean() - mc.mean()) <= 5 * se + 1e-12
+    vg, vc = n_gpu.var(axis=-1).mean(), n_cpu.var(axis=0).mean()
+    assert abs(vg - vc) <= 0.1 * vc
