@@ -360,6 +360,7 @@ def run_twa(pkg, steps: int, tune: bool):
     A = __import__("gpe_gb300.autotune", fromlist=["tune"])
     prm = T.DampedDrivenParams()
     chunk = 50
+    tuned_chunks = []
     choices = {}
     its = []
     for N, B in TWA_GROUPS:
@@ -369,7 +370,10 @@ def run_twa(pkg, steps: int, tune: bool):
             resident, chunk_n, _ = A.tune(lambda r, N=N, B=B: T.make_group(N, B, prm, 400, seed=N, resident=r), k,
                                           trial_steps=200)
             choices[f"{N}x{N}"] = {"resident": resident, "steps_per_graph": chunk_n}
-        its.append(T.make_group(N, B, prm, steps + 2 * chunk, seed=N, resident=resident))
+            tuned_chunks.append(chunk_n)
+        its.append(T.make_group(N, B, prm, steps + 400, seed=N, resident=resident))
+    if tuned_chunks and steps % min(tuned_chunks) == 0:
+        chunk = min(tuned_chunks)  # one graph serves every group: the shortest tuned chunk
     ens = T.Ensemble(its)
     ens.run(chunk, chunk)  # capture + warm-up
     ens.run(steps, chunk)

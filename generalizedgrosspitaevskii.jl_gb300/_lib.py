@@ -97,6 +97,7 @@ SIGNATURES = {
     "gpe_set_state": (c_int, [H, POINTER(GpeState)]),
     "gpe_norm": (c_int, [H, c_void_p]),
     "gpe_energy": (c_int, [H, c_void_p]),
+    "gpe_spectral_moments": (c_int, [H, c_int, c_void_p, c_void_p]),
     "gpe_set_graph": (c_int, [H, c_int64]),
     "gpe_run_async": (c_int, [H, c_int64]),
     "gpe_wait": (c_int, [H]),

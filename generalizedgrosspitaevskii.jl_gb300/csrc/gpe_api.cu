@@ -107,6 +107,10 @@ struct gpe_handle {
   int64_t kval = 0;
   cudaGraphExec_t gexec = nullptr;
   int64_t glaunches = 0;
+  // energy diagnostics: transformed copy of the state, FP64 D and V samples on the device
+  void* escr[2] = {nullptr, nullptr};
+  double2* dsamp = nullptr;
+  double2* vsamp = nullptr;
   std::string err;
 };
 
@@ -251,7 +255,6 @@ int gpe_create(const gpe_desc* desc, gpe_handle** out) {
   if (desc->batch < 1) return fail(nullptr, GPE_ERR_INVALID, "batch must be >= 1");
   if (!(desc->dt > 0) || !std::isfinite(desc->dt)) return fail(nullptr, GPE_ERR_INVALID, "dt must be positive and finite");
   if (!std::isfinite(desc->t0)) return fail(nullptr, GPE_ERR_INVALID, "t0 must be finite");
-  if (desc->ndim == 3) return fail(nullptr, GPE_ERR_UNSUPPORTED, "3D grids are not supported by this build");
   for (int a = 0; a < desc->ndim; ++a) {
     if (!is_pow2(desc->n[a]) || desc->n[a] < 16 || desc->n[a] > 4096)
       return fail(nullptr, GPE_ERR_UNSUPPORTED, "axis %d: n = %lld, need a power of two in [16, 4096]", a, (long long)desc->n[a]);
@@ -443,6 +446,8 @@ int gpe_set_dispersion(gpe_handle* h, const double* D, int kind) {
   const int stored = build_cis(h, D, kind, h->d.dt, 1.0 / (double)h->P, tab);
   h->Dsamples.assign(reinterpret_cast<const cd*>(D), reinterpret_cast<const cd*>(D) + ne);
   h->dkind = kind;
+  cudaFree(h->dsamp);
+  h->dsamp = nullptr;
   return store_ktable(h, tab, stored);
 }
 
@@ -487,6 +492,8 @@ int gpe_set_potential(gpe_handle* h, const double* V, int kind) {
   const int stored = build_cis(h, V, kind, 0.5 * h->d.dt, 1.0, tab);
   h->Vsamples.assign(reinterpret_cast<const cd*>(V), reinterpret_cast<const cd*>(V) + ne);
   h->vskind = kind;
+  cudaFree(h->vsamp);
+  h->vsamp = nullptr;
   return store_vtable(h, tab, stored);
 }
 
@@ -741,7 +748,8 @@ static int enqueue_steps(gpe_handle* h, int64_t nsteps, int64_t save_every, void
     *launches = 1;
     return GPE_OK;
   }
-  // 2D: entry row pass, then (column pass, row pass) per step
+  // 2D / 3D: entry row pass, then (column pass(es), row pass) per step.  3D column
+  // passes: FFT_y, then FFT_z * table * iFFT_z, then iFFT_y.
   const int64_t nrows = h->P / h->n[0] * h->B;
   PassArgs r = a;
   r.tw = h->tw[0];
@@ -754,17 +762,40 @@ static int enqueue_steps(gpe_handle* h, int64_t nsteps, int64_t save_every, void
     LK(h, gpe::launch_row(h->prec, h->M, h->logn[0], r, nrows, h->stream));
   }
   ++nl;
-  PassArgs c = a;
-  c.tw = h->tw[1];
-  c.ld = h->n[0];
-  c.ostride = 0;
-  c.nouter = 1;
-  c.col_fwd = 1;
-  c.col_inv = 1;
+  std::vector<std::pair<PassArgs, int>> cols;  // (args, log2 line length)
+  if (h->ndim == 2) {
+    PassArgs c = a;
+    c.tw = h->tw[1];
+    c.ld = h->n[0];
+    c.ostride = 0;
+    c.nouter = 1;
+    c.col_fwd = c.col_inv = 1;
+    cols.push_back({c, h->logn[1]});
+  } else {
+    PassArgs y = a;  // lines along y at fixed z
+    y.tw = h->tw[1];
+    y.ld = h->n[0];
+    y.ostride = h->n[0] * h->n[1];
+    y.nouter = h->n[2];
+    y.ktab = nullptr;
+    PassArgs z = a;  // lines along z at fixed y, carrying the k-space table
+    z.tw = h->tw[2];
+    z.ld = h->n[0] * h->n[1];
+    z.ostride = h->n[0];
+    z.nouter = h->n[1];
+    z.col_fwd = z.col_inv = 1;
+    PassArgs yf = y, yi = y;
+    yf.col_fwd = 1;
+    yi.col_inv = 1;
+    cols.push_back({yf, h->logn[1]});
+    cols.push_back({z, h->logn[2]});
+    cols.push_back({yi, h->logn[1]});
+  }
   for (int64_t s = 0; s < nsteps; ++s) {
-    {
+    for (auto& cp : cols) {
       TimedLaunch tl(h, 1);
-      LK(h, gpe::launch_col(h->prec, h->M, h->logn[1], c, h->stream));
+      LK(h, gpe::launch_col(h->prec, h->M, cp.second, cp.first, h->stream));
+      ++nl;
     }
     const bool last = (s == nsteps - 1);
     PassArgs rr = a;
@@ -778,7 +809,7 @@ static int enqueue_steps(gpe_handle* h, int64_t nsteps, int64_t save_every, void
       TimedLaunch tl(h, 0);
       LK(h, gpe::launch_row(h->prec, h->M, h->logn[0], rr, nrows, h->stream));
     }
-    nl += 2;
+    ++nl;
   }
   *launches = nl;
   return GPE_OK;
@@ -957,10 +988,66 @@ int gpe_norm(gpe_handle* h, double* out) {
   return GPE_OK;
 }
 
+// escr[m] <- unnormalised spatial FFT of u[m] (all trajectories), with the pass kernels.
+static int transform_copy(gpe_handle* h) {
+  const size_t plane_bytes = (size_t)h->P * h->B * h->csz;
+  for (int m = 0; m < h->M; ++m) {
+    if (!h->escr[m]) CK(h, cudaMalloc(&h->escr[m], plane_bytes));
+    CK(h, cudaMemcpyAsync(h->escr[m], h->u[m], plane_bytes, cudaMemcpyDeviceToDevice, h->stream));
+  }
+  PassArgs f = base_args(h);
+  for (int m = 0; m < h->M; ++m) f.u[m] = h->escr[m];
+  f.ktab = nullptr;
+  f.noise = 0;
+  f.hA = f.hB = -1;
+  PassArgs r = f;
+  r.tw = h->tw[0];
+  r.do_fft = 1;
+  LK(h, gpe::launch_row(h->prec, h->M, h->logn[0], r, h->P / h->n[0] * h->B, h->stream));
+  for (int ax = 1; ax < h->ndim; ++ax) {
+    PassArgs c = f;
+    c.tw = h->tw[ax];
+    c.col_fwd = 1;
+    c.ld = ax == 1 ? h->n[0] : h->n[0] * h->n[1];
+    c.ostride = (h->ndim == 3) ? (ax == 1 ? h->n[0] * h->n[1] : h->n[0]) : 0;
+    c.nouter = (h->ndim == 3) ? (ax == 1 ? h->n[2] : h->n[1]) : 1;
+    LK(h, gpe::launch_col(h->prec, h->M, h->logn[ax], c, h->stream));
+  }
+  return GPE_OK;
+}
+
 int gpe_energy(gpe_handle* h, double* out) {
   if (!h) return GPE_ERR_INVALID;
-  (void)out;
-  return fail(h, GPE_ERR_UNSUPPORTED, "gpe_energy is not available in this build");
+  if (!out) return fail(h, GPE_ERR_INVALID, "null output");
+  CK(h, cudaSetDevice(h->dev));
+  if (h->ktab && h->Dsamples.empty())
+    return fail(h, GPE_ERR_UNSUPPORTED, "energy needs the dispersion samples (gpe_set_dispersion), not a finished table");
+  if (h->vtab && h->Vsamples.empty())
+    return fail(h, GPE_ERR_UNSUPPORTED, "energy needs the potential samples (gpe_set_potential), not a finished table");
+  if (!h->Dsamples.empty() && !h->dsamp) {
+    CK(h, cudaMalloc((void**)&h->dsamp, h->Dsamples.size() * sizeof(double2)));
+    CK(h, cudaMemcpy(h->dsamp, h->Dsamples.data(), h->Dsamples.size() * sizeof(double2), cudaMemcpyHostToDevice));
+  }
+  if (!h->Vsamples.empty() && !h->vsamp) {
+    CK(h, cudaMalloc((void**)&h->vsamp, h->Vsamples.size() * sizeof(double2)));
+    CK(h, cudaMemcpy(h->vsamp, h->Vsamples.data(), h->Vsamples.size() * sizeof(double2), cudaMemcpyHostToDevice));
+  }
+  // the kinetic term needs u~: transform a copy of the state with the pass kernels
+  if (h->dsamp) {
+    int rc = transform_copy(h);
+    if (rc) return rc;
+  }
+  CK(h, cudaMemsetAsync(h->red, 0, 4 * sizeof(double), h->stream));
+  PassArgs a = base_args(h);
+  LK(h, gpe::launch_energy_sums(h->prec, h->M, h->escr, h->u, h->P, h->B, h->dsamp, h->dkind, h->vsamp, h->vskind, a,
+                                h->red, h->stream));
+  double tmp[4];
+  CK(h, cudaMemcpyAsync(tmp, h->red, 4 * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+  CK(h, cudaStreamSynchronize(h->stream));
+  out[0] = tmp[0] * h->dV / (double)h->P;
+  out[1] = tmp[1] * h->dV;
+  out[2] = tmp[2] * h->dV;
+  return GPE_OK;
 }
 
 int gpe_set_graph(gpe_handle* h, int64_t steps_per_graph) {
@@ -1017,6 +1104,34 @@ int gpe_set_timing(gpe_handle* h, int on) {
 int gpe_kernel_times(const gpe_handle* h, double* ms, int64_t* n) {
   if (!h || !ms || !n) return GPE_ERR_INVALID;
   for (int k = 0; k < 3; ++k) { ms[k] = h->kms[k]; n[k] = h->kn[k]; }
+  return GPE_OK;
+}
+
+int gpe_spectral_moments(gpe_handle* h, int comp, double* mean_out, double* second_out) {
+  int rc = check_comp(h, comp);
+  if (rc) return rc;
+  if (!mean_out) return fail(h, GPE_ERR_INVALID, "null output");
+  if (second_out && h->P > 8192) return fail(h, GPE_ERR_INVALID, "the second-moment matrix needs P <= 8192 points");
+  rc = transform_copy(h);
+  if (rc) return rc;
+  double *nb = nullptr, *mean = nullptr, *second = nullptr;
+  const size_t P = (size_t)h->P;
+  if (cudaMalloc((void**)&nb, P * h->B * sizeof(double)) != cudaSuccess ||
+      cudaMalloc((void**)&mean, P * sizeof(double)) != cudaSuccess ||
+      (second_out && cudaMalloc((void**)&second, P * P * sizeof(double)) != cudaSuccess)) {
+    cudaFree(nb);
+    cudaFree(mean);
+    cudaFree(second);
+    return fail(h, GPE_ERR_NOMEM, "device allocation for spectral moments failed");
+  }
+  int lrc = gpe::launch_spectral_moments(h->prec, h->escr[comp], h->P, h->B, nb, mean, second, h->stream);
+  cudaError_t e = lrc ? (cudaError_t)lrc : cudaStreamSynchronize(h->stream);
+  if (e == cudaSuccess) e = cudaMemcpy(mean_out, mean, P * sizeof(double), cudaMemcpyDeviceToHost);
+  if (e == cudaSuccess && second_out) e = cudaMemcpy(second_out, second, P * P * sizeof(double), cudaMemcpyDeviceToHost);
+  cudaFree(nb);
+  cudaFree(mean);
+  cudaFree(second);
+  if (e != cudaSuccess) return fail(h, GPE_ERR_CUDA, "spectral moments failed: %s", cudaGetErrorString(e));
   return GPE_OK;
 }
 

@@ -81,6 +81,15 @@ int launch_plane(int dtype, int M, int logn, const PassArgs& a, cudaStream_t s);
 bool plane_fits(int dtype, int M, int logn);
 // FP64 reductions: out[m] += sum |u_m|^2 (device double array of M entries)
 int launch_norm(int dtype, int M, const PassArgs& a, double* out, cudaStream_t s);
+// FP64 energy sums into out3[0..2] (kinetic on the transformed fields uk with D samples,
+// interaction on ur, potential on ur with V samples); D or V may be null
+int launch_energy_sums(int prec, int M, const void* const* uk, const void* const* ur, int64_t P, int64_t B,
+                       const double2* D, int dkind, const double2* V, int vkind, const PassArgs& a, double* out3,
+                       cudaStream_t s);
+// per-trajectory occupations nb = |u~|^2/P^2, their trajectory mean, and (second != null)
+// the matrix (1/B) sum_b nb[b][k] nb[b][k']
+int launch_spectral_moments(int prec, const void* uk, int64_t P, int64_t B, double* nb, double* mean, double* second,
+                            cudaStream_t s);
 // *k += n on the device (end of a captured chunk of n steps)
 int launch_advance(int64_t* k, int64_t n, cudaStream_t s);
 // FP64 <-> double-word conversion of n complex numbers

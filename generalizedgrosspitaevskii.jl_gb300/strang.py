@@ -198,6 +198,12 @@ class StrangSplittingIterator:
         L.check(self.lib, self.h, self.lib.gpe_norm(self.h, L.ptr(out)))
         return out[: self.prob.M].copy()
 
+    def energy(self) -> np.ndarray:
+        """[kinetic, interaction, potential] energies of the current state (gpe_energy)."""
+        out = np.zeros(4, np.float64)
+        L.check(self.lib, self.h, self.lib.gpe_energy(self.h, L.ptr(out)))
+        return out[:3].copy()
+
     def last_run_ms(self) -> float:
         return float(self.lib.gpe_last_run_ms(self.h))
 

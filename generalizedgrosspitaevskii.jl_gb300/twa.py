@@ -115,3 +115,32 @@ def plain_per_trajectory_rate(N: int, prm: DampedDrivenParams, ntraj: int, nstep
         total_ms += it.last_run_ms()
         it.close()
     return ntraj * nsteps / (total_ms * 1e-3)
+
+
+def spectral_moments(it: StrangSplittingIterator, comp: int = 0, second: bool = True):
+    """GPU trajectory statistics of n_b(k) = |FFT(u)_b(k)|^2 / P^2 (k in FFT order):
+    returns (mean over trajectories, and the matrix (1/B) sum_b n_b(k) n_b(k') or None)."""
+    lib = it.lib
+    P = it.P
+    mean = np.zeros(P)
+    sec = np.zeros((P, P)) if second else None
+    L.check(lib, it.h, lib.gpe_spectral_moments(it.h, comp, L.ptr(mean), L.ptr(sec)))
+    return mean, sec
+
+
+def momentum_statistics(it: StrangSplittingIterator, commutator: float, comp: int = 0):
+    """n(k) and g2(k, k') of a 1D ensemble as the reference's truncated-Wigner example
+    computes them (examples/truncated_wigner.jl:110-165): with psi(k) = fftshift(fft(u))/N,
+    n(k) = <|psi(k)|^2> - c/2 and G2(k,k') = <|psi(k)|^2 |psi(k')|^2 - (1 + delta_kk') c/2
+    (|psi(k)|^2 + |psi(k')|^2 - c/2)>, g2 = G2 / (n(k) n(k')), c = the commutator (1/L).
+    Returns (n, G2, g2) in fftshifted k order."""
+    if it.prob.N != 1:
+        raise ValueError("momentum_statistics follows the 1D example; use spectral_moments for other grids")
+    mean, sec = spectral_moments(it, comp, True)
+    mean = np.fft.fftshift(mean)
+    sec = np.fft.fftshift(sec)
+    c = commutator
+    nk = mean - c / 2
+    delta = np.eye(len(mean))
+    G2 = sec - (1 + delta) * c / 2 * (mean[:, None] + mean[None, :] - c / 2)
+    return nk, G2, G2 / np.outer(nk, nk)

@@ -171,10 +171,19 @@ int gpe_get_state(gpe_handle* h, gpe_state* st);
 int gpe_set_state(gpe_handle* h, const gpe_state* st);
 /* out[m] = sum over batch and grid of |u_m|^2 dV, accumulated in FP64 on the device. */
 int gpe_norm(gpe_handle* h, double* out);
-/* out[0] = kinetic sum_k u~^H D(k) u~ dV/P (real part; needs gpe_set_dispersion),
- * out[1] = interaction sum_r sum_j (1/2) Re(g_jl) |u_j|^2 |u_l|^2 dV,
- * out[2] = potential sum_r u^H V u dV (needs gpe_set_potential), FP64. */
+/* out[0] = kinetic Re sum_k u~^H D(k) u~ dV/P (u~ the unnormalised FFT; needs the samples
+ *          of gpe_set_dispersion),
+ * out[1] = interaction sum_r sum_j [(1/2) sum_l Re(g_jl) |u_l|^2 + Re(c_j)] |u_j|^2 dV,
+ * out[2] = potential Re sum_r u^H V(r) u dV (needs gpe_set_potential samples).
+ * Summed over the batch, accumulated in FP64 on the device. */
 int gpe_energy(gpe_handle* h, double* out);
+
+/* Momentum-space statistics over the trajectories (the post-processing of the reference's
+ * truncated-Wigner example, examples/truncated_wigner.jl:110-165): with n_b(k) =
+ * |FFT(u_comp)_b(k)|^2 / P^2 for trajectory b (FFT unnormalised, k in FFT order),
+ * mean_out[k] = (1/B) sum_b n_b(k) (P values) and, if second_out is not NULL,
+ * second_out[k*P + k'] = (1/B) sum_b n_b(k) n_b(k') (P*P values, P <= 8192). */
+int gpe_spectral_moments(gpe_handle* h, int comp, double* mean_out, double* second_out);
 
 /* ---- graphs, asynchronous runs, ensembles -------------------------------- */
 /* Graph mode: runs of a multiple of steps_per_graph steps (no saves, no replay) replay a

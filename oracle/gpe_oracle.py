@@ -535,3 +535,38 @@ def solve_fp32(prob: OracleProblem, tspan, dt: float, nsaves: int, save_start: b
     it = Fp32Iterator(prob, tspan, dt, nsaves, save_start, xi_source)
     it.u = it.u.astype(np.complex64)
     return it.solve()
+
+
+# --------------------------------------------------------------------------- energy
+def energy(it: "OracleIterator", u: Optional[np.ndarray] = None) -> np.ndarray:
+    """[kinetic, interaction, potential] of the state u (M, *batch, *spatial), FP64, summed
+    over the batch: kinetic = Re sum_k u~^H D u~ dV / P, interaction = sum_j [(1/2) sum_l
+    Re g_jl |u_l|^2 + Re c_j] |u_j|^2 dV, potential = Re sum_r u^H V u dV."""
+    p = it.prob
+    u = it.u if u is None else u
+    nd = p.ndim
+    sp = u.shape[-nd:]
+    dV = float(np.prod([L / n for L, n in zip(p.lengths, reversed(sp))]))
+    P = int(np.prod(sp))
+    out = np.zeros(3)
+    M = u.shape[0]
+
+    def quad(T, kind, v):
+        if kind == "scalar":
+            return sum(np.real(np.conj(v[m]) * T * v[m]).sum() for m in range(M))
+        if kind == "diag":
+            return sum(np.real(np.conj(v[m]) * T[m] * v[m]).sum() for m in range(M))
+        return sum(np.real(np.conj(v[i]) * T[i, j] * v[j]).sum() for i in range(M) for j in range(M))
+
+    if p.dispersion is not None:
+        D, kind = sample_on_grid(p.dispersion, it.rg, p.param, M)
+        ft = np.fft.fftn(u, axes=tuple(range(-nd, 0)))
+        out[0] = quad(D, kind, ft) * dV / P
+    g = np.zeros((M, M)) if p.nonlin_g is None else np.real(np.asarray(p.nonlin_g))
+    c = np.zeros(M) if p.nonlin_c is None else np.real(np.asarray(p.nonlin_c))
+    d = np.abs(u) ** 2
+    out[1] = sum(((0.5 * sum(g[j, l] * d[l] for l in range(M)) + c[j]) * d[j]).sum() for j in range(M)) * dV
+    if p.potential is not None:
+        V, kind = sample_on_grid(p.potential, it.dg, p.param, M)
+        out[2] = quad(V, kind, u) * dV
+    return out

@@ -309,3 +309,52 @@ def test_resident_plane_matches_two_pass(gpe, oracle, lib, N, dtype, M):
     for m in range(M):
         a, b = out[True][m].astype(np.complex128), out[False][m].astype(np.complex128)
         assert oracle.rel_l2(a, b) <= tol
+
+
+@pytest.mark.parametrize("fp64", FP64_MODES)
+@pytest.mark.parametrize("shape", [(32, 16, 16), (16, 32, 64)])
+def test_3d_grids(gpe, oracle, lib, shape, fp64):
+    """3D: x row pass, y forward / z forward-table-inverse / y inverse column passes."""
+    nx, ny, nz = shape
+    L = (8.0, 6.0, 5.0)
+    X, Y, Z = oracle.mesh(oracle.grids(L, (nx, ny, nz))[0])  # C order (nz, ny, nx)
+    u0c = (np.exp(-((X - 4) ** 2 + (Y - 3) ** 2 + (Z - 2.5) ** 2)) * np.exp(1j * X)).astype(np.complex128)
+    disp = lambda k, p: (k[0] ** 2 + k[1] ** 2 + 2 * k[2] ** 2) / 2
+    pot = lambda r, p: 0.1 * (r[2] - 2.5) ** 2
+    gkw = dict(u0=(jl(u0c),), lengths=L, dispersion=disp, potential=pot,
+               nonlinearity=lambda u, p: -1.5 * np.abs(u[0]) ** 2)
+    orc = oracle.OracleProblem(u0=(u0c,), lengths=L, dispersion=disp, potential=pot, nonlin_g=np.array([[-1.5]]))
+    ts, res, ots, ores = run_both(gpe, oracle, gkw, orc, (0.0, 0.2), 0.01, 4, fp64=fp64)
+    assert res[0].shape == (nx, ny, nz, 5)
+    assert_close(oracle, res, ores, 1e-10)
+
+
+@pytest.mark.parametrize("dtype,fp64", PRECISIONS, ids=PREC_IDS)
+@pytest.mark.parametrize("case", ["kerr2d", "polariton", "3d"])
+def test_energy_matches_oracle(gpe, oracle, lib, case, dtype, fp64):
+    if case == "kerr2d":
+        gkw, orc = kerr2d(64, 8.0, -2.0, dtype)
+        gkw["potential"] = orc.potential = (lambda r, p: 0.3 * ((r[0] - 4) ** 2 + (r[1] - 4) ** 2))
+    elif case == "polariton":
+        gkw, orc = polariton2d(N=64, L=128.0, A=5.0, ramp=20.0)
+        gkw["u0"] = tuple(u.astype(dtype) for u in gkw["u0"])
+    else:
+        L = (8.0, 6.0, 5.0)
+        X, Y, Z = oracle.mesh(oracle.grids(L, (32, 16, 16))[0])
+        u0c = (np.exp(-((X - 4) ** 2 + (Y - 3) ** 2 + (Z - 2.5) ** 2)) * np.exp(1j * Y)).astype(np.complex128)
+        disp = lambda k, p: (k[0] ** 2 + k[1] ** 2 + k[2] ** 2) / 2
+        gkw = dict(u0=(jl(u0c).astype(dtype),), lengths=L, dispersion=disp,
+                   nonlinearity=lambda u, p: 2.0 * np.abs(u[0]) ** 2 + 0.5)
+        orc = oracle.OracleProblem(u0=(u0c,), lengths=L, dispersion=disp, nonlin_g=np.array([[2.0]]),
+                                   nonlin_c=np.array([0.5]))
+    prob = gpe.GrossPitaevskiiProblem(**gkw)
+    it = gpe.init(prob, gpe.StrangSplitting(), (0.0, 0.2), dt=0.01, nsaves=2, fp64=fp64)
+    it.step(7)
+    e_gpu = it.energy()
+    u = np.stack([c_order(f).astype(np.complex128) for f in it.get_fields()])
+    it.close()
+    oit = oracle.OracleIterator(orc, (0.0, 0.2), 0.01, 2)
+    e_ref = oracle.energy(oit, u)
+    tol = 1e-10 if dtype == np.complex128 else 1e-5
+    scale = np.abs(e_ref).sum()
+    assert np.all(np.abs(e_gpu - e_ref) <= tol * scale), (e_gpu, e_ref)

@@ -102,3 +102,33 @@ def test_twa_density_statistics_match_fp64_ensemble(gpe, oracle, lib):
     assert abs(mg.mean() - mc.mean()) <= 5 * se + 1e-12
     vg, vc = n_gpu.var(axis=-1).mean(), n_cpu.var(axis=0).mean()
     assert abs(vg - vc) <= 0.1 * vc
+
+
+def test_momentum_statistics_match_numpy(gpe, lib):
+    """n(k), G2(k,k'), g2 of a 1D noisy ensemble computed on the GPU agree with the same
+    formulas evaluated in numpy on the fields (examples/truncated_wigner.jl:110-165)."""
+    T = twa(gpe)
+    N, B, L = 64, 256, 64.0
+    dx = L / N
+    rng = np.random.default_rng(2)
+    u0 = (rng.standard_normal((N, B)) + 1j * rng.standard_normal((N, B))) / math.sqrt(2 * dx)
+    hb = 0.6582
+    gam = 0.047 / hb
+    prob = gpe.GrossPitaevskiiProblem((np.asfortranarray(u0),), (L,),
+                                      dispersion=lambda k, p: hb * k[0] ** 2 / (2 / 6) - 0.49 / hb - 0.5j * gam,
+                                      nonlinearity=lambda u, p: 3e-4 / hb * (np.abs(u[0]) ** 2 - 1 / dx),
+                                      pump=lambda r, p, t: 10.0 + 0 * r[0],
+                                      position_noise_func=lambda u, r, p: math.sqrt(gam / (2 * dx)))
+    it = gpe.init(prob, gpe.StrangSplitting(), (0.0, 10.0), dt=0.05, nsaves=1, rng=5)
+    it.step(200)
+    nk, G2, g2 = T.momentum_statistics(it, 1 / L)
+    sol = it.get_fields()[0]
+    it.close()
+    ft = np.fft.fftshift(np.fft.fft(sol, axis=0), axes=0) / N
+    n_ref = (np.abs(ft) ** 2).mean(axis=1) - 1 / (2 * L)
+    a = np.abs(ft) ** 2
+    c = 1 / L
+    G2_ref = (a @ a.T) / B - (1 + np.eye(N)) * c / 2 * (a.mean(1)[:, None] + a.mean(1)[None, :] - c / 2)
+    assert np.allclose(nk, n_ref, rtol=1e-10, atol=1e-14)
+    assert np.allclose(G2, G2_ref, rtol=1e-9, atol=1e-13 * np.abs(G2_ref).max())
+    assert np.allclose(g2, G2_ref / np.outer(n_ref, n_ref), rtol=1e-8)
