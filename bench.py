@@ -399,6 +399,52 @@ def run_twa(pkg, steps: int, tune: bool):
             "speedup_vs_plain_per_trajectory": value / plain_value}
 
 
+def run_precision_sweep(args):
+    """Precision sweep: 2D Kerr on 2048^2 (L=32, u0 = exp(-|r - r0|^2 / 2^2), r0 = (16, 16),
+    D = |k|^2/2, G = g|u|^2, g = +1 and -2, dt = 0.005, 1000 steps, 20 saves) in FP32,
+    double-word FP64 and native FP64 on the GPU, against the FP64 oracle advanced in
+    lockstep on the host: rel L2 error, norm drift and energy drift at every save."""
+    import __graft_entry__ as G
+    pkg = G.load_package()
+    from oracle import gpe_oracle as O
+    N, Lb, dt, nsteps, nsaves = args.sweep_n, 32.0, 0.005, args.sweep_steps, 20
+    per = nsteps // nsaves
+    dg, _ = O.grids((Lb, Lb), (N, N))
+    X, Y = O.mesh(dg)
+    u0c = np.exp(-((X - 16) ** 2 + (Y - 16) ** 2) / 4.0).astype(np.complex128)
+    disp = lambda k, p: (k[0] ** 2 + k[1] ** 2) / 2
+    report = {"metric": "precision sweep", "grid": [N, N], "steps": nsteps, "saves": nsaves, "dt": dt, "cases": []}
+    cores = os.cpu_count() or 1
+    for g in (1.0, -2.0):
+        orc = O.OracleProblem(u0=(u0c,), lengths=(Lb, Lb), dispersion=disp, nonlin_g=np.array([[g]]))
+        oit = O.OracleIterator(orc, (0.0, nsteps * dt), dt, nsaves, fft_workers=cores)
+        modes = [("f32", np.complex64, "dw"), ("f64-dw", np.complex128, "dw"), ("f64-native", np.complex128, "native")]
+        its = {}
+        for name, dtype, fp64 in modes:
+            prob = pkg.GrossPitaevskiiProblem((np.asfortranarray(u0c.T).astype(dtype),), (Lb, Lb), dispersion=disp,
+                                              nonlinearity=lambda u, p, g=g: g * np.abs(u[0]) ** 2)
+            its[name] = pkg.init(prob, pkg.StrangSplitting(), (0.0, nsteps * dt), dt=dt, nsaves=nsaves, fp64=fp64)
+        e0 = {n: it.energy().sum() for n, it in its.items()}
+        n0 = {n: it.norm()[0] for n, it in its.items()}
+        rows = {n: [] for n in its}
+        t = 0.0
+        for s in range(nsaves):
+            for _ in range(per):
+                t += dt
+                oit.step(t, dt)
+            ref = oit.u[0]
+            for n, it in its.items():
+                it.step(per)
+                u = np.ascontiguousarray(it.get_fields()[0].T).astype(np.complex128)
+                rows[n].append({"t": round(t, 6), "rel_l2": O.rel_l2(u, ref),
+                                "norm_drift": float(it.norm()[0] / n0[n] - 1),
+                                "energy_drift": float((it.energy().sum() - e0[n]) / abs(e0[n]))})
+        for n, it in its.items():
+            it.close()
+        report["cases"].append({"g": g, "modes": rows})
+    print(json.dumps(report), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -413,10 +459,18 @@ def main():
     ap.add_argument("--twa-steps", type=int, default=2000,
                     help="steps of the batched truncated-Wigner ensemble measurement (0 skips it)")
     ap.add_argument("--no-tune", action="store_true", help="skip the ensemble autotuner")
+    ap.add_argument("--precision-sweep", action="store_true",
+                    help="print the FP32 / FP64 precision sweep on 2D Kerr instead of the throughput line")
+    ap.add_argument("--sweep-n", type=int, default=2048)
+    ap.add_argument("--sweep-steps", type=int, default=1000)
     args = ap.parse_args()
     if args.warmup < 3:
         ap.error("--warmup must be >= 3")
     rank, world, local_rank = dist_env()
+    if args.precision_sweep:
+        if rank == 0:
+            run_precision_sweep(args)
+        return
     if args.impl == "reference":
         run_reference(args, rank, world)
         return

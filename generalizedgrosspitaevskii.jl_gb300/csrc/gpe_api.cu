@@ -88,6 +88,11 @@ struct gpe_handle {
   int64_t steps = 0;
   void* save_buf = nullptr;
   size_t save_cap = 0;
+  // save ring: pinned host staging, copy stream and per-slot events (see SaveRing)
+  void* pinned = nullptr;
+  size_t pinned_cap = 0;
+  cudaStream_t cstream = nullptr;
+  std::vector<cudaEvent_t> ring_ready, ring_done;
   void* xi_buf = nullptr;
   size_t xi_cap = 0;
   double* red = nullptr;  // reduction scratch (4 doubles)
@@ -335,6 +340,10 @@ int gpe_destroy(gpe_handle* h) {
   cudaFree(h->ktab);
   cudaFree(h->vtab);
   cudaFree(h->save_buf);
+  if (h->pinned) cudaFreeHost(h->pinned);
+  for (cudaEvent_t e : h->ring_ready) cudaEventDestroy(e);
+  for (cudaEvent_t e : h->ring_done) cudaEventDestroy(e);
+  if (h->cstream) cudaStreamDestroy(h->cstream);
   cudaFree(h->xi_buf);
   cudaFree(h->red);
   for (cudaEvent_t e : h->evpool) cudaEventDestroy(e);
@@ -701,8 +710,54 @@ static int ensure(gpe_handle* h, void** buf, size_t* cap, size_t bytes) {
 
 // Enqueue nsteps steps; saves go to save_dev (layout [m][slot][b][p]) with nsaves_total
 // slots per component.  Returns the number of launches in *launches.
+// Saves of a long two-pass run with a host output go through a ring of kSaveRing device
+// slots: after the row pass that writes save s, a copy stream moves the slot to pinned
+// host memory while the next steps run; the host moves finished slots into the caller's
+// buffer and stays at most kSaveRing saves ahead, and the compute stream waits for a
+// slot's copy before overwriting it.  Device memory for saves stays kSaveRing slots
+// however many saves the run has.
+constexpr int64_t kSaveRing = 4;
+
+struct SaveRing {
+  gpe_handle* h;
+  int64_t nsaves;
+  size_t plane_bytes;
+  char* out;
+  int64_t drained = 0;
+
+  int before(int64_t s) {
+    if (s < kSaveRing) return GPE_OK;
+    int rc = drain(s - kSaveRing + 1);
+    if (rc) return rc;
+    CK(h, cudaStreamWaitEvent(h->stream, h->ring_done[s % kSaveRing], 0));
+    return GPE_OK;
+  }
+  int after(int64_t s) {
+    const int64_t r = s % kSaveRing;
+    CK(h, cudaEventRecord(h->ring_ready[r], h->stream));
+    CK(h, cudaStreamWaitEvent(h->cstream, h->ring_ready[r], 0));
+    for (int m = 0; m < h->M; ++m) {
+      const size_t off = ((size_t)m * kSaveRing + r) * plane_bytes;
+      CK(h, cudaMemcpyAsync((char*)h->pinned + off, (char*)h->save_buf + off, plane_bytes, cudaMemcpyDeviceToHost,
+                            h->cstream));
+    }
+    CK(h, cudaEventRecord(h->ring_done[r], h->cstream));
+    return GPE_OK;
+  }
+  int drain(int64_t upto) {
+    for (; drained < upto; ++drained) {
+      const int64_t r = drained % kSaveRing;
+      CK(h, cudaEventSynchronize(h->ring_done[r]));
+      for (int m = 0; m < h->M; ++m)
+        memcpy(out + ((size_t)m * nsaves + drained) * plane_bytes,
+               (char*)h->pinned + ((size_t)m * kSaveRing + r) * plane_bytes, plane_bytes);
+    }
+    return GPE_OK;
+  }
+};
+
 static int enqueue_steps(gpe_handle* h, int64_t nsteps, int64_t save_every, void* save_dev, int64_t nsaves_total,
-                         const void* xi_dev, int64_t* launches, bool relative = false) {
+                         const void* xi_dev, int64_t* launches, bool relative = false, SaveRing* ring = nullptr) {
   PassArgs a = base_args(h);
   // relative: step indices count from the value in h->kdev (graph capture)
   const int64_t k0 = relative ? 0 : h->steps;
@@ -804,10 +859,22 @@ static int enqueue_steps(gpe_handle* h, int64_t nsteps, int64_t save_every, void
     rr.hA = 2 * (k0 + s) + 1;
     rr.hB = last ? -1 : 2 * (k0 + s + 1);
     rr.do_fft = last ? 0 : 1;
-    if (save_every > 0 && (s + 1) % save_every == 0) slot_ptrs(rr, (s + 1) / save_every - 1);
+    const bool saving = save_every > 0 && (s + 1) % save_every == 0;
+    const int64_t si = saving ? (s + 1) / save_every - 1 : -1;
+    if (saving) {
+      if (ring) {
+        const int rc = ring->before(si);
+        if (rc) return rc;
+      }
+      slot_ptrs(rr, ring ? si % kSaveRing : si);
+    }
     {
       TimedLaunch tl(h, 0);
       LK(h, gpe::launch_row(h->prec, h->M, h->logn[0], rr, nrows, h->stream));
+    }
+    if (saving && ring) {
+      const int rc = ring->after(si);
+      if (rc) return rc;
     }
     ++nl;
   }
@@ -887,13 +954,38 @@ static int run_common(gpe_handle* h, int64_t nsteps, int64_t save_every, void* o
     if (h->prec == gpe::PREC_DW) LK(h, gpe::launch_f64_to_dw(h->xi_buf, h->xi_buf, (int64_t)(xb / 16), h->stream));
   }
   void* save_dev = nullptr;
+  // the two-pass path writes one save per row pass, so a ring can stream them out
+  const bool single_launch = !h->ktab || h->ndim == 1 ||
+                             (h->ndim == 2 && h->n[0] == h->n[1] && !(h->d.flags & GPE_FLAG_NO_RESIDENT) &&
+                              gpe::plane_fits(h->prec, h->M, h->logn[0]));
+  const bool use_ring = nsaves > kSaveRing && !out_is_dev && !single_launch;
+  SaveRing ring{h, nsaves, plane_bytes, (char*)out};
   if (nsaves > 0) {
     if (out_is_dev) {
       save_dev = out;
     } else {
-      int rc = ensure(h, &h->save_buf, &h->save_cap, (size_t)h->M * nsaves * plane_bytes);
+      const int64_t slots = use_ring ? kSaveRing : nsaves;
+      int rc = ensure(h, &h->save_buf, &h->save_cap, (size_t)h->M * slots * plane_bytes);
       if (rc) return rc;
       save_dev = h->save_buf;
+    }
+  }
+  if (use_ring) {
+    const size_t pb = (size_t)h->M * kSaveRing * plane_bytes;
+    if (h->pinned_cap < pb) {
+      if (h->pinned) cudaFreeHost(h->pinned);
+      h->pinned = nullptr;
+      h->pinned_cap = 0;
+      CK(h, cudaHostAlloc(&h->pinned, pb, cudaHostAllocDefault));
+      h->pinned_cap = pb;
+    }
+    if (!h->cstream) CK(h, cudaStreamCreateWithFlags(&h->cstream, cudaStreamNonBlocking));
+    while ((int64_t)h->ring_ready.size() < kSaveRing) {
+      cudaEvent_t a, b;
+      CK(h, cudaEventCreateWithFlags(&a, cudaEventDisableTiming));
+      CK(h, cudaEventCreateWithFlags(&b, cudaEventDisableTiming));
+      h->ring_ready.push_back(a);
+      h->ring_done.push_back(b);
     }
   }
   h->evkind.clear();
@@ -908,7 +1000,8 @@ static int run_common(gpe_handle* h, int64_t nsteps, int64_t save_every, void* o
     int rc = replay_graph(h, nsteps, &launches);
     if (rc) return rc;
   } else {
-    int rc = enqueue_steps(h, nsteps, save_every, save_dev, nsaves, xi_host ? h->xi_buf : nullptr, &launches);
+    int rc = enqueue_steps(h, nsteps, save_every, save_dev, use_ring ? kSaveRing : nsaves,
+                           xi_host ? h->xi_buf : nullptr, &launches, false, use_ring ? &ring : nullptr);
     if (rc) return rc;
   }
   CK(h, cudaEventRecord(h->ev1, h->stream));
@@ -937,7 +1030,12 @@ static int run_common(gpe_handle* h, int64_t nsteps, int64_t save_every, void* o
   }
   h->t = t;
   h->steps += nsteps;
-  if (nsaves > 0 && !out_is_dev) CK(h, cudaMemcpy(out, save_dev, (size_t)h->M * nsaves * plane_bytes, cudaMemcpyDeviceToHost));
+  if (use_ring) {
+    const int rc = ring.drain(nsaves);
+    if (rc) return rc;
+  } else if (nsaves > 0 && !out_is_dev) {
+    CK(h, cudaMemcpy(out, save_dev, (size_t)h->M * nsaves * plane_bytes, cudaMemcpyDeviceToHost));
+  }
   return GPE_OK;
 }
 

@@ -29,8 +29,9 @@ struct LineCfg {
   using C = typename CT<Real>::T;
   static constexpr int N = 1 << LOGN;
   // points per thread: column pass (E) and row pass (ER, which also carries the
-  // pointwise half steps and so keeps fewer points live)
-  static constexpr int EMAX = (sizeof(C) == 16 && M == 2) ? 8 : 16;
+  // pointwise half steps and so keeps fewer points live).  FP32 column passes use 8 so
+  // two CTAs share an SM and one's loads overlap the other's FFTs.
+  static constexpr int EMAX = (sizeof(C) == 16 && M == 2) || sizeof(C) == 8 ? 8 : 16;
   static constexpr int E = cmin(EMAX, N / 2);
   static constexpr int T = N / E;  // threads per line, column pass
   static constexpr int ERMAX = (M == 2) ? 8 : 16;
@@ -47,7 +48,9 @@ struct LineCfg {
 #define GPE_ROW_MIN_BLOCKS 2
 #endif
   static constexpr int ROW_MINB = GPE_ROW_MIN_BLOCKS;
+  static constexpr int COL_MINB_WANT = sizeof(C) == 8 ? 2 : 1;
   static constexpr int COL_THREADS = CC * T;
+  static constexpr int COL_MINB = COL_THREADS <= 512 ? COL_MINB_WANT : 1;
   static constexpr size_t ROW_SMEM = (size_t)L * N * sizeof(C);
   static constexpr size_t COL_SMEM = (size_t)CC * N * sizeof(C);
 };
@@ -396,17 +399,31 @@ __device__ __forceinline__ void half_points(typename CT<Real>::T (&x)[M][E], con
   using C = typename CT<Real>::T;
   C pn[M], px[M];
   load_pump<Real, M>(a, h, pn, px);
+  if constexpr (sizeof(C) <= 8) {
+    // FP32: the half step is short, so unrolled copies fit the instruction cache and
+    // interleave the independent points
+#pragma unroll
+    for (int i = 0; i < E; ++i) {
+      C v[M];
+#pragma unroll
+      for (int m = 0; m < M; ++m) v[m] = x[m][i];
+      half_step<Real, M>(v, a, p0 + (int64_t)T * i, b, h, pn, px);
+#pragma unroll
+      for (int m = 0; m < M; ++m) x[m][i] = v[m];
+    }
+  } else {
 #pragma unroll 1
-  for (int i = 0; i < E; ++i) {
-    C v[M];
+    for (int i = 0; i < E; ++i) {
+      C v[M];
 #pragma unroll
-    for (int m = 0; m < M; ++m) v[m] = x[m][0];
-    half_step<Real, M>(v, a, p0 + (int64_t)T * i, b, h, pn, px);
+      for (int m = 0; m < M; ++m) v[m] = x[m][0];
+      half_step<Real, M>(v, a, p0 + (int64_t)T * i, b, h, pn, px);
 #pragma unroll
-    for (int m = 0; m < M; ++m) {
+      for (int m = 0; m < M; ++m) {
 #pragma unroll
-      for (int q = 0; q + 1 < E; ++q) x[m][q] = x[m][q + 1];
-      x[m][E - 1] = v[m];
+        for (int q = 0; q + 1 < E; ++q) x[m][q] = x[m][q + 1];
+        x[m][E - 1] = v[m];
+      }
     }
   }
 }
@@ -465,7 +482,7 @@ row_kernel(const PassArgs a, const int64_t nlines) {
 
 // ------------------------------------------------------------------ column pass
 template <typename Real, int LOGN, int M>
-__global__ void __launch_bounds__(LineCfg<Real, M, LOGN>::COL_THREADS)
+__global__ void __launch_bounds__(LineCfg<Real, M, LOGN>::COL_THREADS, LineCfg<Real, M, LOGN>::COL_MINB)
 col_kernel(const PassArgs a) {
   using Cfg = LineCfg<Real, M, LOGN>;
   using C = typename CT<Real>::T;

@@ -144,3 +144,34 @@ def momentum_statistics(it: StrangSplittingIterator, commutator: float, comp: in
     delta = np.eye(len(mean))
     G2 = sec - (1 + delta) * c / 2 * (mean[:, None] + mean[None, :] - c / 2)
     return nk, G2, G2 / np.outer(nk, nk)
+
+
+def local_moment_sums(fields: np.ndarray, batch_axis: int = -1):
+    """Per-site sums over the local trajectories: (count, sum |u|^2, sum |u|^4) in FP64."""
+    n = np.abs(np.asarray(fields).astype(np.complex128)) ** 2
+    n = np.moveaxis(n, batch_axis, 0)
+    return n.shape[0], n.sum(axis=0), (n * n).sum(axis=0)
+
+
+def allreduce_moments(fields: np.ndarray, group=None, batch_axis: int = -1):
+    """Ensemble mean and variance of |u|^2 per site when the trajectories are sharded over
+    ranks (one process per GPU, each advancing its own trajectories with no exchange
+    during the run).  The one collective is this all-reduce of (count, sum n, sum n^2)
+    in FP64 over torch.distributed (NCCL or gloo).  Without an initialised process group
+    it reduces the local trajectories only."""
+    cnt, s1, s2 = local_moment_sums(fields, batch_axis)
+    try:
+        import torch
+        import torch.distributed as dist
+        active = dist.is_available() and dist.is_initialized()
+    except ImportError:
+        active = False
+    if active:
+        buf = torch.from_numpy(np.concatenate([[float(cnt)], s1.ravel(), s2.ravel()]))
+        dist.all_reduce(buf, op=dist.ReduceOp.SUM, group=group)
+        v = buf.numpy()
+        cnt = v[0]
+        s1 = v[1:1 + s1.size].reshape(s1.shape)
+        s2 = v[1 + s1.size:].reshape(s1.shape)
+    mean = s1 / cnt
+    return mean, s2 / cnt - mean * mean
