@@ -445,6 +445,42 @@ def run_precision_sweep(args):
     print(json.dumps(report), flush=True)
 
 
+def run_fno(args):
+    """Learned surrogate: train the FNO (4 spectral layers, width 32, 16 modes per axis,
+    BF16 GEMM operands, FP32 accumulation) on polariton windows (128^2, L=256, window =
+    20 steps of dt=0.05) the solver generates for random constant pump amplitudes in
+    [0, 6], then roll out to steady state with a plain-solver check every 10 windows."""
+    import __graft_entry__ as G
+    pkg = G.load_package()
+    F = __import__("gpe_gb300.fno", fromlist=["FNO"])
+    import torch
+    t0 = time.perf_counter()
+    amps, saves = F.generate_pairs(args.fno_traj, args.fno_windows, seed=1)
+    t_gen = time.perf_counter() - t0
+    scale = float(np.abs(saves).max()) or 1.0
+    X, Y = F.pairs_to_tensors(amps, saves, scale)
+    cfg = F.FNOConfig()
+    model = F.FNO(cfg, seed=0)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    losses = F.train(model, X, Y, epochs=args.fno_epochs, batch=16, lr=2e-3)
+    torch.cuda.synchronize()
+    t_train = time.perf_counter() - t0
+    results = []
+    for A in (2.7, 4.9):
+        h1, h2, st = F.hybrid_rollout(model, A, args.fno_rollout, scale)
+        p1, p2, ms_plain = F.plain_rollout(A, args.fno_rollout)
+        ref = np.concatenate([p1.ravel(), p2.ravel()])
+        got = np.concatenate([h1.ravel(), h2.ravel()])
+        err = float(np.linalg.norm(got - ref) / max(np.linalg.norm(ref), 1e-30))
+        results.append({"pump_amplitude": A, "windows": args.fno_rollout, "hybrid_ms": st["ms"], "plain_ms": ms_plain,
+                        "speedup": ms_plain / st["ms"], "final_rel_l2_vs_plain": err, "checks": st["checks"],
+                        "fallbacks": st["fallbacks"], "max_check_rel_l2": st["max_check_err"]})
+    print(json.dumps({"metric": "FNO surrogate hybrid rollout", "pairs": int(X.shape[0]),
+                      "generation_s": t_gen, "train_s": t_train, "epochs": args.fno_epochs,
+                      "loss_first_last": [losses[0], losses[-1]], "rollouts": results}), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -463,6 +499,11 @@ def main():
                     help="print the FP32 / FP64 precision sweep on 2D Kerr instead of the throughput line")
     ap.add_argument("--sweep-n", type=int, default=2048)
     ap.add_argument("--sweep-steps", type=int, default=1000)
+    ap.add_argument("--fno", action="store_true", help="train the FNO surrogate and time the hybrid rollout")
+    ap.add_argument("--fno-traj", type=int, default=100)
+    ap.add_argument("--fno-windows", type=int, default=200)
+    ap.add_argument("--fno-epochs", type=int, default=10)
+    ap.add_argument("--fno-rollout", type=int, default=400)
     args = ap.parse_args()
     if args.warmup < 3:
         ap.error("--warmup must be >= 3")
@@ -470,6 +511,10 @@ def main():
     if args.precision_sweep:
         if rank == 0:
             run_precision_sweep(args)
+        return
+    if args.fno:
+        if rank == 0:
+            run_fno(args)
         return
     if args.impl == "reference":
         run_reference(args, rank, world)

@@ -32,6 +32,7 @@ template <typename Real, int M> int launch_nl_only_t(const PassArgs&, cudaStream
 template <typename Real, int M> int launch_plane_t(int, const PassArgs&, cudaStream_t);
 template <typename Real, int M> bool plane_fits_t(int);
 template <typename Real, int M> int launch_norm_t(const PassArgs&, double*, cudaStream_t);
+template <typename Real> int launch_mat_t(const PassArgs&, cudaStream_t);
 
 // dtype here is the pass precision (PREC_F64, PREC_F32, PREC_DW)
 #define GPE_DISPATCH(FN, ...)                                                                  \
@@ -44,6 +45,11 @@ int launch_col(int dtype, int M, int logn, const PassArgs& a, cudaStream_t s) { 
 int launch_line1d(int dtype, int M, int logn, const PassArgs& a, cudaStream_t s) { GPE_DISPATCH(launch_line1d_t, logn, a, s) }
 int launch_nl_only(int dtype, int M, const PassArgs& a, cudaStream_t s) { GPE_DISPATCH(launch_nl_only_t, a, s) }
 int launch_norm(int dtype, int M, const PassArgs& a, double* out, cudaStream_t s) { GPE_DISPATCH(launch_norm_t, a, out, s) }
+int launch_mat(int dtype, const PassArgs& a, cudaStream_t s) {
+  if (dtype == PREC_F64) return launch_mat_t<double>(a, s);
+  if (dtype == PREC_DW) return launch_mat_t<DWR>(a, s);
+  return launch_mat_t<float>(a, s);
+}
 int launch_plane(int dtype, int M, int logn, const PassArgs& a, cudaStream_t s) { GPE_DISPATCH(launch_plane_t, logn, a, s) }
 bool plane_fits(int dtype, int M, int logn) { GPE_DISPATCH(plane_fits_t, logn) }
 }  // namespace gpe
@@ -84,6 +90,8 @@ struct gpe_handle {
   double g[2][2][2] = {};
   double c[2][2] = {};
   int nl_on[2] = {0, 0};
+  int nl_matrix = 0;
+  double* nlm = nullptr;  // device copy of the matrix nonlinearity coefficients
   double t = 0.0;
   int64_t steps = 0;
   void* save_buf = nullptr;
@@ -339,6 +347,7 @@ int gpe_destroy(gpe_handle* h) {
   for (int a = 0; a < 3; ++a) cudaFree(h->tw[a]);
   cudaFree(h->ktab);
   cudaFree(h->vtab);
+  cudaFree(h->nlm);
   cudaFree(h->save_buf);
   if (h->pinned) cudaFreeHost(h->pinned);
   for (cudaEvent_t e : h->ring_ready) cudaEventDestroy(e);
@@ -479,6 +488,8 @@ int gpe_set_ktable(gpe_handle* h, const double* table, int kind) {
 }
 
 static int store_vtable(gpe_handle* h, const std::vector<cd>& tab, int kind) {
+  if (h->nl_matrix && kind == GPE_TABLE_DIAG)
+    return fail(h, GPE_ERR_UNSUPPORTED, "a matrix nonlinearity with a diagonal potential is not supported");
   if (kind == GPE_TABLE_MATRIX && (h->nl_on[0] || h->nl_on[1]))
     return fail(h, GPE_ERR_UNSUPPORTED, "a matrix potential with a diagonal nonlinearity is undefined (SVector * SMatrix)");
   cudaFree(h->vtab);
@@ -539,10 +550,30 @@ int gpe_set_nonlinearity(gpe_handle* h, const double* g, const double* c) {
   }
   if ((on[0] || on[1]) && h->vkind == GPE_TABLE_MATRIX)
     return fail(h, GPE_ERR_UNSUPPORTED, "a diagonal nonlinearity with a matrix potential is undefined (SVector * SMatrix)");
+  h->nl_matrix = 0;
   memcpy(h->g, gg, sizeof gg);
   memcpy(h->c, cc, sizeof cc);
   h->nl_on[0] = on[0];
   h->nl_on[1] = on[1];
+  return GPE_OK;
+}
+
+int gpe_set_matrix_nonlinearity(gpe_handle* h, const double* g, const double* c) {
+  if (!h) return GPE_ERR_INVALID;
+  if (h->M != 2) return fail(h, GPE_ERR_UNSUPPORTED, "the matrix nonlinearity needs two components");
+  if (!g) return fail(h, GPE_ERR_INVALID, "null coefficients");
+  if (!all_finite(g, 16) || (c && !all_finite(c, 8))) return fail(h, GPE_ERR_NONFINITE, "nonlinearity has NaN or Inf");
+  if (h->vkind == GPE_TABLE_DIAG)
+    return fail(h, GPE_ERR_UNSUPPORTED, "a matrix nonlinearity with a diagonal potential is not supported");
+  double coef[24];
+  for (int q = 0; q < 16; ++q) coef[q] = g[q];
+  for (int q = 0; q < 8; ++q) coef[16 + q] = c ? c[q] : 0.0;
+  CK(h, cudaSetDevice(h->dev));
+  if (!h->nlm) CK(h, cudaMalloc(&h->nlm, sizeof coef));
+  CK(h, cudaMemcpyAsync(h->nlm, coef, sizeof coef, cudaMemcpyHostToDevice, h->stream));
+  CK(h, cudaStreamSynchronize(h->stream));
+  h->nl_matrix = 1;
+  h->nl_on[0] = h->nl_on[1] = 0;
   return GPE_OK;
 }
 
@@ -676,6 +707,7 @@ static PassArgs base_args(gpe_handle* h) {
     a.etaprof[m] = h->etaprof[m];
   }
   a.pprof_cplx = h->pprof_cplx;
+  a.nlm = h->nl_matrix ? h->nlm : nullptr;
   a.noise = h->noise;
   a.seed_lo = (uint32_t)h->seed;
   a.seed_hi = (uint32_t)(h->seed >> 32);
@@ -756,9 +788,150 @@ struct SaveRing {
   }
 };
 
+// Matrix nonlinearity family: the real-space half steps run in a pointwise pass of their
+// own (mat_kernel) between FFT-only line passes, so the line kernels of the diagonal
+// families keep their register allocation.  Per step: kinetic part, then [half A][save]
+// [half B] pointwise; the first half step of the run opens it.
+static int enqueue_matrix_steps(gpe_handle* h, PassArgs a, int64_t k0, int64_t nsteps, int64_t save_every,
+                                void* save_dev, int64_t nsaves_total, int64_t* launches, SaveRing* ring) {
+  const int64_t plane = h->P * h->B;
+  auto slot_ptrs = [&](PassArgs& pa, int64_t slot) {
+    for (int m = 0; m < 2; ++m) pa.save[m] = (char*)save_dev + ((size_t)m * nsaves_total + slot) * plane * h->csz;
+  };
+  int64_t nl = 0;
+  if (!h->ktab) {
+    a.nsteps = nsteps;
+    a.step0 = k0;
+    a.save_every = save_every;
+    a.save_stride = plane;
+    if (save_every > 0) slot_ptrs(a, 0);
+    TimedLaunch tl(h, 2);
+    LK(h, gpe::launch_mat(h->prec, a, h->stream));
+    *launches = 1;
+    return GPE_OK;
+  }
+  // FFT-only argument blocks: every real-space term off
+  PassArgs f = a;
+  f.vkind = gpe::TAB_NONE;
+  f.nl_on[0] = f.nl_on[1] = 0;
+  f.nlm = nullptr;
+  f.pprof[0] = f.pprof[1] = nullptr;
+  f.noise = gpe::NOISE_OFF;
+  f.save[0] = f.save[1] = nullptr;
+  f.hA = f.hB = -1;
+  f.save_every = 0;
+  const int64_t nrows = h->P / h->n[0] * h->B;
+  auto row = [&](int ifft, int fft) -> int {
+    PassArgs r = f;
+    r.tw = h->tw[0];
+    r.do_ifft = ifft;
+    r.do_fft = fft;
+    TimedLaunch tl(h, 0);
+    LK(h, gpe::launch_row(h->prec, 2, h->logn[0], r, nrows, h->stream));
+    ++nl;
+    return GPE_OK;
+  };
+  std::vector<std::pair<PassArgs, int>> cols;
+  if (h->ndim == 2) {
+    PassArgs c = f;
+    c.tw = h->tw[1];
+    c.ld = h->n[0];
+    c.ostride = 0;
+    c.nouter = 1;
+    c.col_fwd = c.col_inv = 1;
+    cols.push_back({c, h->logn[1]});
+  } else if (h->ndim == 3) {
+    PassArgs y = f;
+    y.tw = h->tw[1];
+    y.ld = h->n[0];
+    y.ostride = h->n[0] * h->n[1];
+    y.nouter = h->n[2];
+    y.ktab = nullptr;
+    PassArgs z = f;
+    z.tw = h->tw[2];
+    z.ld = h->n[0] * h->n[1];
+    z.ostride = h->n[0];
+    z.nouter = h->n[1];
+    z.col_fwd = z.col_inv = 1;
+    PassArgs yf = y, yi = y;
+    yf.col_fwd = 1;
+    yi.col_inv = 1;
+    cols.push_back({yf, h->logn[1]});
+    cols.push_back({z, h->logn[2]});
+    cols.push_back({yi, h->logn[1]});
+  }
+  auto kinetic = [&]() -> int {
+    if (h->ndim == 1) {
+      PassArgs l = f;
+      l.tw = h->tw[0];
+      l.nsteps = 1;
+      l.step0 = 0;
+      TimedLaunch tl(h, 2);
+      LK(h, gpe::launch_line1d(h->prec, 2, h->logn[0], l, h->stream));
+      ++nl;
+      return GPE_OK;
+    }
+    int rc = row(0, 1);
+    if (rc) return rc;
+    for (auto& cp : cols) {
+      TimedLaunch tl(h, 1);
+      LK(h, gpe::launch_col(h->prec, 2, cp.second, cp.first, h->stream));
+      ++nl;
+    }
+    return row(1, 0);
+  };
+  {
+    PassArgs m = a;
+    m.nsteps = 0;
+    m.hA = -1;
+    m.hB = 2 * k0;
+    m.save[0] = m.save[1] = nullptr;
+    TimedLaunch tl(h, 2);
+    LK(h, gpe::launch_mat(h->prec, m, h->stream));
+    ++nl;
+  }
+  for (int64_t s = 0; s < nsteps; ++s) {
+    int rc = kinetic();
+    if (rc) return rc;
+    const bool last = (s == nsteps - 1);
+    PassArgs m = a;
+    m.nsteps = 0;
+    m.hA = 2 * (k0 + s) + 1;
+    m.hB = last ? -1 : 2 * (k0 + s + 1);
+    m.save[0] = m.save[1] = nullptr;
+    const bool saving = save_every > 0 && (s + 1) % save_every == 0;
+    const int64_t si = saving ? (s + 1) / save_every - 1 : -1;
+    if (saving) {
+      if (ring) {
+        rc = ring->before(si);
+        if (rc) return rc;
+      }
+      slot_ptrs(m, ring ? si % kSaveRing : si);
+    }
+    {
+      TimedLaunch tl(h, 2);
+      LK(h, gpe::launch_mat(h->prec, m, h->stream));
+    }
+    ++nl;
+    if (saving && ring) {
+      rc = ring->after(si);
+      if (rc) return rc;
+    }
+  }
+  *launches = nl;
+  return GPE_OK;
+}
+
 static int enqueue_steps(gpe_handle* h, int64_t nsteps, int64_t save_every, void* save_dev, int64_t nsaves_total,
                          const void* xi_dev, int64_t* launches, bool relative = false, SaveRing* ring = nullptr) {
   PassArgs a = base_args(h);
+  if (h->nl_matrix) {
+    a.xi = xi_dev;
+    const int64_t k0m = relative ? 0 : h->steps;
+    if (relative) a.kbase = h->kdev;
+    a.xi_h0 = 2 * k0m;
+    return enqueue_matrix_steps(h, a, k0m, nsteps, save_every, save_dev, nsaves_total, launches, ring);
+  }
   // relative: step indices count from the value in h->kdev (graph capture)
   const int64_t k0 = relative ? 0 : h->steps;
   if (relative) a.kbase = h->kdev;
@@ -955,9 +1128,9 @@ static int run_common(gpe_handle* h, int64_t nsteps, int64_t save_every, void* o
   }
   void* save_dev = nullptr;
   // the two-pass path writes one save per row pass, so a ring can stream them out
-  const bool single_launch = !h->ktab || h->ndim == 1 ||
-                             (h->ndim == 2 && h->n[0] == h->n[1] && !(h->d.flags & GPE_FLAG_NO_RESIDENT) &&
-                              gpe::plane_fits(h->prec, h->M, h->logn[0]));
+  const bool single_launch = !h->ktab || (!h->nl_matrix && (h->ndim == 1 || (h->ndim == 2 && h->n[0] == h->n[1] &&
+                                                                            !(h->d.flags & GPE_FLAG_NO_RESIDENT) &&
+                                                                            gpe::plane_fits(h->prec, h->M, h->logn[0]))));
   const bool use_ring = nsaves > kSaveRing && !out_is_dev && !single_launch;
   SaveRing ring{h, nsaves, plane_bytes, (char*)out};
   if (nsaves > 0) {
@@ -1117,6 +1290,7 @@ static int transform_copy(gpe_handle* h) {
 int gpe_energy(gpe_handle* h, double* out) {
   if (!h) return GPE_ERR_INVALID;
   if (!out) return fail(h, GPE_ERR_INVALID, "null output");
+  if (h->nl_matrix) return fail(h, GPE_ERR_UNSUPPORTED, "energy is defined for the diagonal nonlinearity families only");
   CK(h, cudaSetDevice(h->dev));
   if (h->ktab && h->Dsamples.empty())
     return fail(h, GPE_ERR_UNSUPPORTED, "energy needs the dispersion samples (gpe_set_dispersion), not a finished table");

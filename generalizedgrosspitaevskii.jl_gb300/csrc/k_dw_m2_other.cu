@@ -3,4 +3,5 @@
 #include "passes.cuh"
 namespace gpe {
 GPE_INSTANTIATE_OTHER(DWR, 2)
+GPE_INSTANTIATE_MAT(DWR)
 }  // namespace gpe

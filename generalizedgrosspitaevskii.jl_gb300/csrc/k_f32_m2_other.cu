@@ -3,4 +3,5 @@
 #include "passes.cuh"
 namespace gpe {
 GPE_INSTANTIATE_OTHER(float, 2)
+GPE_INSTANTIATE_MAT(float)
 }  // namespace gpe

@@ -3,4 +3,5 @@
 #include "passes.cuh"
 namespace gpe {
 GPE_INSTANTIATE_OTHER(double, 2)
+GPE_INSTANTIATE_MAT(double)
 }  // namespace gpe

@@ -37,6 +37,10 @@ struct PassArgs {
   double c[2][2];
   float gf[2][2][2], gl[2][2][2];
   float cf[2][2], cl[2][2];
+  // matrix nonlinearity (M = 2), null when off: 24 doubles on the device, g[a][b][l] (re, im)
+  // then c[a][b] (re, im), G_ab = sum_l g[a][b][l] |u_l|^2 + c[a][b]; the per-point phase
+  // exp(-i delta G) is a 2x2 matrix exponential
+  const double* nlm;
   // pump F_m = a_m(t) p_m(r): profile (real or complex) and the per-boundary
   // coefficients (dt/4) a_m(t_h), both stored in the pass precision
   const void* pprof[2];
@@ -76,6 +80,8 @@ int launch_row(int dtype, int M, int logn, const PassArgs& a, int64_t nlines, cu
 int launch_col(int dtype, int M, int logn, const PassArgs& a, cudaStream_t s);
 int launch_line1d(int dtype, int M, int logn, const PassArgs& a, cudaStream_t s);
 int launch_nl_only(int dtype, int M, const PassArgs& a, cudaStream_t s);
+// pointwise pass of the 2x2 matrix nonlinearity family (M = 2, a.nlm set)
+int launch_mat(int dtype, const PassArgs& a, cudaStream_t s);
 // whole-trajectory resident 2D kernel (square grids of side 2^logn that fit in shared memory)
 int launch_plane(int dtype, int M, int logn, const PassArgs& a, cudaStream_t s);
 bool plane_fits(int dtype, int M, int logn);

@@ -190,8 +190,95 @@ __device__ __forceinline__ void draw_xi(const PassArgs& a, int64_t p, int64_t b,
   }
 }
 
-// Real-space half step h (delta = dt/2) at spatial point p of trajectory b, on the
-// M values u (src/kernels.jl:37-54):
+// exp(-i delta G) for a 2x2 complex matrix G (row-major g[4] as (re, im)), FP64:
+// e^{tr/2} [cosh(s) I + sinh(s)/s (A - tr/2 I)], A = -i delta G, s^2 = ((a-d)/2)^2 + bc,
+// with the series 1 + s^2/6 + s^4/120 for sinh(s)/s when |s| < 1e-3.
+struct cd2 {
+  double x, y;
+};
+__device__ __forceinline__ cd2 cdmul(cd2 a, cd2 b) { return {a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x}; }
+__device__ __forceinline__ cd2 cdadd(cd2 a, cd2 b) { return {a.x + b.x, a.y + b.y}; }
+__device__ __forceinline__ cd2 cdsub(cd2 a, cd2 b) { return {a.x - b.x, a.y - b.y}; }
+__device__ __forceinline__ cd2 cdsqrt(cd2 z) {
+  const double r = hypot(z.x, z.y);
+  if (r == 0.0) return {0.0, 0.0};
+  const double t = sqrt(0.5 * (r + fabs(z.x)));
+  return z.x >= 0.0 ? cd2{t, z.y / (2.0 * t)} : cd2{fabs(z.y) / (2.0 * t), copysign(t, z.y)};
+}
+__device__ inline void expm2_dev(const cd2 (&G)[4], double delta, cd2 (&E)[4]) {
+  cd2 A[4];
+#pragma unroll
+  for (int q = 0; q < 4; ++q) A[q] = {delta * G[q].y, -delta * G[q].x};  // -i delta G
+  const cd2 ht = {0.5 * (A[0].x + A[3].x), 0.5 * (A[0].y + A[3].y)};
+  const cd2 hd = {0.5 * (A[0].x - A[3].x), 0.5 * (A[0].y - A[3].y)};
+  const cd2 s = cdsqrt(cdadd(cdmul(hd, hd), cdmul(A[1], A[2])));
+  double sh_, ch_, sn, cs;
+  sincos(s.y, &sn, &cs);
+  sh_ = sinh(s.x);
+  ch_ = cosh(s.x);
+  const cd2 chs = {ch_ * cs, sh_ * sn};
+  cd2 shs;
+  if (hypot(s.x, s.y) < 1e-3) {
+    const cd2 s2 = cdmul(s, s);
+    const cd2 s4 = cdmul(s2, s2);
+    shs = {1.0 + s2.x / 6.0 + s4.x / 120.0, s2.y / 6.0 + s4.y / 120.0};
+  } else {
+    const cd2 sinhs = {sh_ * cs, ch_ * sn};
+    const double den = s.x * s.x + s.y * s.y;
+    shs = {(sinhs.x * s.x + sinhs.y * s.y) / den, (sinhs.y * s.x - sinhs.x * s.y) / den};
+  }
+  double es, ec;
+  sincos(ht.y, &es, &ec);
+  const double em = exp(ht.x);
+  const cd2 e = {em * ec, em * es};
+  E[0] = cdmul(e, cdadd(chs, cdmul(shs, cdsub(A[0], ht))));
+  E[3] = cdmul(e, cdadd(chs, cdmul(shs, cdsub(A[3], ht))));
+  E[1] = cdmul(e, cdmul(shs, A[1]));
+  E[2] = cdmul(e, cdmul(shs, A[2]));
+}
+
+template <typename C> __device__ __forceinline__ cd2 to_cd2(const C& v) { return {(double)v.x, (double)v.y}; }
+template <> __device__ __forceinline__ cd2 to_cd2<dwc>(const dwc& v) { return {dw_to_double(re(v)), dw_to_double(im(v))}; }
+template <typename C> __device__ __forceinline__ C from_cd2(cd2 v) { C r; r.x = v.x; r.y = v.y; return r; }
+template <> __device__ __forceinline__ dwc from_cd2<dwc>(cd2 v) { return mk(dw_from(v.x), dw_from(v.y)); }
+
+// E = exp(-i delta G(u)) V at one point for the matrix family, V the potential table entry
+// (scalar or 2x2; none when vkind is neither), evaluated in FP64 for every pass precision.
+template <typename Real>
+__device__ __forceinline__ void matrix_phase(const typename CT<Real>::T (&u)[2], const PassArgs& a, int64_t p,
+                                             typename CT<Real>::T (&Em)[4]) {
+  using C = typename CT<Real>::T;
+  const cd2 v0 = to_cd2(u[0]), v1 = to_cd2(u[1]);
+  const double d0 = v0.x * v0.x + v0.y * v0.y, d1 = v1.x * v1.x + v1.y * v1.y;
+  cd2 G[4], E[4];
+#pragma unroll
+  for (int ab = 0; ab < 4; ++ab) {
+    const double* g = a.nlm + 4 * ab;
+    const double* c = a.nlm + 16 + 2 * ab;
+    G[ab] = {__ldg(c) + __ldg(g) * d0 + __ldg(g + 2) * d1, __ldg(c + 1) + __ldg(g + 1) * d0 + __ldg(g + 3) * d1};
+  }
+  expm2_dev(G, 0.5 * a.dt, E);
+  if (a.vkind == TAB_SCALAR) {
+    const cd2 v = to_cd2(ldgc((const C*)a.vtab + p));
+#pragma unroll
+    for (int q = 0; q < 4; ++q) E[q] = cdmul(E[q], v);
+  } else if (a.vkind == TAB_MATRIX) {
+    cd2 V[4];
+#pragma unroll
+    for (int q = 0; q < 4; ++q) V[q] = to_cd2(ldgc((const C*)a.vtab + (int64_t)q * a.P + p));
+    const cd2 r0 = cdadd(cdmul(E[0], V[0]), cdmul(E[1], V[2]));
+    const cd2 r1 = cdadd(cdmul(E[0], V[1]), cdmul(E[1], V[3]));
+    const cd2 r2 = cdadd(cdmul(E[2], V[0]), cdmul(E[3], V[2]));
+    const cd2 r3 = cdadd(cdmul(E[2], V[1]), cdmul(E[3], V[3]));
+    E[0] = r0;
+    E[1] = r1;
+    E[2] = r2;
+    E[3] = r3;
+  }
+#pragma unroll
+  for (int q = 0; q < 4; ++q) Em[q] = from_cd2<C>(E[q]);
+}
+
 //   u <- cis(-delta G(u)) V (u + delta/2 F_now) + delta/2 F_next - i sqrt(delta) eta xi
 // G is evaluated on u before the pump is added (src/kernels.jl:40,44).
 // pn/px: pump coefficients (dt/4)a(t_h), (dt/4)a(t_{h+1}).
@@ -764,6 +851,90 @@ __global__ void __launch_bounds__(256) nl_only_kernel(const PassArgs a) {
   }
 }
 
+// Half step h of the matrix family (SMatrix G, src/kernels.jl:23-25,36-50):
+//   u <- exp(-i delta G(u)) V (u + delta/2 F_now) + delta/2 F_next - i sqrt(delta) eta xi
+template <typename Real>
+__device__ __forceinline__ void matrix_half_step(typename CT<Real>::T (&u)[2], const PassArgs& a, int64_t p,
+                                                 int64_t b, int64_t h) {
+  using C = typename CT<Real>::T;
+  C pn[2], px[2];
+  load_pump<Real, 2>(a, h, pn, px);
+  C Em[4];
+  matrix_phase<Real>(u, a, p, Em);
+  C prof[2];
+#pragma unroll
+  for (int j = 0; j < 2; ++j) {
+    if (a.pprof[j]) {
+      prof[j] = a.pprof_cplx ? ldgc((const C*)a.pprof[j] + p) : Prof<Real>::cplx(a.pprof[j], p);
+      u[j] = cadd(u[j], cmul(pn[j], prof[j]));
+    }
+  }
+  const C y0 = cadd(cmul(Em[0], u[0]), cmul(Em[1], u[1]));
+  const C y1 = cadd(cmul(Em[2], u[0]), cmul(Em[3], u[1]));
+  u[0] = y0;
+  u[1] = y1;
+#pragma unroll
+  for (int j = 0; j < 2; ++j)
+    if (a.pprof[j]) u[j] = cadd(u[j], cmul(px[j], prof[j]));
+  if (a.noise != NOISE_OFF) {
+    C xi[2];
+    draw_xi<Real, 2>(a, p, b, h, xi);
+#pragma unroll
+    for (int j = 0; j < 2; ++j) {
+      C nf;
+      if constexpr (std::is_same<Real, DWR>::value) {
+        nf = mk({a.nfacf[j][0], a.nfacl[j][0]}, {a.nfacf[j][1], a.nfacl[j][1]});
+        if (a.etaprof[j]) {
+          const float2 e = __ldg((const float2*)a.etaprof[j] + p);
+          nf = cscale(nf, dw{e.x, e.y});
+        }
+      } else {
+        nf.x = Coef<Real>::nf(a, j, 0);
+        nf.y = Coef<Real>::nf(a, j, 1);
+        if (a.etaprof[j]) nf = cscale(nf, __ldg((const Real*)a.etaprof[j] + p));
+      }
+      u[j] = cadd(u[j], cmul(nf, xi[j]));
+    }
+  }
+}
+
+// Pointwise pass of the matrix family.  nsteps > 0: whole steps of a problem without a
+// k-space table (saves every save_every steps, like nl_only_kernel); otherwise the real-
+// space part of a row-pass program between two FFT-only passes: [half hA] [save] [half hB].
+template <typename Real>
+__global__ void __launch_bounds__(256) mat_kernel(const PassArgs a) {
+  using C = typename CT<Real>::T;
+  const int64_t total = a.P * a.B;
+  const int64_t kb = a.kbase ? *a.kbase : 0;
+  for (int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; q < total; q += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t b = q / a.P, p = q - b * a.P;
+    C v[2] = {((const C*)a.u[0])[q], ((const C*)a.u[1])[q]};
+    if (a.nsteps > 0) {
+      for (int64_t s = 0; s < a.nsteps; ++s) {
+#pragma unroll 1
+        for (int half = 0; half < 2; ++half) matrix_half_step<Real>(v, a, p, b, 2 * (a.step0 + kb + s) + half);
+        if (a.save_every > 0 && ((s + 1) % a.save_every) == 0) {
+          const int64_t slot = (s + 1) / a.save_every - 1;
+#pragma unroll
+          for (int m = 0; m < 2; ++m) store_save<Real>(a.save[m], slot * a.save_stride + q, v[m]);
+        }
+      }
+    } else {
+#pragma unroll 1
+      for (int ph = 0; ph < 2; ++ph) {
+        const int64_t hr = ph ? a.hB : a.hA;
+        if (hr >= 0) matrix_half_step<Real>(v, a, p, b, hr + 2 * kb);
+        if (ph == 0 && a.save[0]) {
+#pragma unroll
+          for (int m = 0; m < 2; ++m) store_save<Real>(a.save[m], q, v[m]);
+        }
+      }
+    }
+#pragma unroll
+    for (int m = 0; m < 2; ++m) ((C*)a.u[m])[q] = v[m];
+  }
+}
+
 // ------------------------------------------------------------------ FP64 norm
 template <typename C> __device__ __forceinline__ double abs2d(const C& v) {
   return (double)v.x * (double)v.x + (double)v.y * (double)v.y;
@@ -896,6 +1067,14 @@ int launch_nl_only_t(const PassArgs& a, cudaStream_t s) {
   nl_only_kernel<Real, M><<<(unsigned)blocks, 256, 0, s>>>(a);
   return (int)cudaGetLastError();
 }
+template <typename Real>
+int launch_mat_t(const PassArgs& a, cudaStream_t s) {
+  const int64_t total = a.P * a.B;
+  int64_t blocks = (total + 255) / 256;
+  if (blocks > 152 * 16) blocks = 152 * 16;
+  mat_kernel<Real><<<(unsigned)blocks, 256, 0, s>>>(a);
+  return (int)cudaGetLastError();
+}
 template <typename Real, int M>
 int launch_norm_t(const PassArgs& a, double* out, cudaStream_t s) {
   const int64_t total = a.P * a.B;
@@ -912,6 +1091,7 @@ int launch_norm_t(const PassArgs& a, double* out, cudaStream_t s) {
 #define GPE_INSTANTIATE_PLANE(REAL, MM)                                      \
   template int launch_plane_t<REAL, MM>(int, const PassArgs&, cudaStream_t);  \
   template bool plane_fits_t<REAL, MM>(int);
+#define GPE_INSTANTIATE_MAT(REAL) template int launch_mat_t<REAL>(const PassArgs&, cudaStream_t);
 #define GPE_INSTANTIATE_OTHER(REAL, MM)                                           \
   template int launch_line1d_t<REAL, MM>(int, const PassArgs&, cudaStream_t);    \
   template int launch_nl_only_t<REAL, MM>(const PassArgs&, cudaStream_t);        \

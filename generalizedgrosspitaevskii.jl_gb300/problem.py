@@ -154,6 +154,11 @@ def sample_table(f: Callable, axes, param, M: int):
     return out, kind
 
 
+class MatrixNonlinearity(NotImplementedError):
+    """Raised by the diagonal fit when the closure returns a non-diagonal SMatrix; the
+    caller then fits the matrix family (``classify_matrix_nonlinearity``)."""
+
+
 def _as_components(G, M, shape):
     G = as_array(G, shape)
     if G.shape == shape or G.ndim == 0:
@@ -164,7 +169,7 @@ def _as_components(G, M, shape):
         for j in range(M):
             off[j, j] = 0
         if np.any(off != 0):
-            raise NotImplementedError("non-diagonal (SMatrix) nonlinearities are not supported by the GPU backend")
+            raise MatrixNonlinearity("the nonlinearity returns a non-diagonal matrix")
         G = np.stack([G[j, j] for j in range(M)])
     return np.broadcast_to(G, (M,) + shape)
 
@@ -189,6 +194,42 @@ def classify_nonlinearity(fn: Callable, M: int, param, rng=None):
         if err > 1e-9 * max(1.0, np.abs(G).max()):
             raise NotImplementedError(
                 "nonlinearity is not of the form G_j = sum_l g_jl |u_l|^2 + c_j supported by the GPU backend")
+    return g, c
+
+
+def classify_matrix_nonlinearity(fn: Callable, M: int, param, rng=None):
+    """Fit the matrix family G_ab(u) = sum_l g[a,b,l] |u_l|^2 + c[a,b] to a closure that
+    returns a 2x2 SMatrix per point (src/kernels.jl:23-25,44 applies cis(-delta G) as a
+    matrix exponential) and verify the fit on random fields.  Returns (g (2,2,2) complex,
+    c (2,2) complex), C order, as gpe_set_matrix_nonlinearity takes them."""
+    if M != 2:
+        raise NotImplementedError("the matrix nonlinearity family needs two components")
+    K = 8
+    shape = (K,)
+
+    def mat(u):
+        G = as_array(fn(u, param), shape)
+        if G.ndim == 0 or G.shape == shape:
+            G = np.broadcast_to(G, shape)[None, None] * np.eye(2)[:, :, None]
+        if G.shape[:2] != (2, 2):
+            raise NotImplementedError(f"nonlinearity of shape {G.shape} is neither per component nor a 2x2 matrix")
+        return np.broadcast_to(G, (2, 2) + shape).astype(np.complex128)
+
+    zeros = tuple(np.zeros(K, np.complex128) for _ in range(2))
+    c = mat(zeros)[:, :, 0].copy()
+    g = np.zeros((2, 2, 2), np.complex128)
+    for l in range(2):
+        u = tuple((np.ones(K, np.complex128) if m == l else np.zeros(K, np.complex128)) for m in range(2))
+        g[:, :, l] = mat(u)[:, :, 0] - c
+    rng = rng or np.random.default_rng(12345)
+    for scale in (0.3, 1.7, 11.0):
+        u = tuple(scale * (rng.standard_normal(K) + 1j * rng.standard_normal(K)) for _ in range(2))
+        G = mat(u)
+        dens = np.stack([np.abs(x) ** 2 for x in u])
+        fit = c[:, :, None] + np.einsum("abl,lk->abk", g, dens)
+        if np.abs(G - fit).max() > 1e-9 * max(1.0, np.abs(G).max()):
+            raise NotImplementedError(
+                "matrix nonlinearity is not of the form G_ab = sum_l g_abl |u_l|^2 + c_ab supported by the GPU backend")
     return g, c
 
 

@@ -15,7 +15,8 @@ from typing import Callable, Optional
 import numpy as np
 
 from . import _lib as L
-from .problem import (GrossPitaevskiiProblem, SeparablePump, classify_noise, classify_nonlinearity,
+from .problem import (GrossPitaevskiiProblem, MatrixNonlinearity, SeparablePump, classify_matrix_nonlinearity,
+                      classify_noise, classify_nonlinearity,
                       classify_pump, direct_grid, reciprocal_grid, sample_table)
 
 
@@ -117,8 +118,15 @@ class StrangSplittingIterator:
             D, kind = sample_table(prob.dispersion, rg, prob.param, M)
             L.check(lib, h, lib.gpe_set_dispersion(h, L.ptr(np.ascontiguousarray(D)), kind))
         if prob.nonlinearity is not None:
-            g, c = classify_nonlinearity(prob.nonlinearity, M, prob.param)
-            L.check(lib, h, lib.gpe_set_nonlinearity(h, L.ptr(np.ascontiguousarray(g)), L.ptr(np.ascontiguousarray(c))))
+            try:
+                g, c = classify_nonlinearity(prob.nonlinearity, M, prob.param)
+            except MatrixNonlinearity:
+                g, c = classify_matrix_nonlinearity(prob.nonlinearity, M, prob.param)
+                L.check(lib, h, lib.gpe_set_matrix_nonlinearity(h, L.ptr(np.ascontiguousarray(g)),
+                                                                L.ptr(np.ascontiguousarray(c))))
+            else:
+                L.check(lib, h, lib.gpe_set_nonlinearity(h, L.ptr(np.ascontiguousarray(g)),
+                                                         L.ptr(np.ascontiguousarray(c))))
         if prob.potential is not None:
             V, kind = sample_table(prob.potential, dg, prob.param, M)
             L.check(lib, h, lib.gpe_set_potential(h, L.ptr(np.ascontiguousarray(V)), kind))

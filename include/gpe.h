@@ -135,6 +135,11 @@ int gpe_set_vtable(gpe_handle* h, const double* table, int kind);
  * reference's tests and examples (e.g. test/kerr_propagation.jl:24,
  * examples/exciton_polariton.jl:50). */
 int gpe_set_nonlinearity(gpe_handle* h, const double* g, const double* c);
+/* Matrix nonlinearity family for two components (the SMatrix form of
+ * src/kernels.jl:23-25,44): G_ab(u) = sum_l g[(a*2+b)*2+l] |u_l|^2 + c[a*2+b] (complex,
+ * interleaved), applied as the per-point 2x2 exponential exp(-i dt/2 G) (times a scalar or
+ * matrix potential table).  Replaces any diagonal nonlinearity; c may be NULL. */
+int gpe_set_matrix_nonlinearity(gpe_handle* h, const double* g, const double* c);
 /* Separable pump F_comp(r, t) = a(t) * p(r).  profile: P real FP64 values (or P
  * interleaved complex when profile_complex != 0); amp: n_amp complex FP64 values of
  * a(t) at the reference's pump sampling times: amp[0] = a(t0), amp[2k+1] =

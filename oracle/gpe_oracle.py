@@ -210,6 +210,7 @@ class OracleProblem:
     nonlin_g: Optional[np.ndarray] = None  # (M, M) complex
     nonlin_c: Optional[np.ndarray] = None  # (M,) complex
     nonlin_fn: Optional[Callable] = None   # fields (M, ...) -> diag G (M, ...)
+    nonlin_matrix: Optional[Callable] = None  # fields (2, ...) -> matrix G (2, 2, ...)
     pump_profile: Optional[np.ndarray] = None   # (M, *spatial) complex
     pump_amp: Optional[Callable] = None         # t -> (M,) complex
     pump_fn: Optional[Callable] = None          # t -> (M, *spatial) complex
@@ -281,7 +282,11 @@ class OracleIterator:
         return None
 
     def _diag_G(self, u):
+        """G(u): per component (M, ...) for the diagonal families, (M, M, ...) for the
+        matrix family (an SMatrix-valued nonlinearity, src/kernels.jl:23-25)."""
         p = self.prob
+        if p.nonlin_matrix is not None:
+            return np.asarray(p.nonlin_matrix(u), dtype=np.complex128)
         if p.nonlin_fn is not None:
             return np.asarray(p.nonlin_fn(u), dtype=np.complex128)
         if p.nonlin_g is None and p.nonlin_c is None:
@@ -309,6 +314,20 @@ class OracleIterator:
         """_mul(cis(-dt G), table) applied to the M-vector v (src/kernels.jl:44,48):
         scalar and diagonal tables act elementwise, a matrix table as a mat-vec."""
         E = None
+        if G is not None and G.ndim == v.ndim + 1:
+            # matrix family: E = cis(-dt G) as a 2x2 exponential, times the table (scalar or
+            # matrix, src/kernels.jl:44), then a mat-vec
+            E = expm_2x2_or_1x1(-1j * dt_half * G)
+            if table is not None:
+                if kind == "diag":
+                    raise NotImplementedError("matrix G with a diagonal table is not supported")
+                T = self._bcast(table, 2 if kind == "matrix" else 0, v.ndim)
+                if kind == "matrix":
+                    E = np.stack([np.stack([E[i, 0] * T[0, j] + E[i, 1] * T[1, j] for j in range(2)])
+                                  for i in range(2)])
+                else:
+                    E = E * T
+            return np.stack([E[i, 0] * v[0] + E[i, 1] * v[1] for i in range(2)])
         if G is not None:
             E = np.exp(-1j * dt_half * G)
         if table is not None:

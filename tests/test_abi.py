@@ -25,9 +25,11 @@ def test_every_declared_symbol_is_exported(lib, gpe):
     names = declared_functions()
     assert len(names) >= 20
     L = __import__("gpe_gb300._lib", fromlist=["SIGNATURES"])
+    F = __import__("gpe_gb300.fno", fromlist=["FNO_SIGNATURES"])
+    sigs = dict(L.SIGNATURES, **F.FNO_SIGNATURES)
     for n in names:
         assert hasattr(lib, n), f"{n} declared in include/ but not exported"
-        assert n in L.SIGNATURES, f"{n} has no ctypes signature"
+        assert n in sigs, f"{n} has no ctypes signature"
 
 
 def test_struct_layout_matches_c(gpe, tmp_path):
@@ -50,6 +52,25 @@ int main(void) {{
     want = [ctypes.sizeof(D), D.n.offset, D.lengths.offset, D.batch.offset, D.ncomp.offset, D.dt.offset,
             D.t0.offset, D.device.offset, ctypes.sizeof(S), S.noise_mode.offset]
     assert got == want
+
+
+def test_fno_struct_layouts_match_c(gpe, tmp_path):
+    F = __import__("gpe_gb300.fno", fromlist=["GemmDesc"])
+    src = tmp_path / "fno_layout.c"
+    src.write_text(f'''#include <stdio.h>
+#include <stddef.h>
+#include "{ROOT / 'include' / 'gpe_fno.h'}"
+int main(void) {{
+  printf("%zu %zu %zu %zu %zu %zu\\n", sizeof(gpe_gemm_desc), offsetof(gpe_gemm_desc, c_z),
+         offsetof(gpe_gemm_desc, alpha), sizeof(gpe_permute_desc), offsetof(gpe_permute_desc, d),
+         offsetof(gpe_gemm_desc, batch));
+  return 0;
+}}''')
+    exe = tmp_path / "fno_layout"
+    subprocess.run(["gcc", "-O0", "-I", str(ROOT / "include"), "-o", str(exe), str(src)], check=True)
+    got = [int(v) for v in subprocess.run([str(exe)], capture_output=True, text=True, check=True).stdout.split()]
+    G, Pm = F.GemmDesc, F.PermDesc
+    assert got == [ctypes.sizeof(G), G.c_z.offset, G.alpha.offset, ctypes.sizeof(Pm), Pm.d.offset, G.batch.offset]
 
 
 def _desc(L, **kw):

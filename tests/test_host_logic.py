@@ -40,8 +40,29 @@ def test_nonlinearity_classification(gpe):
     assert np.allclose(g, [[0.01 - 0.2j]]) and np.allclose(c, [-(0.01 - 0.2j) * 2])
     with pytest.raises(NotImplementedError):
         classify_nonlinearity(lambda u, p: np.abs(u[0]) ** 4, 1, None)
-    with pytest.raises(NotImplementedError):
+    # a non-diagonal SMatrix is handed to the matrix family
+    from gpe_gb300.problem import MatrixNonlinearity
+    with pytest.raises(MatrixNonlinearity):
         classify_nonlinearity(lambda u, p: [[np.abs(u[0]) ** 2, 1.0 + 0 * u[0]], [1.0 + 0 * u[0], np.abs(u[1]) ** 2]], 2, None)
+
+
+def test_matrix_nonlinearity_classification(gpe):
+    """G_ab = sum_l g_abl |u_l|^2 + c_ab recovered from an SMatrix closure; a scalar closure
+    is the identity matrix times it; a non-polynomial closure or one component is refused."""
+    from gpe_gb300.problem import classify_matrix_nonlinearity
+    fn = lambda u, p: [[0.8 * np.abs(u[0]) ** 2 - 0.03j, 0.9 + 0.05 * np.abs(u[1]) ** 2],
+                       [0.9 + 0 * u[0], 0.5 * np.abs(u[1]) ** 2 + 0.2 * np.abs(u[0]) ** 2 + 0.1]]
+    g, c = classify_matrix_nonlinearity(fn, 2, None)
+    assert g.shape == (2, 2, 2) and c.shape == (2, 2)
+    assert np.allclose(g[0, 0], [0.8, 0]) and np.allclose(g[0, 1], [0, 0.05])
+    assert np.allclose(g[1, 0], [0, 0]) and np.allclose(g[1, 1], [0.2, 0.5])
+    assert np.allclose(c, [[-0.03j, 0.9], [0.9, 0.1]])
+    g, c = classify_matrix_nonlinearity(lambda u, p: 2.0 * np.abs(u[1]) ** 2, 2, None)
+    assert np.allclose(g[0, 0], [0, 2]) and np.allclose(g[1, 1], [0, 2]) and np.allclose(g[0, 1], 0)
+    with pytest.raises(NotImplementedError):
+        classify_matrix_nonlinearity(lambda u, p: [[np.abs(u[0]) ** 4, 0 * u[0]], [0 * u[0], 0 * u[0]]], 2, None)
+    with pytest.raises(NotImplementedError):
+        classify_matrix_nonlinearity(lambda u, p: np.abs(u[0]) ** 2, 1, None)
 
 
 def test_pump_classification(gpe):

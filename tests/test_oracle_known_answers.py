@@ -170,3 +170,71 @@ def test_pump_times_follow_the_reference_order():
     """init samples F(t0); step k (end time t_k) samples t_k + dt/2 and t_k + dt."""
     pt = O.pump_times(1.0, 0.5, 3)
     assert np.allclose(pt, [1.0, 1.75, 2.0, 2.25, 2.5, 2.75, 3.0])
+
+
+def test_matrix_nonlinearity_linear_coupling_closed_form():
+    """Matrix family with a constant coupling G = [[d, k], [k, -d]] and a scalar dispersion:
+    G and D commute, so the split step is exact, u(t) = exp(-i t G) exp(-i t D) u0, with
+    exp(-i t G) = cos(w t) I - i sin(w t) G / w, w = sqrt(d^2 + k^2) (a two-level Rabi
+    rotation)."""
+    N, L, dt, nsaves = 32, 8.0, 0.07, 15
+    dg, rg = O.grids((L, L), (N, N))
+    X, Y = O.mesh(dg)
+    a0 = np.exp(-((X - 4) ** 2 + (Y - 4) ** 2)) * (1 + 0.3j * X)
+    b0 = 0.5 * np.exp(-((X - 3) ** 2 + (Y - 5) ** 2) / 2)
+    d, k = 0.4, 1.3
+    G = np.array([[d, k], [k, -d]], np.complex128)
+    prob = O.OracleProblem(u0=(a0, b0), lengths=(L, L), dispersion=lambda q, p: (q[0] ** 2 + q[1] ** 2) / 2,
+                           nonlin_matrix=lambda u: np.broadcast_to(G.reshape(2, 2, *([1] * (u.ndim - 1))),
+                                                                   (2, 2) + u.shape[1:]))
+    ts, res = O.solve(prob, (0.0, nsaves * dt), dt, nsaves)
+    KX, KY = O.mesh(rg)
+    K2 = KX ** 2 + KY ** 2
+    w = math.hypot(d, k)
+    for i, t in enumerate(ts):
+        fa = np.fft.ifft2(np.exp(-1j * K2 / 2 * t) * np.fft.fft2(a0))
+        fb = np.fft.ifft2(np.exp(-1j * K2 / 2 * t) * np.fft.fft2(b0))
+        c, s = math.cos(w * t), math.sin(w * t)
+        ea = c * fa - 1j * s / w * (d * fa + k * fb)
+        eb = c * fb - 1j * s / w * (k * fa - d * fb)
+        assert O.rel_l2(np.stack([res[0, i], res[1, i]]), np.stack([ea, eb])) <= 1e-12
+
+
+def test_matrix_exponential_matches_scipy():
+    """The closed-form 2x2 exponential of the oracle (used for cis(-delta G) of an SMatrix
+    nonlinearity) against scipy.linalg.expm on random complex matrices, including nearly
+    degenerate ones (the series branch) and exactly diagonal ones."""
+    from scipy.linalg import expm
+    rng = np.random.default_rng(4)
+    A = rng.standard_normal((2, 2, 40)) + 1j * rng.standard_normal((2, 2, 40))
+    A[:, :, :10] *= 1e-4
+    A[0, 1, 10:15] = A[1, 0, 10:15] = 0
+    A[1, 1, 15:20] = A[0, 0, 15:20] + 1e-5
+    A[0, 1, 15:20] *= 1e-4
+    E = O.expm_2x2_or_1x1(A)
+    for q in range(A.shape[-1]):
+        want = expm(A[:, :, q])
+        assert np.abs(E[:, :, q] - want).max() <= 1e-13 * max(1.0, np.abs(want).max())
+
+
+def test_diagonal_matrix_nonlinearity_equals_diagonal_family():
+    """A 2x2 SMatrix nonlinearity that happens to be diagonal reproduces the per-component
+    (SVector) family: cis of a diagonal matrix is the diagonal of the cis values."""
+    N, L, dt, nsaves = 32, 10.0, 0.05, 6
+    dg, _ = O.grids((L,), (N,))
+    (X,) = O.mesh(dg)
+    u0 = (np.exp(-(X - 5) ** 2) + 0j, 0.7 * np.exp(-(X - 4) ** 2 / 3) + 0.1j)
+    g = np.array([[1.0, 0.4 - 0.05j], [0.3, -0.8]])
+    c = np.array([0.2, -0.1 + 0.02j])
+
+    def gmat(u):
+        dens = np.abs(u) ** 2
+        G = np.zeros((2, 2) + u.shape[1:], np.complex128)
+        for j in range(2):
+            G[j, j] = g[j, 0] * dens[0] + g[j, 1] * dens[1] + c[j]
+        return G
+
+    kw = dict(u0=u0, lengths=(L,), dispersion=lambda q, p: np.stack([q[0] ** 2 / 2, q[0] ** 2 / 3]))
+    _, ra = O.solve(O.OracleProblem(nonlin_g=g, nonlin_c=c, **kw), (0.0, nsaves * dt), dt, nsaves)
+    _, rb = O.solve(O.OracleProblem(nonlin_matrix=gmat, **kw), (0.0, nsaves * dt), dt, nsaves)
+    assert O.rel_l2(ra, rb) <= 1e-13
