@@ -340,11 +340,44 @@ def run_gpu(args, rank, world, local_rank):
                                  for i, k in enumerate(["row", "col"])}},
         "clocks": clk.summary(),
     }
+    if args.anchor_steps > 0:
+        line["kerr1024"] = run_kerr1024(pkg, lib, L, local_rank, args.anchor_steps)
     if not args.no_cpu:
         line["cpu_baseline"] = cpu_baseline()
     if args.twa_steps > 0:
         line["twa"] = run_twa(pkg, args.twa_steps, tune=not args.no_tune)
     print(json.dumps(line), flush=True)
+
+
+def run_kerr1024(pkg, lib, L, device, steps):
+    """Scalar Kerr at 1024^2 (L=32, u0 = exp(-|r - r0|^2 / 4), r0 = (16, 16), D = |k|^2/2,
+    G = |u|^2, dt = 0.005), FP64 fields: a single field (16 MiB, L2-resident) and 16
+    independent copies (256 MiB, streamed from HBM), double-word and native FP64.
+    Algorithmic bytes per point-step: two passes each reading and writing the field
+    (4 x 16 B) plus the scalar k-space table (16 B) = 80 B."""
+    N, Lb, dt = 1024, 32.0, 0.005
+    x = np.arange(N) * (Lb / N)
+    X, Y = np.meshgrid(x, x, indexing="ij")
+    base = np.exp(-((X - 16) ** 2 + (Y - 16) ** 2) / 4.0).astype(np.complex128)
+    peak, _ = measured_peaks()
+    out = []
+    for B, fp64 in ((1, "dw"), (16, "dw"), (16, "native")):
+        u0 = np.asfortranarray(np.repeat(base[:, :, None], B, axis=2)) if B > 1 else np.asfortranarray(base)
+        prob = pkg.GrossPitaevskiiProblem((u0,), (Lb, Lb), dispersion=lambda k, p: (k[0] ** 2 + k[1] ** 2) / 2,
+                                          nonlinearity=lambda u, p: np.abs(u[0]) ** 2)
+        it = pkg.StrangSplittingIterator(prob, (0.0, 1e3 * dt), dt=dt, nsaves=1, device=device, fp64=fp64)
+        it.step(5)
+        L.check(lib, it.h, lib.gpe_run(it.h, steps, 0, None, None))
+        ms = lib.gpe_last_run_ms(it.h)
+        it.close()
+        v = N * N * B * steps / (ms * 1e-3)
+        gbs = 80.0 * v / 1e9
+        out.append({"batch": B, "arith": "f64-dw" if fp64 == "dw" else "f64", "steps": steps,
+                    "ms_per_step": ms / steps, "value": v, "unit": "grid-point-steps/s",
+                    "algorithmic_gbs": gbs, "frac_of_hbm": gbs / peak,
+                    "l2": "field L2-resident (16 MiB)" if B == 1 else "256 MiB of fields, streamed from HBM"})
+    return {"workload": "scalar Kerr 1024x1024 FP64, L=32, G=|u|^2, dt=0.005 (80 algorithmic B per point-step)",
+            "runs": out}
 
 
 TWA_GROUPS = [(64, 342), (128, 341), (256, 341)]  # 1024 trajectories over three grids
@@ -463,9 +496,16 @@ def run_fno(args):
     model = F.FNO(cfg, seed=0)
     torch.cuda.synchronize()
     t0 = time.perf_counter()
-    losses = F.train(model, X, Y, epochs=args.fno_epochs, batch=16, lr=2e-3)
+    losses = F.train(model, X, Y, epochs=args.fno_epochs, batch=16, lr=2e-3,
+                     log=lambda m: print(m, file=sys.stderr, flush=True))
     torch.cuda.synchronize()
     t_train = time.perf_counter() - t0
+    # held-out windows: rel L2 of one surrogate window against the solver's
+    va, vs = F.generate_pairs(4, 50, seed=99)
+    VX, VY = F.pairs_to_tensors(va, vs, scale)
+    with torch.no_grad():
+        pred = torch.cat([model.forward(VX[i:i + 16].contiguous()) for i in range(0, VX.shape[0], 16)])
+    win_err = float(torch.linalg.norm(pred - VY) / torch.linalg.norm(VY))
     results = []
     for A in (2.7, 4.9):
         h1, h2, st = F.hybrid_rollout(model, A, args.fno_rollout, scale)
@@ -475,10 +515,15 @@ def run_fno(args):
         err = float(np.linalg.norm(got - ref) / max(np.linalg.norm(ref), 1e-30))
         results.append({"pump_amplitude": A, "windows": args.fno_rollout, "hybrid_ms": st["ms"], "plain_ms": ms_plain,
                         "speedup": ms_plain / st["ms"], "final_rel_l2_vs_plain": err, "checks": st["checks"],
-                        "fallbacks": st["fallbacks"], "max_check_rel_l2": st["max_check_err"]})
+                        "fallbacks": st["fallbacks"], "restarts": st["restarts"],
+                        "max_check_rel_l2": st["max_check_err"]})
+    per_window = {}
+    for B in (1, 64):
+        per_window[str(B)] = {"surrogate_ms": F.surrogate_window_ms(model, B), "plain_ms": F.plain_window_ms(B)}
     print(json.dumps({"metric": "FNO surrogate hybrid rollout", "pairs": int(X.shape[0]),
                       "generation_s": t_gen, "train_s": t_train, "epochs": args.fno_epochs,
-                      "loss_first_last": [losses[0], losses[-1]], "rollouts": results}), flush=True)
+                      "loss_per_epoch": losses, "heldout_window_rel_l2": win_err, "rollouts": results,
+                      "window_cost_by_batch": per_window}), flush=True)
 
 
 def main():
@@ -495,6 +540,8 @@ def main():
     ap.add_argument("--twa-steps", type=int, default=2000,
                     help="steps of the batched truncated-Wigner ensemble measurement (0 skips it)")
     ap.add_argument("--no-tune", action="store_true", help="skip the ensemble autotuner")
+    ap.add_argument("--anchor-steps", type=int, default=200,
+                    help="steps of the scalar Kerr 1024^2 FP64 measurement (0 skips it)")
     ap.add_argument("--precision-sweep", action="store_true",
                     help="print the FP32 / FP64 precision sweep on 2D Kerr instead of the throughput line")
     ap.add_argument("--sweep-n", type=int, default=2048)

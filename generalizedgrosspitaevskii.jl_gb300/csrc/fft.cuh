@@ -132,12 +132,21 @@ __device__ __forceinline__ C twc(C d) {
   }
 }
 
+// Butterfly sums: plain for FP32 / FP64; for double-word values the closing
+// renormalisation is deferred to the end of the line transform (fft_line).
+template <typename C> __device__ __forceinline__ C badd(C a, C b) { return cadd(a, b); }
+template <typename C> __device__ __forceinline__ C bsub(C a, C b) { return csub(a, b); }
+template <typename C> __device__ __forceinline__ C bfinish(C a) { return a; }
+template <> __device__ __forceinline__ dwc badd<dwc>(dwc a, dwc b) { return cadd_lazy(a, b); }
+template <> __device__ __forceinline__ dwc bsub<dwc>(dwc a, dwc b) { return csub_lazy(a, b); }
+template <> __device__ __forceinline__ dwc bfinish<dwc>(dwc a) { return crenorm(a); }
+
 // Radix-2 decimation-in-frequency layer of half-size H over an array of R points.
 template <int R, int DIR, int H, int B, int I, typename C>
 __device__ __forceinline__ void dif_bfly(C (&v)[R]) {
   C a = v[B + I], c = v[B + I + H];
-  v[B + I] = cadd(a, c);
-  v[B + I + H] = twc<DIR, 2 * H, I>(csub(a, c));
+  v[B + I] = badd(a, c);
+  v[B + I + H] = twc<DIR, 2 * H, I>(bsub(a, c));
 }
 template <int R, int DIR, int H, int B, int I, typename C>
 __device__ __forceinline__ void dif_row(C (&v)[R]) {
@@ -256,6 +265,8 @@ __device__ __forceinline__ void fft_stages(C (&x)[E], int t, const Lay& lay, con
 template <typename C, int N, int E, int DIR, class Lay>
 __device__ __forceinline__ void fft_line(C (&x)[E], int t, const Lay& lay, const C* __restrict__ tw) {
   fft_stages<C, N, E, DIR, 1>(x, t, lay, tw);
+#pragma unroll
+  for (int i = 0; i < E; ++i) x[i] = bfinish(x[i]);
 }
 
 }  // namespace gpe

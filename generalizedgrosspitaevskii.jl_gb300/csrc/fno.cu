@@ -169,8 +169,12 @@ __global__ void bias_grad_kernel(const float* dy, float* dbias, int64_t B, int64
   }
 }
 
-__global__ void axpy_kernel(float* y, const float* x, float alpha, int64_t n) {
-  for (int64_t i = gidx(); i < n; i += gstride()) y[i] += alpha * x[i];
+__global__ void axpy_kernel(float* y, const float* x, float alpha, int64_t n, int64_t batch, int64_t ys, int64_t xs) {
+  const int64_t total = n * batch;
+  for (int64_t q = gidx(); q < total; q += gstride()) {
+    const int64_t z = q / n, i = q - z * n;
+    y[z * ys + i] += alpha * x[z * xs + i];
+  }
 }
 
 // grad = 2 (pred - target) / n; partial sums of squares into loss_acc (FP64)
@@ -248,8 +252,11 @@ int gpe_fno_bias_grad(const float* dy, float* dbias, int64_t B, int64_t C, int64
   return cudaGetLastError() == cudaSuccess ? GPE_OK : GPE_ERR_CUDA;
 }
 
-int gpe_fno_axpy(float* y, const float* x, float alpha, int64_t n, void* stream) {
-  axpy_kernel<<<grid_for(n), 256, 0, (cudaStream_t)stream>>>(y, x, alpha, n);
+int gpe_fno_axpy(float* y, const float* x, float alpha, int64_t n, int64_t batch, int64_t y_stride, int64_t x_stride,
+                 void* stream) {
+  if (n < 0 || batch < 0) return GPE_ERR_INVALID;
+  if (n == 0 || batch == 0) return GPE_OK;
+  axpy_kernel<<<grid_for(n * batch), 256, 0, (cudaStream_t)stream>>>(y, x, alpha, n, batch, y_stride, x_stride);
   return cudaGetLastError() == cudaSuccess ? GPE_OK : GPE_ERR_CUDA;
 }
 

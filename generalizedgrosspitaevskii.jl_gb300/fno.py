@@ -51,7 +51,8 @@ FNO_SIGNATURES = {
     "gpe_fno_gelu_bwd": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int64, ctypes.c_void_p]),
     "gpe_fno_bias_grad": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int64, ctypes.c_int64,
                                          ctypes.c_int64, ctypes.c_void_p]),
-    "gpe_fno_axpy": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_float, ctypes.c_int64, ctypes.c_void_p]),
+    "gpe_fno_axpy": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_float, ctypes.c_int64, ctypes.c_int64,
+                                    ctypes.c_int64, ctypes.c_int64, ctypes.c_void_p]),
     "gpe_fno_mse": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
                                    ctypes.c_int64, ctypes.c_void_p]),
     "gpe_fno_sum_slices": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int64, ctypes.c_int64,
@@ -77,6 +78,13 @@ def _ptr(t) -> int:
     return t.data_ptr()
 
 
+def _stream():
+    """torch's current CUDA stream, so the kernels order with torch's copies and can be
+    captured into a CUDA graph."""
+    import torch
+    return ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+
+
 def _chk(rc):
     if rc != 0:
         raise L.GPEError(rc, "FNO kernel launch failed")
@@ -86,7 +94,7 @@ def gemm(A, B, C, M, N, K, a, b, c, batch=1, alpha=1.0, beta=0.0):
     """C = alpha A B + beta C with (row, col, batch) strides a, b, c (element units)."""
     d = GemmDesc(_ptr(A), _ptr(B), _ptr(C), M, N, K, a[0], a[1], a[2] if len(a) > 2 else 0,
                  b[0], b[1], b[2] if len(b) > 2 else 0, c[0], c[1], c[2] if len(c) > 2 else 0, batch, alpha, beta)
-    _chk(_lib().gpe_fno_gemm(ctypes.byref(d), None))
+    _chk(_lib().gpe_fno_gemm(ctypes.byref(d), _stream()))
 
 
 def permute(src, dst, dims, perm):
@@ -95,7 +103,7 @@ def permute(src, dst, dims, perm):
     for i, (x, p) in enumerate(zip(dims, perm)):
         d.d[i] = x
         d.perm[i] = p
-    _chk(_lib().gpe_fno_permute(_ptr(src), _ptr(dst), ctypes.byref(d), None))
+    _chk(_lib().gpe_fno_permute(_ptr(src), _ptr(dst), ctypes.byref(d), _stream()))
 
 
 def inverse_perm(perm):
@@ -184,7 +192,7 @@ class FNO:
         for b in range(B):
             gemm(dy[b], x[b], part[b * chunks:], cout, cin, pc, (P, 1, pc), (1, P, pc), (cin, 1, cout * cin),
                  batch=chunks)
-        _chk(_lib().gpe_fno_sum_slices(_ptr(part), _ptr(dW), cout * cin, B * chunks, None))
+        _chk(_lib().gpe_fno_sum_slices(_ptr(part), _ptr(dW), cout * cin, B * chunks, _stream()))
 
     # -- spectral path S v
     def _spectral(self, l, v, B, save):
@@ -251,7 +259,7 @@ class FNO:
         cache = {"a": a, "layers": []}
         v = self._empty(B, C, P)
         self._pointwise(self.p["lift_w"], a, v, B, cfg.cin, C, P)
-        _chk(lib.gpe_fno_bias_act(_ptr(v), _ptr(self.p["lift_b"]), None, B, C, P, 0, None))
+        _chk(lib.gpe_fno_bias_act(_ptr(v), _ptr(self.p["lift_b"]), None, B, C, P, 0, _stream()))
         for l in range(cfg.layers):
             save = {} if train else None
             S = self._spectral(l, v, B, save)
@@ -259,21 +267,44 @@ class FNO:
             act = int(l < cfg.layers - 1)
             pre = self._empty(B, C, P) if (train and act) else None
             _chk(lib.gpe_fno_bias_act(_ptr(S), _ptr(self.p[f"b{l}"]), _ptr(pre) if pre is not None else None,
-                                      B, C, P, act, None))
+                                      B, C, P, act, _stream()))
             if train:
                 save.update(v=v, pre=pre)
                 cache["layers"].append(save)
             v = S
         out = self._empty(B, cfg.cout, P)
         self._pointwise(self.p["proj_w"], v, out, B, C, cfg.cout, P)
-        _chk(lib.gpe_fno_bias_act(_ptr(out), _ptr(self.p["proj_b"]), None, B, cfg.cout, P, 0, None))
+        _chk(lib.gpe_fno_bias_act(_ptr(out), _ptr(self.p["proj_b"]), None, B, cfg.cout, P, 0, _stream()))
         # residual: the output is the input field (channels 0..cout-1 of a) plus the change
-        for b in range(B):
-            _chk(lib.gpe_fno_axpy(_ptr(out[b]), _ptr(a[b]), 1.0, cfg.cout * P, None))
+        _chk(lib.gpe_fno_axpy(_ptr(out), _ptr(a), 1.0, cfg.cout * P, B, cfg.cout * P, cfg.cin * P, _stream()))
         cache["v_last"] = v
         if train:
             self.cache = cache
         return out
+
+    def graphed(self, B: int):
+        """The inference forward pass for batch B captured once into a CUDA graph.  Returns
+        run(x) -> out; out is a static buffer that the next run overwrites."""
+        import torch
+        graphs = self.__dict__.setdefault("_graphs", {})
+        if B not in graphs:
+            xs = torch.zeros((B, self.cfg.cin, self.cfg.N ** 2), device=self.dev)
+            side = torch.cuda.Stream()
+            side.wait_stream(torch.cuda.current_stream())
+            with torch.cuda.stream(side):
+                self.forward(xs)  # allocations happen outside the capture
+            torch.cuda.current_stream().wait_stream(side)
+            g = torch.cuda.CUDAGraph()
+            with torch.cuda.graph(g):
+                out = self.forward(xs)
+            graphs[B] = (g, xs, out)
+        g, xs, out = graphs[B]
+
+        def run(x):
+            xs.copy_(x)
+            g.replay()
+            return out
+        return run
 
     def backward(self, dout):
         """Gradients of the last training forward with respect to every parameter
@@ -282,7 +313,7 @@ class FNO:
         cache = self.cache
         B = dout.shape[0]
         lib = _lib()
-        _chk(lib.gpe_fno_bias_grad(_ptr(dout), _ptr(self.g["proj_b"]), B, cfg.cout, P, None))
+        _chk(lib.gpe_fno_bias_grad(_ptr(dout), _ptr(self.g["proj_b"]), B, cfg.cout, P, _stream()))
         self._pointwise_wgrad(dout, cache["v_last"], self.g["proj_w"], B, C, cfg.cout, P)
         dv = self._empty(B, C, P)
         # dv = proj_w^T dout
@@ -290,14 +321,14 @@ class FNO:
         for l in reversed(range(cfg.layers)):
             sv = cache["layers"][l]
             if sv["pre"] is not None:
-                _chk(lib.gpe_fno_gelu_bwd(_ptr(dv), _ptr(sv["pre"]), B * C * P, None))
-            _chk(lib.gpe_fno_bias_grad(_ptr(dv), _ptr(self.g[f"b{l}"]), B, C, P, None))
+                _chk(lib.gpe_fno_gelu_bwd(_ptr(dv), _ptr(sv["pre"]), B * C * P, _stream()))
+            _chk(lib.gpe_fno_bias_grad(_ptr(dv), _ptr(self.g[f"b{l}"]), B, C, P, _stream()))
             self._pointwise_wgrad(dv, sv["v"], self.g[f"w{l}"], B, C, C, P)
             dvin = self._spectral_bwd(l, dv, B, sv["Gm"])
             # pointwise path: dvin += W^T dv
             gemm(dv, self.p[f"w{l}"], dvin, P, C, C, (1, P, C * P), (C, 1, 0), (1, P, C * P), batch=B, beta=1.0)
             dv = dvin
-        _chk(lib.gpe_fno_bias_grad(_ptr(dv), _ptr(self.g["lift_b"]), B, C, P, None))
+        _chk(lib.gpe_fno_bias_grad(_ptr(dv), _ptr(self.g["lift_b"]), B, C, P, _stream()))
         self._pointwise_wgrad(dv, cache["a"], self.g["lift_w"], B, cfg.cin, C, P)
         self.cache = None
 
@@ -307,14 +338,14 @@ class FNO:
         n = pred.numel()
         grad = torch.empty_like(pred)
         acc = torch.zeros(1, dtype=torch.float64, device=self.dev)
-        _chk(_lib().gpe_fno_mse(_ptr(pred), _ptr(target), _ptr(grad), _ptr(acc), n, None))
+        _chk(_lib().gpe_fno_mse(_ptr(pred), _ptr(target), _ptr(grad), _ptr(acc), n, _stream()))
         return float(acc.item()) / n, grad
 
     def adam_step(self, lr=1e-3, b1=0.9, b2=0.999, eps=1e-8):
         self.t += 1
         for k in self.p:
             _chk(_lib().gpe_fno_adam(_ptr(self.p[k]), _ptr(self.g[k]), _ptr(self.m[k]), _ptr(self.v[k]),
-                                     self.p[k].numel(), lr, b1, b2, eps, self.t, None))
+                                     self.p[k].numel(), lr, b1, b2, eps, self.t, _stream()))
 
     def params_numpy(self):
         return {k: v.detach().cpu().numpy() for k, v in self.p.items()}
@@ -426,8 +457,11 @@ def hybrid_rollout(model: "FNO", A: float, windows: int, scale: float, check_eve
     """Advance the polariton from u0 = 0 by `windows` windows with the surrogate.  Every
     check_every-th window is judged: the plain solver advances the same state one window
     and the surrogate's prediction is accepted only if its rel L2 distance to the solver's
-    is <= tol; otherwise the solver's window is taken (fallback).  Returns (u1, u2,
-    stats) with stats = {checks, fallbacks, max_check_err, ms}."""
+    is <= tol.  Otherwise (fallback), and when the state left the training range or is no
+    longer finite (restart), the plain solver redoes the windows since the last accepted
+    state, so the result is never further from the plain solver than the accepted
+    surrogate windows make it.  Returns (u1, u2, stats)
+    with stats = {checks, fallbacks, restarts, max_check_err, ms}."""
     import time
     import torch
     from .strang import StrangSplitting, init
@@ -435,38 +469,86 @@ def hybrid_rollout(model: "FNO", A: float, windows: int, scale: float, check_eve
     it = init(prob, StrangSplitting(), (0.0, (windows + 1) * steps_per_window * dt), dt=dt, nsaves=windows + 1)
     it.lib.gpe_set_graph(it.h, steps_per_window)
     state = torch.tensor(fields_to_channels(np.zeros((N, N)), np.zeros((N, N)), A, scale), device="cuda")[None]
-    checks = fallbacks = 0
+    good, good_w = state.clone(), 0
+    checks = fallbacks = restarts = 0
     max_err = 0.0
+
+    def solver_windows(st, w0, n):
+        u1, u2 = channels_to_fields(st[0].cpu().numpy(), scale, N)
+        it.set_fields((u1, u2))
+        s = it.state()
+        s.steps, s.t = w0 * steps_per_window, w0 * steps_per_window * dt
+        it.set_state(s)
+        it.step(n * steps_per_window)
+        v1, v2 = it.get_fields()
+        return fields_to_channels(v1, v2, A, scale)
+
+    fwd = model.graphed(1)
     torch.cuda.synchronize()
     t0 = time.perf_counter()
     for w in range(windows):
-        pred = model.forward(state)
+        pred = fwd(state)
         if (w + 1) % check_every == 0:
             checks += 1
-            u1, u2 = channels_to_fields(state[0].cpu().numpy(), scale, N)
-            it.set_fields((u1, u2))
-            st = it.state()
-            st.steps = w * steps_per_window
-            it.set_state(st)
-            it.step(steps_per_window)
-            v1, v2 = it.get_fields()
-            ref = fields_to_channels(v1, v2, A, scale)
+            # a state that left the range of the training data (|channel| <= 1) or is no
+            # longer finite has diverged: the solver redoes the windows since the last
+            # accepted state
+            amax = float(state[0, :4].abs().max())
+            if not math.isfinite(amax) or amax > 4.0:
+                restarts += 1
+                ref = solver_windows(good, good_w, w + 1 - good_w)
+                state = torch.tensor(ref, device="cuda")[None]
+                good, good_w = state.clone(), w + 1
+                continue
+            ref = solver_windows(state, w, 1)
             got = pred[0, :4].cpu().numpy()
             err = float(np.linalg.norm(got - ref[:4]) / max(np.linalg.norm(ref[:4]), 1e-30))
+            if not math.isfinite(err):
+                err = float("inf")
             max_err = max(max_err, err)
             if err > tol:
+                # the surrogate is off here, so the windows since the last accepted state
+                # are not trusted either: the solver redoes them
                 fallbacks += 1
+                ref = solver_windows(good, good_w, w + 1 - good_w)
                 state = torch.tensor(ref, device="cuda")[None]
-                continue
+            else:
+                nxt = torch.empty_like(state)
+                nxt[:, :4] = pred
+                nxt[:, 4] = state[:, 4]
+                state = nxt
+            good, good_w = state.clone(), w + 1
+            continue
         nxt = torch.empty_like(state)
         nxt[:, :4] = pred
         nxt[:, 4] = state[:, 4]
         state = nxt
+    amax = float(state[0, :4].abs().max())
+    if not math.isfinite(amax) or amax > 4.0:
+        restarts += 1
+        state = torch.tensor(solver_windows(good, good_w, windows - good_w), device="cuda")[None]
     torch.cuda.synchronize()
     ms = (time.perf_counter() - t0) * 1e3
     it.close()
     u1, u2 = channels_to_fields(state[0].cpu().numpy(), scale, N)
-    return u1, u2, {"checks": checks, "fallbacks": fallbacks, "max_check_err": max_err, "ms": ms}
+    return u1, u2, {"checks": checks, "fallbacks": fallbacks, "restarts": restarts, "max_check_err": max_err,
+                    "ms": ms}
+
+
+def surrogate_window_ms(model: "FNO", batch: int, reps: int = 20) -> float:
+    """Mean time of one surrogate window (one graph-replayed forward pass) for `batch`
+    fields at once."""
+    import time
+    import torch
+    x = torch.zeros((batch, model.cfg.cin, model.cfg.N ** 2), device="cuda")
+    fwd = model.graphed(batch)
+    fwd(x)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(reps):
+        fwd(x)
+    torch.cuda.synchronize()
+    return (time.perf_counter() - t0) * 1e3 / reps
 
 
 def plain_rollout(A: float, windows: int, N: int = 128, L: float = 256.0, dt: float = 0.05,
@@ -489,3 +571,21 @@ def plain_rollout(A: float, windows: int, N: int = 128, L: float = 256.0, dt: fl
     u1, u2 = it.get_fields()
     it.close()
     return u1, u2, ms
+
+
+def plain_window_ms(batch: int, reps: int = 10, N: int = 128, L: float = 256.0, dt: float = 0.05,
+                    steps_per_window: int = 20, A: float = 3.0) -> float:
+    """Mean time of one plain-solver window (steps_per_window steps, graph mode) for
+    `batch` independent fields at once."""
+    import time
+    from .strang import StrangSplitting, init
+    z = np.zeros((N, N, batch), np.complex64) if batch > 1 else np.zeros((N, N), np.complex64)
+    prob = polariton_problem(N, L, A, u0=(z, z))
+    it = init(prob, StrangSplitting(), (0.0, (reps + 2) * steps_per_window * dt), dt=dt, nsaves=1)
+    it.lib.gpe_set_graph(it.h, steps_per_window)
+    it.step(steps_per_window)
+    t0 = time.perf_counter()
+    it.step(reps * steps_per_window)
+    ms = (time.perf_counter() - t0) * 1e3 / reps
+    it.close()
+    return ms

@@ -49,8 +49,9 @@ int gpe_fno_bias_act(float* x, const float* bias, float* pre, int64_t B, int64_t
 int gpe_fno_gelu_bwd(float* dy, const float* pre, int64_t n, void* stream);
 /* dbias[c] = sum_{b,p} dy[b][c][p] */
 int gpe_fno_bias_grad(const float* dy, float* dbias, int64_t B, int64_t C, int64_t P, void* stream);
-/* y += alpha * x */
-int gpe_fno_axpy(float* y, const float* x, float alpha, int64_t n, void* stream);
+/* y[z * y_stride + i] += alpha * x[z * x_stride + i] for z < batch, i < n */
+int gpe_fno_axpy(float* y, const float* x, float alpha, int64_t n, int64_t batch, int64_t y_stride, int64_t x_stride,
+                 void* stream);
 /* *loss_acc += sum (pred - target)^2 (FP64); grad (may be NULL) = 2 (pred - target) / n */
 int gpe_fno_mse(const float* pred, const float* target, float* grad, double* loss_acc, int64_t n, void* stream);
 /* dst[i] = sum over z < slices of src[z*n + i] (split-K reduction) */

@@ -119,7 +119,7 @@ def test_matrix_nonlinearity_1d_philox(gpe, oracle, lib, fp64):
 
 @pytest.mark.parametrize("dtype,fp64", PRECISIONS, ids=PREC_IDS)
 def test_matrix_nonlinearity_3d(gpe, oracle, lib, dtype, fp64):
-    shape_c, L = (8, 16, 32), (8.0, 6.0, 5.0)
+    shape_c, L = (16, 16, 32), (8.0, 6.0, 5.0)
     a, b = two_comp_u0(shape_c, L)
     disp = lambda k, p: (k[0] ** 2 + k[1] ** 2 + k[2] ** 2) / 2
     gkw = dict(u0=(jl(a).astype(dtype), jl(b).astype(dtype)), lengths=L, dispersion=disp, nonlinearity=gmat_closure)
