@@ -224,6 +224,23 @@ def algorithmic_bytes(dtype):
     return {"row": row, "col": col}
 
 
+def dram_traffic(dtype: str, fp64: str, kernel: str):
+    """DRAM bytes per grid point of one launch of `kernel` ("row" / "col"), read from the
+    ncu summary in profiles/dram_traffic.md (rows "| precision | pass | bytes |"), or None."""
+    p = ROOT / "profiles" / "dram_traffic.md"
+    if not p.exists():
+        return None
+    prec = "f32" if dtype == "c64" else ("f64" if fp64 == "native" else "f64-dw")
+    for ln in p.read_text().splitlines():
+        cells = [c.strip() for c in ln.strip().strip("|").split("|")]
+        if len(cells) >= 3 and cells[0] == prec and cells[1] == kernel:
+            try:
+                return float(cells[2])
+            except ValueError:
+                return None
+    return None
+
+
 def run_gpu(args, rank, world, local_rank):
     import __graft_entry__ as G
     pkg = G.load_package()
@@ -311,15 +328,9 @@ def run_gpu(args, rank, world, local_rank):
     dom = max(per_launch, key=lambda k: kms[0] if k == "row" else kms[1])
     d_ms, d_b = per_launch[dom]
     achieved = d_b * P * B / (d_ms * 1e-3) / 1e9
-    traffic = None
-    tp = ROOT / "profiles" / "traffic.json"
-    if tp.exists():
-        try:
-            traffic = json.loads(tp.read_text()).get(f"{args.dtype}_{dom}_bytes_per_point")
-            if traffic is not None:
-                traffic = traffic * P * B
-        except Exception:
-            traffic = None
+    traffic = dram_traffic(args.dtype, args.fp64, dom)
+    if traffic is not None:
+        traffic = traffic * P * B
     line = {
         "metric": "grid-point-steps/s", "value": value, "unit": "grid-point-steps/s", "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_clean / args.steps, "higher_is_better": True,

@@ -51,13 +51,18 @@ struct LineCfg {
 #define GPE_ROW_MIN_BLOCKS 2
 #endif
 #ifndef GPE_ROW_MIN_BLOCKS_F32
-#define GPE_ROW_MIN_BLOCKS_F32 2
+#define GPE_ROW_MIN_BLOCKS_F32 3
 #endif
-  static constexpr int ROW_MINB = sizeof(C) == 8 ? GPE_ROW_MIN_BLOCKS_F32 : GPE_ROW_MIN_BLOCKS;
+  // blocks of more than 256 threads (lines of 4096 points) keep 128 registers a thread
+  static constexpr int ROW_MINB = L * TR > 256 ? 1 : (sizeof(C) == 8 ? GPE_ROW_MIN_BLOCKS_F32 : GPE_ROW_MIN_BLOCKS);
   static constexpr int COL_MINB_WANT = sizeof(C) == 8 ? 2 : 1;
   static constexpr int COL_THREADS = CC * T;
   static constexpr int COL_MINB = COL_THREADS <= 512 ? COL_MINB_WANT : 1;
   static constexpr size_t ROW_SMEM = (size_t)L * N * sizeof(C);
+  // 16-byte precisions stage the half steps through shared memory (every component of
+  // every line of the block), so one non-unrolled point loop needs no register rotation
+  static constexpr bool ROW_STAGE = sizeof(C) == 16 && (size_t)M * L * N * sizeof(C) <= 96 * 1024;
+  static constexpr size_t ROW_KERNEL_SMEM = ROW_STAGE ? (size_t)M * L * N * sizeof(C) : ROW_SMEM;
   static constexpr size_t COL_SMEM = (size_t)CC * N * sizeof(C);
 };
 
@@ -536,6 +541,51 @@ __device__ __forceinline__ void half_points(typename CT<Real>::T (&x)[M][E], con
   }
 }
 
+// Half steps A and B (with the save between them) of the points a thread holds, staged
+// through shared memory: x[m][i] (point p0 + T*i) goes to slot line[m*cstride + t + T*i],
+// one non-unrolled loop visits the points, and the results come back into x.  Used for
+// 16-byte precisions, whose half step is several hundred instructions: one copy of it,
+// and no register rotation.
+template <typename Real, int M, int E>
+__device__ __forceinline__ void staged_halves(typename CT<Real>::T (&x)[M][E], const PassArgs& a,
+                                              typename CT<Real>::T* line, int cstride, int t, int T, int64_t p0,
+                                              int64_t g0, int64_t b, bool active) {
+  using C = typename CT<Real>::T;
+  if (a.hA < 0 && a.hB < 0 && !a.save[0]) return;  // FFT-only pass
+  const int64_t kb = a.kbase ? 2 * *a.kbase : 0;
+#pragma unroll
+  for (int m = 0; m < M; ++m)
+#pragma unroll
+    for (int i = 0; i < E; ++i) line[m * cstride + t + T * i] = x[m][i];
+#pragma unroll 1
+  for (int i = 0; i < E; ++i) {
+    C v[M];
+#pragma unroll
+    for (int m = 0; m < M; ++m) v[m] = line[m * cstride + t + T * i];
+    const int64_t p = p0 + (int64_t)T * i;
+#pragma unroll 1
+    for (int hh = 0; hh < 2; ++hh) {
+      const int64_t hr = hh ? a.hB : a.hA;
+      if (hr >= 0) {
+        C pn[M], px[M];
+        load_pump<Real, M>(a, hr + kb, pn, px);
+        half_step<Real, M>(v, a, p, b, hr + kb, pn, px);
+      }
+      if (hh == 0 && a.save[0] && active) {
+#pragma unroll
+        for (int m = 0; m < M; ++m) store_save<Real>(a.save[m], g0 + (int64_t)T * i, v[m]);
+      }
+    }
+#pragma unroll
+    for (int m = 0; m < M; ++m) line[m * cstride + t + T * i] = v[m];
+  }
+#pragma unroll
+  for (int m = 0; m < M; ++m)
+#pragma unroll
+    for (int i = 0; i < E; ++i) x[m][i] = line[m * cstride + t + T * i];
+  __syncthreads();  // the next line transform's exchange reuses these slots
+}
+
 // ------------------------------------------------------------------ row pass
 template <typename Real, int LOGN, int M>
 __global__ void __launch_bounds__(LineCfg<Real, M, LOGN>::ROW_THREADS, LineCfg<Real, M, LOGN>::ROW_MINB)
@@ -569,6 +619,12 @@ row_kernel(const PassArgs a, const int64_t nlines) {
   for (int ph = 0; ph < 4; ++ph) {
     if (ph == 0 || ph == 3) {
       if (ph == 0 ? a.do_ifft : a.do_fft) fft_components<C, N, E, M>(x, ph == 0, t, lay, tw);
+      continue;
+    }
+    if constexpr (Cfg::ROW_STAGE) {
+      // both half steps (and the save between them) in one pass over the points, staged
+      // through this line's shared-memory slots; each thread touches only its own slots
+      if (ph == 1) staged_halves<Real, M, E>(x, a, sm + l * N, L * N, t, T, p0, g0, b, active);
       continue;
     }
     const int64_t hr = ph == 2 ? a.hB : a.hA;
@@ -1005,10 +1061,10 @@ template <typename Real, int M, int LOGN>
 int launch_row_n(const PassArgs& a, int64_t nlines, cudaStream_t s) {
   using Cfg = LineCfg<Real, M, LOGN>;
   auto k = row_kernel<Real, LOGN, M>;
-  int e = set_smem(k, Cfg::ROW_SMEM);
+  int e = set_smem(k, Cfg::ROW_KERNEL_SMEM);
   if (e) return e;
   const int64_t blocks = (nlines + Cfg::L - 1) / Cfg::L;
-  k<<<(unsigned)blocks, Cfg::ROW_THREADS, Cfg::ROW_SMEM, s>>>(a, nlines);
+  k<<<(unsigned)blocks, Cfg::ROW_THREADS, Cfg::ROW_KERNEL_SMEM, s>>>(a, nlines);
   return (int)cudaGetLastError();
 }
 template <typename Real, int M, int LOGN>
