@@ -214,13 +214,15 @@ def config_dict(dtype, B, world):
             "parallelism": f"replicas x{world}" if world > 1 else "single GPU"}
 
 
-def algorithmic_bytes(dtype):
-    """Bytes per grid point per launch of each pass (fields read + written once, tables
-    and pump profile read once).  c = complex size, r = real size."""
+def algorithmic_bytes(dtype, B: int):
+    """Bytes per grid point (of one copy) per launch of each pass: both components read
+    and written once, plus the tables every copy shares read once per launch (the photon
+    pump profile, r bytes a point; the 2x2 k-space table, 4c bytes a point) and so
+    divided over the B copies.  c = complex size, r = real size."""
     c = 16 if dtype == np.complex128 else 8
     r = c // 2
-    row = 2 * 2 * c + r       # 2 components in + out, photon pump profile
-    col = 2 * 2 * c + 4 * c   # 2 components in + out, 2x2 k-space table
+    row = 2 * 2 * c + r / B
+    col = 2 * 2 * c + 4 * c / B
     return {"row": row, "col": col}
 
 
@@ -322,7 +324,7 @@ def run_gpu(args, rank, world, local_rank):
 
     if rank != 0:
         return
-    ab = algorithmic_bytes(dtype)
+    ab = algorithmic_bytes(dtype, B)
     peak, peak_kind = measured_peaks()
     per_launch = {"row": (kms[0] / max(kn[0], 1), ab["row"]), "col": (kms[1] / max(kn[1], 1), ab["col"])}
     dom = max(per_launch, key=lambda k: kms[0] if k == "row" else kms[1])

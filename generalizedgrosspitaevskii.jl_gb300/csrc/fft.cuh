@@ -269,4 +269,79 @@ __device__ __forceinline__ void fft_line(C (&x)[E], int t, const Lay& lay, const
   for (int i = 0; i < E; ++i) x[i] = bfinish(x[i]);
 }
 
+// Joint transform of the M lines (components) a thread holds: each twiddle is loaded
+// once for all components, and one pair of barriers per stage serves all of them.
+// Component m exchanges through lay.base + m * cstride.
+template <typename C, int N, int E, int R, int NS, int DIR, bool LAST, int M, class Lay>
+__device__ __forceinline__ void fft_stage_joint(C (&x)[M][E], int t, const Lay& lay, int cstride,
+                                                const C* __restrict__ tw) {
+  constexpr int T = N / E, Q = E / R;
+#pragma unroll
+  for (int q = 0; q < Q; ++q) {
+    C v[M][R];
+#pragma unroll
+    for (int m = 0; m < M; ++m)
+#pragma unroll
+      for (int r = 0; r < R; ++r) v[m][r] = x[m][q + r * Q];
+    const int j = t + q * T;
+    if constexpr (NS > 1) {
+      const int k = j & (NS - 1);
+      constexpr int TS = N / (NS * R);
+#pragma unroll
+      for (int r = 1; r < R; ++r) {
+        const C w = ldgc(tw + k * r * TS);
+#pragma unroll
+        for (int m = 0; m < M; ++m) v[m][r] = (DIR < 0) ? cmul(v[m][r], w) : cmulc(v[m][r], w);
+      }
+    }
+#pragma unroll
+    for (int m = 0; m < M; ++m) dft_regs<R, DIR>(v[m]);
+    if constexpr (LAST) {
+#pragma unroll
+      for (int m = 0; m < M; ++m)
+#pragma unroll
+        for (int r = 0; r < R; ++r) x[m][q + r * Q] = v[m][r];
+    } else {
+      const int jb = (j / NS) * NS * R + (j & (NS - 1));
+#pragma unroll
+      for (int r = 0; r < R; ++r) {
+        const int ad = lay.template addr<NS, R>(jb + r * NS);
+#pragma unroll
+        for (int m = 0; m < M; ++m) lay.base[m * cstride + ad] = v[m][r];
+      }
+    }
+  }
+}
+
+template <typename C, int N, int E, int DIR, int NS, int M, class Lay>
+__device__ __forceinline__ void fft_stages_joint(C (&x)[M][E], int t, const Lay& lay, int cstride,
+                                                 const C* __restrict__ tw) {
+  constexpr int REM = N / NS;
+  constexpr int R = REM >= E ? E : REM;
+  constexpr bool LAST = (NS * R == N);
+  constexpr int T = N / E;
+  fft_stage_joint<C, N, E, R, NS, DIR, LAST, M>(x, t, lay, cstride, tw);
+  if constexpr (!LAST) {
+    __syncthreads();
+#pragma unroll
+    for (int i = 0; i < E; ++i) {
+      const int ad = lay.template addr<NS, R>(t + T * i);
+#pragma unroll
+      for (int m = 0; m < M; ++m) x[m][i] = lay.base[m * cstride + ad];
+    }
+    __syncthreads();
+    fft_stages_joint<C, N, E, DIR, NS * R, M>(x, t, lay, cstride, tw);
+  }
+}
+
+template <typename C, int N, int E, int DIR, int M, class Lay>
+__device__ __forceinline__ void fft_line_joint(C (&x)[M][E], int t, const Lay& lay, int cstride,
+                                               const C* __restrict__ tw) {
+  fft_stages_joint<C, N, E, DIR, 1, M>(x, t, lay, cstride, tw);
+#pragma unroll
+  for (int m = 0; m < M; ++m)
+#pragma unroll
+    for (int i = 0; i < E; ++i) x[m][i] = bfinish(x[m][i]);
+}
+
 }  // namespace gpe

@@ -45,7 +45,10 @@ struct LineCfg {
   static constexpr int CCMAX = 128 / (int)sizeof(C);  // columns per tile: one 128-byte row
   static constexpr int TPB = (M == 2) ? 512 : 1024;
   static constexpr int SMEM_LIMIT = 200 * 1024;
-  static constexpr int CC = cmax(1, cmin(cmin(CCMAX, cmax(1, TPB / T)), pow2floor(SMEM_LIMIT / (N * (int)sizeof(C)))));
+  // FP32 lines of two components transform jointly (each component its own exchange)
+  static constexpr bool JOINT = sizeof(C) == 8 && M == 2;
+  static constexpr int CC = cmax(1, cmin(cmin(CCMAX, cmax(1, TPB / T)),
+                                         pow2floor(SMEM_LIMIT / (N * (int)sizeof(C) * (JOINT ? M : 1)))));
   static constexpr int ROW_THREADS = L * TR;
 #ifndef GPE_ROW_MIN_BLOCKS
 #define GPE_ROW_MIN_BLOCKS 2
@@ -59,11 +62,8 @@ struct LineCfg {
   static constexpr int COL_THREADS = CC * T;
   static constexpr int COL_MINB = COL_THREADS <= 512 ? COL_MINB_WANT : 1;
   static constexpr size_t ROW_SMEM = (size_t)L * N * sizeof(C);
-  // 16-byte precisions stage the half steps through shared memory (every component of
-  // every line of the block), so one non-unrolled point loop needs no register rotation
-  static constexpr bool ROW_STAGE = sizeof(C) == 16 && (size_t)M * L * N * sizeof(C) <= 96 * 1024;
-  static constexpr size_t ROW_KERNEL_SMEM = ROW_STAGE ? (size_t)M * L * N * sizeof(C) : ROW_SMEM;
-  static constexpr size_t COL_SMEM = (size_t)CC * N * sizeof(C);
+  static constexpr size_t ROW_KERNEL_SMEM = JOINT ? (size_t)M * L * N * sizeof(C) : ROW_SMEM;
+  static constexpr size_t COL_SMEM = (size_t)(JOINT ? M : 1) * CC * N * sizeof(C);
 };
 
 // ------------------------------------------------------------------ scalar helpers
@@ -482,9 +482,22 @@ __device__ __forceinline__ void conj_all(C (&x)[E]) {
 // Transform every component's line in place: forward (unnormalised) or inverse (the
 // 1/P is folded into the k-space table).  One FFT instance serves all components and
 // both directions: component 1 is swapped into the slot of component 0 and back.
-template <typename C, int N, int E, int M, class Lay>
+template <typename C, int N, int E, int M, class Lay, bool JOINT = false>
 __device__ __forceinline__ void fft_components(C (&x)[M][E], bool inverse, int t, const Lay& lay,
-                                               const C* __restrict__ tw) {
+                                               const C* __restrict__ tw, int cstride = 0) {
+  if constexpr (JOINT) {
+    // all components in one pass (FP32: the twiddle loads and barriers are shared)
+    if (inverse) {
+#pragma unroll
+      for (int m = 0; m < M; ++m) conj_all(x[m]);
+    }
+    fft_line_joint<C, N, E, -1, M>(x, t, lay, cstride, tw);
+    if (inverse) {
+#pragma unroll
+      for (int m = 0; m < M; ++m) conj_all(x[m]);
+    }
+    return;
+  }
 #pragma unroll 1
   for (int m = 0; m < M; ++m) {
     if (inverse) conj_all(x[0]);
@@ -541,51 +554,6 @@ __device__ __forceinline__ void half_points(typename CT<Real>::T (&x)[M][E], con
   }
 }
 
-// Half steps A and B (with the save between them) of the points a thread holds, staged
-// through shared memory: x[m][i] (point p0 + T*i) goes to slot line[m*cstride + t + T*i],
-// one non-unrolled loop visits the points, and the results come back into x.  Used for
-// 16-byte precisions, whose half step is several hundred instructions: one copy of it,
-// and no register rotation.
-template <typename Real, int M, int E>
-__device__ __forceinline__ void staged_halves(typename CT<Real>::T (&x)[M][E], const PassArgs& a,
-                                              typename CT<Real>::T* line, int cstride, int t, int T, int64_t p0,
-                                              int64_t g0, int64_t b, bool active) {
-  using C = typename CT<Real>::T;
-  if (a.hA < 0 && a.hB < 0 && !a.save[0]) return;  // FFT-only pass
-  const int64_t kb = a.kbase ? 2 * *a.kbase : 0;
-#pragma unroll
-  for (int m = 0; m < M; ++m)
-#pragma unroll
-    for (int i = 0; i < E; ++i) line[m * cstride + t + T * i] = x[m][i];
-#pragma unroll 1
-  for (int i = 0; i < E; ++i) {
-    C v[M];
-#pragma unroll
-    for (int m = 0; m < M; ++m) v[m] = line[m * cstride + t + T * i];
-    const int64_t p = p0 + (int64_t)T * i;
-#pragma unroll 1
-    for (int hh = 0; hh < 2; ++hh) {
-      const int64_t hr = hh ? a.hB : a.hA;
-      if (hr >= 0) {
-        C pn[M], px[M];
-        load_pump<Real, M>(a, hr + kb, pn, px);
-        half_step<Real, M>(v, a, p, b, hr + kb, pn, px);
-      }
-      if (hh == 0 && a.save[0] && active) {
-#pragma unroll
-        for (int m = 0; m < M; ++m) store_save<Real>(a.save[m], g0 + (int64_t)T * i, v[m]);
-      }
-    }
-#pragma unroll
-    for (int m = 0; m < M; ++m) line[m * cstride + t + T * i] = v[m];
-  }
-#pragma unroll
-  for (int m = 0; m < M; ++m)
-#pragma unroll
-    for (int i = 0; i < E; ++i) x[m][i] = line[m * cstride + t + T * i];
-  __syncthreads();  // the next line transform's exchange reuses these slots
-}
-
 // ------------------------------------------------------------------ row pass
 template <typename Real, int LOGN, int M>
 __global__ void __launch_bounds__(LineCfg<Real, M, LOGN>::ROW_THREADS, LineCfg<Real, M, LOGN>::ROW_MINB)
@@ -618,13 +586,8 @@ row_kernel(const PassArgs a, const int64_t nlines) {
 #pragma unroll 1
   for (int ph = 0; ph < 4; ++ph) {
     if (ph == 0 || ph == 3) {
-      if (ph == 0 ? a.do_ifft : a.do_fft) fft_components<C, N, E, M>(x, ph == 0, t, lay, tw);
-      continue;
-    }
-    if constexpr (Cfg::ROW_STAGE) {
-      // both half steps (and the save between them) in one pass over the points, staged
-      // through this line's shared-memory slots; each thread touches only its own slots
-      if (ph == 1) staged_halves<Real, M, E>(x, a, sm + l * N, L * N, t, T, p0, g0, b, active);
+      if (ph == 0 ? a.do_ifft : a.do_fft)
+        fft_components<C, N, E, M, RowLayout<C>, Cfg::JOINT>(x, ph == 0, t, lay, tw, L * N);
       continue;
     }
     const int64_t hr = ph == 2 ? a.hB : a.hA;
@@ -674,7 +637,8 @@ col_kernel(const PassArgs a) {
 #pragma unroll 1
   for (int ph = 0; ph < 3; ++ph) {
     if (ph != 1) {
-      if (ph == 0 ? a.col_fwd : a.col_inv) fft_components<C, N, E, M>(x, ph == 2, t, lay, tw);
+      if (ph == 0 ? a.col_fwd : a.col_inv)
+        fft_components<C, N, E, M, ColLayout<C, CC>, Cfg::JOINT>(x, ph == 2, t, lay, tw, CC * N);
       continue;
     }
     if (a.ktab) {
