@@ -203,13 +203,16 @@ struct RowLayout {
   }
 };
 
-// Column layout: CC lines (columns) interleaved, point n of column c at n*CC + c.
-// Threads of the same row touch consecutive slots, so no swizzle is needed.
+// Column layout: CC lines (columns) interleaved, point n of column c at
+// (n + n/8)*CC + c: one padding row after every 8 rows.  The reads of a stage and the
+// writes of the later stages touch consecutive rows; the first stage writes rows 8t + r
+// for neighbouring threads t, which the padding spreads over both halves of the bank
+// space (without it, 8-byte elements hit the same 16 banks four times over).
 template <typename C, int CC>
 struct ColLayout {
   C* base;  // already offset by the column index
   template <int NS, int R>
-  __device__ __forceinline__ int addr(int idx) const { return idx * CC; }
+  __device__ __forceinline__ int addr(int idx) const { return (idx + (idx >> 3)) * CC; }
 };
 
 // One Stockham stage.  x: this thread's E points; t: thread index in the line.

@@ -47,8 +47,9 @@ struct LineCfg {
   static constexpr int SMEM_LIMIT = 200 * 1024;
   // FP32 lines of two components transform jointly (each component its own exchange)
   static constexpr bool JOINT = sizeof(C) == 8 && M == 2;
+  static constexpr int NPAD = N + N / 8;  // rows of a column-pass exchange (ColLayout padding)
   static constexpr int CC = cmax(1, cmin(cmin(CCMAX, cmax(1, TPB / T)),
-                                         pow2floor(SMEM_LIMIT / (N * (int)sizeof(C) * (JOINT ? M : 1)))));
+                                         pow2floor(SMEM_LIMIT / (NPAD * (int)sizeof(C) * (JOINT ? M : 1)))));
   static constexpr int ROW_THREADS = L * TR;
 #ifndef GPE_ROW_MIN_BLOCKS
 #define GPE_ROW_MIN_BLOCKS 2
@@ -63,7 +64,7 @@ struct LineCfg {
   static constexpr int COL_MINB = COL_THREADS <= 512 ? COL_MINB_WANT : 1;
   static constexpr size_t ROW_SMEM = (size_t)L * N * sizeof(C);
   static constexpr size_t ROW_KERNEL_SMEM = JOINT ? (size_t)M * L * N * sizeof(C) : ROW_SMEM;
-  static constexpr size_t COL_SMEM = (size_t)(JOINT ? M : 1) * CC * N * sizeof(C);
+  static constexpr size_t COL_SMEM = (size_t)(JOINT ? M : 1) * CC * NPAD * sizeof(C);
 };
 
 // ------------------------------------------------------------------ scalar helpers
@@ -496,19 +497,19 @@ __device__ __forceinline__ void fft_components(C (&x)[M][E], bool inverse, int t
 #pragma unroll
       for (int m = 0; m < M; ++m) conj_all(x[m]);
     }
-    return;
-  }
+  } else {
 #pragma unroll 1
-  for (int m = 0; m < M; ++m) {
-    if (inverse) conj_all(x[0]);
-    fft_line<C, N, E, -1>(x[0], t, lay, tw);
-    if (inverse) conj_all(x[0]);
-    if constexpr (M == 2) {
+    for (int m = 0; m < M; ++m) {
+      if (inverse) conj_all(x[0]);
+      fft_line<C, N, E, -1>(x[0], t, lay, tw);
+      if (inverse) conj_all(x[0]);
+      if constexpr (M == 2) {
 #pragma unroll
-      for (int i = 0; i < E; ++i) {
-        const C tmp = x[0][i];
-        x[0][i] = x[1][i];
-        x[1][i] = tmp;
+        for (int i = 0; i < E; ++i) {
+          const C tmp = x[0][i];
+          x[0][i] = x[1][i];
+          x[1][i] = tmp;
+        }
       }
     }
   }
@@ -525,7 +526,14 @@ __device__ __forceinline__ void half_points(typename CT<Real>::T (&x)[M][E], con
   using C = typename CT<Real>::T;
   C pn[M], px[M];
   load_pump<Real, M>(a, h, pn, px);
-  if constexpr (sizeof(C) <= 8) {
+// FP32 points per trip of the half-step loop: 2 measured fastest on the 512^2 polariton
+// row pass (0.61 ms against 0.68 ms with all 8 unrolled, whose code spills out of the
+// instruction cache, and 0.64 ms with 1)
+#ifndef GPE_F32_HALF_UNROLL
+#define GPE_F32_HALF_UNROLL 2
+#endif
+  constexpr int U = GPE_F32_HALF_UNROLL < E ? GPE_F32_HALF_UNROLL : E;
+  if constexpr (sizeof(C) <= 8 && U == E) {
     // FP32: the half step is short, so unrolled copies fit the instruction cache and
     // interleave the independent points
 #pragma unroll
@@ -536,6 +544,25 @@ __device__ __forceinline__ void half_points(typename CT<Real>::T (&x)[M][E], con
       half_step<Real, M>(v, a, p0 + (int64_t)T * i, b, h, pn, px);
 #pragma unroll
       for (int m = 0; m < M; ++m) x[m][i] = v[m];
+    }
+  } else if constexpr (sizeof(C) <= 8) {
+    // FP32, U points a trip: U copies of the half step, the arrays rotated by U a trip
+#pragma unroll 1
+    for (int i0 = 0; i0 < E; i0 += U) {
+      C v[U][M];
+#pragma unroll
+      for (int u = 0; u < U; ++u) {
+#pragma unroll
+        for (int m = 0; m < M; ++m) v[u][m] = x[m][u];
+        half_step<Real, M>(v[u], a, p0 + (int64_t)T * (i0 + u), b, h, pn, px);
+      }
+#pragma unroll
+      for (int m = 0; m < M; ++m) {
+#pragma unroll
+        for (int q = 0; q + U < E; ++q) x[m][q] = x[m][q + U];
+#pragma unroll
+        for (int u = 0; u < U; ++u) x[m][E - U + u] = v[u][m];
+      }
     }
   } else {
 #pragma unroll 1
@@ -638,7 +665,7 @@ col_kernel(const PassArgs a) {
   for (int ph = 0; ph < 3; ++ph) {
     if (ph != 1) {
       if (ph == 0 ? a.col_fwd : a.col_inv)
-        fft_components<C, N, E, M, ColLayout<C, CC>, Cfg::JOINT>(x, ph == 2, t, lay, tw, CC * N);
+        fft_components<C, N, E, M, ColLayout<C, CC>, Cfg::JOINT>(x, ph == 2, t, lay, tw, CC * Cfg::NPAD);
       continue;
     }
     if (a.ktab) {
