@@ -197,15 +197,25 @@ __device__ __forceinline__ void load_pump(const PassArgs& a, int64_t h, typename
   }
 }
 
-// xi for half step h at point p of trajectory b (Philox or replayed)
+// xi for half step h at point p of trajectory b (Philox or replayed).  Philox blocks:
+// with two components the point's own block, words (0,1) and (2,3); with one component
+// the points x and x + n0/2 of a row share the block of the lower one (words (0,1) for
+// it, (2,3) for the upper one), so no draw is wasted.
 template <typename Real, int M>
 __device__ __forceinline__ void draw_xi(const PassArgs& a, int64_t p, int64_t b, int64_t h,
                                         typename CT<Real>::T (&xi)[M]) {
   using C = typename CT<Real>::T;
   if (a.noise == NOISE_PHILOX) {
-    const uint4 r = Philox4x32::gen(noise_counter(p, b, h), a.seed_lo, a.seed_hi);
-    xi[0] = Xi<Real>::get(r.x, r.y);
-    if constexpr (M == 2) xi[M - 1] = Xi<Real>::get(r.z, r.w);
+    if constexpr (M == 1) {
+      const int64_t hx = a.n0 >> 1;
+      const bool up = (p & (a.n0 - 1)) >= hx;
+      const uint4 r = Philox4x32::gen(noise_counter(up ? p - hx : p, b, h), a.seed_lo, a.seed_hi);
+      xi[0] = Xi<Real>::get(up ? r.z : r.x, up ? r.w : r.y);
+    } else {
+      const uint4 r = Philox4x32::gen(noise_counter(p, b, h), a.seed_lo, a.seed_hi);
+      xi[0] = Xi<Real>::get(r.x, r.y);
+      xi[M - 1] = Xi<Real>::get(r.z, r.w);
+    }
   } else {
     const C* xb = (const C*)a.xi;
 #pragma unroll
@@ -309,7 +319,8 @@ template <typename Real, int M>
 __device__ __forceinline__ void half_step(typename CT<Real>::T (&u)[M], const PassArgs& a,
                                           int64_t p, int64_t b, int64_t h,
                                           const typename CT<Real>::T (&pn)[M],
-                                          const typename CT<Real>::T (&px)[M]) {
+                                          const typename CT<Real>::T (&px)[M],
+                                          const typename CT<Real>::T* xi_pre = nullptr) {
   using C = typename CT<Real>::T;
   C E[M];
   bool hasE[M];
@@ -408,7 +419,12 @@ __device__ __forceinline__ void half_step(typename CT<Real>::T (&u)[M], const Pa
     if (a.pprof[j]) u[j] = cadd(u[j], pump_mul(px[j], prof[j], a.pprof_cplx));
   if (a.noise != NOISE_OFF) {
     C xi[M];
-    draw_xi<Real, M>(a, p, b, h, xi);
+    if (xi_pre) {
+#pragma unroll
+      for (int j = 0; j < M; ++j) xi[j] = xi_pre[j];
+    } else {
+      draw_xi<Real, M>(a, p, b, h, xi);
+    }
 #pragma unroll
     for (int j = 0; j < M; ++j) {
       C nf;
@@ -544,6 +560,31 @@ __device__ __forceinline__ void half_points(typename CT<Real>::T (&x)[M][E], con
       half_step<Real, M>(v, a, p0 + (int64_t)T * i, b, h, pn, px);
 #pragma unroll
       for (int m = 0; m < M; ++m) x[m][i] = v[m];
+    }
+  } else if constexpr (sizeof(C) <= 8 && M == 1) {
+    // FP32, one component: a trip takes the points x and x + n0/2 (slots i and i + E/2),
+    // which share one Philox block; both halves of the array rotate by one a trip
+    constexpr int H = E / 2;
+#pragma unroll 1
+    for (int i = 0; i < H; ++i) {
+      C v0[1] = {x[0][0]}, v1[1] = {x[0][H]};
+      const int64_t pa = p0 + (int64_t)T * i, pb = pa + (int64_t)T * H;
+      C xa[1], xb[1];
+      const bool pre = a.noise == NOISE_PHILOX;
+      if (pre) {
+        const uint4 r = Philox4x32::gen(noise_counter(pa, b, h), a.seed_lo, a.seed_hi);
+        xa[0] = Xi<Real>::get(r.x, r.y);
+        xb[0] = Xi<Real>::get(r.z, r.w);
+      }
+      half_step<Real, 1>(v0, a, pa, b, h, pn, px, pre ? xa : nullptr);
+      half_step<Real, 1>(v1, a, pb, b, h, pn, px, pre ? xb : nullptr);
+#pragma unroll
+      for (int q = 0; q + 1 < H; ++q) {
+        x[0][q] = x[0][q + 1];
+        x[0][H + q] = x[0][H + q + 1];
+      }
+      x[0][H - 1] = v0[0];
+      x[0][E - 1] = v1[0];
     }
   } else if constexpr (sizeof(C) <= 8) {
     // FP32, U points a trip: U copies of the half step, the arrays rotated by U a trip

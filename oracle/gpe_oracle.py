@@ -502,8 +502,10 @@ def box_muller_f32(w0, w1):
 
 class PhiloxNoise:
     """xi for half step h as drawn by the GPU noise path: counter (point, trajectory,
-    h mod 2^32, h >> 32), key (seed mod 2^32, seed >> 32); components 0 and 1 use word
-    pairs (0,1) and (2,3).  Returns (M, *batch, *spatial) in C order."""
+    h mod 2^32, h >> 32), key (seed mod 2^32, seed >> 32).  Two components: point p draws
+    its own block, components 0 and 1 use word pairs (0,1) and (2,3).  One component: the
+    points x and x + nx/2 of a row share the block of the lower one, which takes words
+    (0,1) and the upper one (2,3).  Returns (M, *batch, *spatial) in C order."""
 
     def __init__(self, seed: int, M: int, batch_shape, spatial_shape_c, fp32: bool = False):
         self.seed = int(seed)
@@ -517,11 +519,19 @@ class PhiloxNoise:
         B = int(np.prod(self.batch_shape)) if self.batch_shape else 1
         p = np.tile(np.arange(P, dtype=np.uint64), B)
         b = np.repeat(np.arange(B, dtype=np.uint64), P)
+        upper = None
+        if self.M == 1:
+            half = np.uint64(self.spatial[-1] // 2)
+            upper = (p % np.uint64(self.spatial[-1])) >= half
+            p = np.where(upper, p - half, p)
         hl = np.full(P * B, h & 0xFFFFFFFF, np.uint64)
         hh = np.full(P * B, (h >> 32) & 0xFFFFFFFF, np.uint64)
         w = philox4x32_10(p, b, hl, hh, self.seed & 0xFFFFFFFF, (self.seed >> 32) & 0xFFFFFFFF)
         bm = box_muller_f32 if self.fp32 else box_muller_f64
-        xs = [bm(w[0], w[1]), bm(w[2], w[3])][: self.M]
+        if self.M == 1:
+            xs = [np.where(upper, bm(w[2], w[3]), bm(w[0], w[1]))]
+        else:
+            xs = [bm(w[0], w[1]), bm(w[2], w[3])]
         return np.stack(xs).astype(np.complex128).reshape((self.M,) + self.batch_shape + self.spatial)
 
 
