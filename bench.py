@@ -539,6 +539,42 @@ def run_fno(args):
                       "window_cost_by_batch": per_window}), flush=True)
 
 
+def run_twa_breakdown(args):
+    """Per-group timing of the TWA ensemble: each group alone in a graph of 50 steps,
+    resident plane kernel and two-pass path, 500 timed steps (one JSON line)."""
+    import __graft_entry__ as G
+    G.load_package()
+    T = __import__("gpe_gb300.twa", fromlist=["Ensemble"])
+    prm = T.DampedDrivenParams()
+    out = []
+    for N, B in TWA_GROUPS:
+        for res in (True, False):
+            it = T.make_group(N, B, prm, 1000, seed=N, resident=res)
+            ens = T.Ensemble([it])
+            ens.run(50, 50)
+            ens.run(500, 50)
+            ms = ens.last_run_ms()
+            out.append({"grid": [N, N], "trajectories": B, "resident": res, "ms_per_step": ms / 500,
+                        "traj_steps_per_s": B * 500 / (ms * 1e-3), "point_steps_per_s": N * N * B * 500 / (ms * 1e-3)})
+            ens.close()
+            it.close()
+    print(json.dumps({"metric": "TWA per-group step time", "groups": out}), flush=True)
+
+
+def run_twa_group_steps(args):
+    """A handful of plain steps of one TWA group (the capture case for ncu)."""
+    import __graft_entry__ as G
+    G.load_package()
+    T = __import__("gpe_gb300.twa", fromlist=["Ensemble"])
+    prm = T.DampedDrivenParams()
+    N = args.twa_group
+    B = dict(TWA_GROUPS)[N]
+    it = T.make_group(N, B, prm, 100, seed=N, resident=False)
+    it.step(args.steps)
+    print(json.dumps({"grid": [N, N], "trajectories": B, "steps": int(it.state().steps)}), flush=True)
+    it.close()
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -553,6 +589,9 @@ def main():
     ap.add_argument("--twa-steps", type=int, default=2000,
                     help="steps of the batched truncated-Wigner ensemble measurement (0 skips it)")
     ap.add_argument("--no-tune", action="store_true", help="skip the ensemble autotuner")
+    ap.add_argument("--twa-breakdown", action="store_true", help="print per-group TWA step times instead")
+    ap.add_argument("--twa-group", type=int, default=0,
+                    help="run --steps plain steps of the TWA group on this grid (an ncu capture case)")
     ap.add_argument("--anchor-steps", type=int, default=200,
                     help="steps of the scalar Kerr 1024^2 FP64 measurement (0 skips it)")
     ap.add_argument("--precision-sweep", action="store_true",
@@ -575,6 +614,14 @@ def main():
     if args.fno:
         if rank == 0:
             run_fno(args)
+        return
+    if args.twa_breakdown:
+        if rank == 0:
+            run_twa_breakdown(args)
+        return
+    if args.twa_group:
+        if rank == 0:
+            run_twa_group_steps(args)
         return
     if args.impl == "reference":
         run_reference(args, rank, world)

@@ -203,16 +203,18 @@ struct RowLayout {
   }
 };
 
-// Column layout: CC lines (columns) interleaved, point n of column c at
-// (n + n/8)*CC + c: one padding row after every 8 rows.  The reads of a stage and the
-// writes of the later stages touch consecutive rows; the first stage writes rows 8t + r
-// for neighbouring threads t, which the padding spreads over both halves of the bank
-// space (without it, 8-byte elements hit the same 16 banks four times over).
+// Column layout: CC lines (columns) interleaved, point n of column c at n*CC + c; for
+// 8-byte elements with one padding row after every 8 rows, (n + n/8)*CC + c.  The reads
+// of a stage and the writes of the later stages touch consecutive rows; the first stage
+// writes rows 8t + r for neighbouring threads t, which the padding spreads over both
+// halves of the bank space (without it, 8-byte elements hit the same 16 banks four
+// times over; 16-byte elements fill all 32 banks either way).
 template <typename C, int CC>
 struct ColLayout {
+  static constexpr bool PAD = sizeof(C) == 8;
   C* base;  // already offset by the column index
   template <int NS, int R>
-  __device__ __forceinline__ int addr(int idx) const { return (idx + (idx >> 3)) * CC; }
+  __device__ __forceinline__ int addr(int idx) const { return (PAD ? idx + (idx >> 3) : idx) * CC; }
 };
 
 // One Stockham stage.  x: this thread's E points; t: thread index in the line.

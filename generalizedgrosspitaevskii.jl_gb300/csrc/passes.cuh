@@ -47,7 +47,7 @@ struct LineCfg {
   static constexpr int SMEM_LIMIT = 200 * 1024;
   // FP32 lines of two components transform jointly (each component its own exchange)
   static constexpr bool JOINT = sizeof(C) == 8 && M == 2;
-  static constexpr int NPAD = N + N / 8;  // rows of a column-pass exchange (ColLayout padding)
+  static constexpr int NPAD = sizeof(C) == 8 ? N + N / 8 : N;  // rows of a column exchange (ColLayout)
   static constexpr int CC = cmax(1, cmin(cmin(CCMAX, cmax(1, TPB / T)),
                                          pow2floor(SMEM_LIMIT / (NPAD * (int)sizeof(C) * (JOINT ? M : 1)))));
   static constexpr int ROW_THREADS = L * TR;
