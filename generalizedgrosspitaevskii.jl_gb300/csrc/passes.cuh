@@ -43,7 +43,10 @@ struct LineCfg {
   static constexpr int ROWT = 256;
   static constexpr int L = TR >= ROWT ? 1 : ROWT / TR;  // lines per row-pass block
   static constexpr int CCMAX = 128 / (int)sizeof(C);  // columns per tile: one 128-byte row
-  static constexpr int TPB = (M == 2) ? 512 : 1024;
+#ifndef GPE_COL_TPB_M2
+#define GPE_COL_TPB_M2 512
+#endif
+  static constexpr int TPB = (M == 2) ? GPE_COL_TPB_M2 : 1024;
   static constexpr int SMEM_LIMIT = 200 * 1024;
   // FP32 lines of two components transform jointly (each component its own exchange)
   static constexpr bool JOINT = sizeof(C) == 8 && M == 2;
@@ -59,9 +62,12 @@ struct LineCfg {
 #endif
   // blocks of more than 256 threads (lines of 4096 points) keep 128 registers a thread
   static constexpr int ROW_MINB = L * TR > 256 ? 1 : (sizeof(C) == 8 ? GPE_ROW_MIN_BLOCKS_F32 : GPE_ROW_MIN_BLOCKS);
-  static constexpr int COL_MINB_WANT = sizeof(C) == 8 ? 2 : 1;
+#ifndef GPE_COL_MINB_F32
+#define GPE_COL_MINB_F32 2
+#endif
+  static constexpr int COL_MINB_WANT = sizeof(C) == 8 ? GPE_COL_MINB_F32 : 1;
   static constexpr int COL_THREADS = CC * T;
-  static constexpr int COL_MINB = COL_THREADS <= 512 ? COL_MINB_WANT : 1;
+  static constexpr int COL_MINB = COL_THREADS * COL_MINB_WANT <= 2048 ? COL_MINB_WANT : 1;
   static constexpr size_t ROW_SMEM = (size_t)L * N * sizeof(C);
   static constexpr size_t ROW_KERNEL_SMEM = JOINT ? (size_t)M * L * N * sizeof(C) : ROW_SMEM;
   static constexpr size_t COL_SMEM = (size_t)(JOINT ? M : 1) * CC * NPAD * sizeof(C);
