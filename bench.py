@@ -410,14 +410,15 @@ def run_twa(pkg, steps: int, tune: bool):
     choices = {}
     its = []
     for N, B in TWA_GROUPS:
-        resident = True
+        resident, variant = True, 0
         if tune:
             k = A.key(N, 1, "c64", B, A.gpu_name())
-            resident, chunk_n, _ = A.tune(lambda r, N=N, B=B: T.make_group(N, B, prm, 400, seed=N, resident=r), k,
-                                          trial_steps=200)
-            choices[f"{N}x{N}"] = {"resident": resident, "steps_per_graph": chunk_n}
+            resident, variant, chunk_n, _ = A.tune(
+                lambda r, v, N=N, B=B: T.make_group(N, B, prm, 400, seed=N, resident=r, variant=v), k,
+                trial_steps=200, variants=(0, 1))
+            choices[f"{N}x{N}"] = {"resident": resident, "variant": variant, "steps_per_graph": chunk_n}
             tuned_chunks.append(chunk_n)
-        its.append(T.make_group(N, B, prm, steps + 400, seed=N, resident=resident))
+        its.append(T.make_group(N, B, prm, steps + 400, seed=N, resident=resident, variant=variant))
     if tuned_chunks and steps % min(tuned_chunks) == 0:
         chunk = min(tuned_chunks)  # one graph serves every group: the shortest tuned chunk
     ens = T.Ensemble(its)
@@ -541,20 +542,21 @@ def run_fno(args):
 
 def run_twa_breakdown(args):
     """Per-group timing of the TWA ensemble: each group alone in a graph of 50 steps,
-    resident plane kernel and two-pass path, 500 timed steps (one JSON line)."""
+    resident plane kernel and the two-pass path in both line tilings, 500 timed steps
+    (one JSON line)."""
     import __graft_entry__ as G
     G.load_package()
     T = __import__("gpe_gb300.twa", fromlist=["Ensemble"])
     prm = T.DampedDrivenParams()
     out = []
     for N, B in TWA_GROUPS:
-        for res in (True, False):
-            it = T.make_group(N, B, prm, 1000, seed=N, resident=res)
+        for res, var in ((True, 0), (False, 0), (False, 1)):
+            it = T.make_group(N, B, prm, 1000, seed=N, resident=res, variant=var)
             ens = T.Ensemble([it])
             ens.run(50, 50)
             ens.run(500, 50)
             ms = ens.last_run_ms()
-            out.append({"grid": [N, N], "trajectories": B, "resident": res, "ms_per_step": ms / 500,
+            out.append({"grid": [N, N], "trajectories": B, "resident": res, "variant": var, "ms_per_step": ms / 500,
                         "traj_steps_per_s": B * 500 / (ms * 1e-3), "point_steps_per_s": N * N * B * 500 / (ms * 1e-3)})
             ens.close()
             it.close()

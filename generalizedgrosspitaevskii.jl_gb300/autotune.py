@@ -5,6 +5,9 @@ configurations on the actual problem for a few chunks of steps and keeps the fas
 
 * path: the resident plane kernel (whole trajectory in shared memory, when the grid fits)
   or the two-pass HBM path;
+* line tiling of the two-pass path (``gpe_set_variant``): for FP32 one-component fields
+  16 points a thread along x and 8 along y (variant 0) or 8 and 16 (variant 1), i.e. the
+  radix of the register stages and the tile shape of each pass;
 * steps_per_graph: the chunk length captured in the CUDA graph (launch amortisation vs
   graph size).
 
@@ -57,22 +60,24 @@ def key(N: int, M: int, dtype: str, ntraj: int, gpu: str) -> str:
     return f"{gpu}|N{N}|M{M}|{dtype}|B{ntraj}"
 
 
-def tune(make_iterator: Callable[[bool], object], k: str, chunks: Iterable[int] = CANDIDATE_CHUNKS,
-         trial_steps: int = 200, force: bool = False) -> Tuple[bool, int, dict]:
-    """Pick (resident, steps_per_graph) for one group.  make_iterator(resident) builds a
-    fresh iterator for the group.  Returns (resident, steps_per_graph, timings)."""
+def tune(make_iterator: Callable[[bool, int], object], k: str, chunks: Iterable[int] = CANDIDATE_CHUNKS,
+         trial_steps: int = 200, force: bool = False, variants: Iterable[int] = (0,)) -> Tuple[bool, int, int, dict]:
+    """Pick (resident, variant, steps_per_graph) for one group.  make_iterator(resident,
+    variant) builds a fresh iterator for the group; ``variants`` are the line tilings to
+    try on the two-pass path.  Returns (resident, variant, steps_per_graph, timings)."""
     db = _load()
-    if not force and k in db:
+    if not force and k in db and "variant" in db[k]:
         r = db[k]
-        return bool(r["resident"]), int(r["steps_per_graph"]), r.get("timings", {})
+        return bool(r["resident"]), int(r["variant"]), int(r["steps_per_graph"]), r.get("timings", {})
     from .twa import Ensemble
     timings = {}
     best = None
-    for resident in (True, False):
+    candidates = [(True, 0)] + [(False, v) for v in variants]
+    for resident, variant in candidates:
         for chunk in chunks:
             if trial_steps % chunk:
                 continue
-            it = make_iterator(resident)
+            it = make_iterator(resident, variant)
             ens = Ensemble([it])
             try:
                 ens.run(chunk, chunk)  # capture + warm-up
@@ -81,9 +86,9 @@ def tune(make_iterator: Callable[[bool], object], k: str, chunks: Iterable[int] 
             finally:
                 ens.close()
                 it.close()
-            timings[f"resident={resident},chunk={chunk}"] = ms
+            timings[f"resident={resident},variant={variant},chunk={chunk}"] = ms
             if best is None or ms < best[0]:
-                best = (ms, resident, chunk)
-    db[k] = {"resident": best[1], "steps_per_graph": best[2], "timings": timings}
+                best = (ms, resident, variant, chunk)
+    db[k] = {"resident": best[1], "variant": best[2], "steps_per_graph": best[3], "timings": timings}
     _store(db)
-    return best[1], best[2], timings
+    return best[1], best[2], best[3], timings

@@ -25,8 +25,8 @@
 using cd = std::complex<double>;
 
 namespace gpe {
-template <typename Real, int M> int launch_row_t(int, const PassArgs&, int64_t, cudaStream_t);
-template <typename Real, int M> int launch_col_t(int, const PassArgs&, cudaStream_t);
+template <typename Real, int M, int V> int launch_row_t(int, const PassArgs&, int64_t, cudaStream_t);
+template <typename Real, int M, int V> int launch_col_t(int, const PassArgs&, cudaStream_t);
 template <typename Real, int M> int launch_line1d_t(int, const PassArgs&, cudaStream_t);
 template <typename Real, int M> int launch_nl_only_t(const PassArgs&, cudaStream_t);
 template <typename Real, int M> int launch_plane_t(int, const PassArgs&, cudaStream_t);
@@ -40,8 +40,19 @@ template <typename Real> int launch_mat_t(const PassArgs&, cudaStream_t);
   if (dtype == PREC_DW) return M == 1 ? FN<DWR, 1>(__VA_ARGS__) : FN<DWR, 2>(__VA_ARGS__);        \
   return M == 1 ? FN<float, 1>(__VA_ARGS__) : FN<float, 2>(__VA_ARGS__);
 
-int launch_row(int dtype, int M, int logn, const PassArgs& a, int64_t nl, cudaStream_t s) { GPE_DISPATCH(launch_row_t, logn, a, nl, s) }
-int launch_col(int dtype, int M, int logn, const PassArgs& a, cudaStream_t s) { GPE_DISPATCH(launch_col_t, logn, a, s) }
+// variant 1 (alternative line tiling) exists for FP32 one-component fields only
+int launch_row(int dtype, int M, int logn, const PassArgs& a, int64_t nl, cudaStream_t s, int variant) {
+  if (variant == 1 && dtype == PREC_F32 && M == 1) return launch_row_t<float, 1, 1>(logn, a, nl, s);
+  if (dtype == PREC_F64) return M == 1 ? launch_row_t<double, 1, 0>(logn, a, nl, s) : launch_row_t<double, 2, 0>(logn, a, nl, s);
+  if (dtype == PREC_DW) return M == 1 ? launch_row_t<DWR, 1, 0>(logn, a, nl, s) : launch_row_t<DWR, 2, 0>(logn, a, nl, s);
+  return M == 1 ? launch_row_t<float, 1, 0>(logn, a, nl, s) : launch_row_t<float, 2, 0>(logn, a, nl, s);
+}
+int launch_col(int dtype, int M, int logn, const PassArgs& a, cudaStream_t s, int variant) {
+  if (variant == 1 && dtype == PREC_F32 && M == 1) return launch_col_t<float, 1, 1>(logn, a, s);
+  if (dtype == PREC_F64) return M == 1 ? launch_col_t<double, 1, 0>(logn, a, s) : launch_col_t<double, 2, 0>(logn, a, s);
+  if (dtype == PREC_DW) return M == 1 ? launch_col_t<DWR, 1, 0>(logn, a, s) : launch_col_t<DWR, 2, 0>(logn, a, s);
+  return M == 1 ? launch_col_t<float, 1, 0>(logn, a, s) : launch_col_t<float, 2, 0>(logn, a, s);
+}
 int launch_line1d(int dtype, int M, int logn, const PassArgs& a, cudaStream_t s) { GPE_DISPATCH(launch_line1d_t, logn, a, s) }
 int launch_nl_only(int dtype, int M, const PassArgs& a, cudaStream_t s) { GPE_DISPATCH(launch_nl_only_t, a, s) }
 int launch_norm(int dtype, int M, const PassArgs& a, double* out, cudaStream_t s) { GPE_DISPATCH(launch_norm_t, a, out, s) }
@@ -90,6 +101,7 @@ struct gpe_handle {
   double g[2][2][2] = {};
   double c[2][2] = {};
   int nl_on[2] = {0, 0};
+  int variant = 0;  // line tiling of the two-pass passes (gpe_set_variant)
   int nl_matrix = 0;
   double* nlm = nullptr;  // device copy of the matrix nonlinearity coefficients
   double t = 0.0;
@@ -987,7 +999,7 @@ static int enqueue_steps(gpe_handle* h, int64_t nsteps, int64_t save_every, void
   r.hB = -1;
   {
     TimedLaunch tl(h, 0);
-    LK(h, gpe::launch_row(h->prec, h->M, h->logn[0], r, nrows, h->stream));
+    LK(h, gpe::launch_row(h->prec, h->M, h->logn[0], r, nrows, h->stream, h->variant));
   }
   ++nl;
   std::vector<std::pair<PassArgs, int>> cols;  // (args, log2 line length)
@@ -1022,7 +1034,7 @@ static int enqueue_steps(gpe_handle* h, int64_t nsteps, int64_t save_every, void
   for (int64_t s = 0; s < nsteps; ++s) {
     for (auto& cp : cols) {
       TimedLaunch tl(h, 1);
-      LK(h, gpe::launch_col(h->prec, h->M, cp.second, cp.first, h->stream));
+      LK(h, gpe::launch_col(h->prec, h->M, cp.second, cp.first, h->stream, h->variant));
       ++nl;
     }
     const bool last = (s == nsteps - 1);
@@ -1043,7 +1055,7 @@ static int enqueue_steps(gpe_handle* h, int64_t nsteps, int64_t save_every, void
     }
     {
       TimedLaunch tl(h, 0);
-      LK(h, gpe::launch_row(h->prec, h->M, h->logn[0], rr, nrows, h->stream));
+      LK(h, gpe::launch_row(h->prec, h->M, h->logn[0], rr, nrows, h->stream, h->variant));
     }
     if (saving && ring) {
       const int rc = ring->after(si);
@@ -1319,6 +1331,21 @@ int gpe_energy(gpe_handle* h, double* out) {
   out[0] = tmp[0] * h->dV / (double)h->P;
   out[1] = tmp[1] * h->dV;
   out[2] = tmp[2] * h->dV;
+  return GPE_OK;
+}
+
+int gpe_set_variant(gpe_handle* h, int variant) {
+  if (!h) return GPE_ERR_INVALID;
+  if (variant < 0 || variant > 1) return fail(h, GPE_ERR_INVALID, "variant %d: expected 0 or 1", variant);
+  if (variant == 1 && !(h->prec == gpe::PREC_F32 && h->M == 1))
+    return fail(h, GPE_ERR_UNSUPPORTED, "variant 1 exists for FP32 one-component fields only");
+  if (variant != h->variant) {
+    h->variant = variant;
+    if (h->gexec) {  // a captured chunk holds the old kernels
+      cudaGraphExecDestroy(h->gexec);
+      h->gexec = nullptr;
+    }
+  }
   return GPE_OK;
 }
 

@@ -76,8 +76,9 @@ struct PassArgs {
 enum PassPrec { PREC_F64 = 0, PREC_F32 = 1, PREC_DW = 2 };
 
 // Launchers: return 0 or a cudaError_t value.  logn = log2 of the line length.
-int launch_row(int dtype, int M, int logn, const PassArgs& a, int64_t nlines, cudaStream_t s);
-int launch_col(int dtype, int M, int logn, const PassArgs& a, cudaStream_t s);
+// variant: line tiling (0 default; 1 = the alternative FP32 one-component tiling)
+int launch_row(int dtype, int M, int logn, const PassArgs& a, int64_t nlines, cudaStream_t s, int variant = 0);
+int launch_col(int dtype, int M, int logn, const PassArgs& a, cudaStream_t s, int variant = 0);
 int launch_line1d(int dtype, int M, int logn, const PassArgs& a, cudaStream_t s);
 int launch_nl_only(int dtype, int M, const PassArgs& a, cudaStream_t s);
 // pointwise pass of the 2x2 matrix nonlinearity family (M = 2, a.nlm set)

@@ -23,21 +23,25 @@ __host__ __device__ constexpr int cmin(int a, int b) { return a < b ? a : b; }
 __host__ __device__ constexpr int cmax(int a, int b) { return a > b ? a : b; }
 __host__ __device__ constexpr int pow2floor(int v) { return v <= 1 ? 1 : 2 * pow2floor(v / 2); }
 
-// Tiling of a line of 2^LOGN points for precision Real and M components.
-template <typename Real, int M, int LOGN>
+// Tiling of a line of 2^LOGN points for precision Real and M components.  V selects an
+// alternative tiling where one exists (FP32, one component: V=1 holds 8 points a thread
+// in the row pass and 16 in the column pass instead of 16 and 8); the ensemble
+// autotuner picks V per grid size.
+template <typename Real, int M, int LOGN, int V = 0>
 struct LineCfg {
   using C = typename CT<Real>::T;
   static constexpr int N = 1 << LOGN;
   // points per thread: column pass (E) and row pass (ER, which also carries the
   // pointwise half steps and so keeps fewer points live).  FP32 column passes use 8 so
   // two CTAs share an SM and one's loads overlap the other's FFTs.
-  static constexpr int EMAX = (sizeof(C) == 16 && M == 2) || sizeof(C) == 8 ? 8 : 16;
+  static constexpr bool ALT = V == 1 && sizeof(C) == 8 && M == 1;
+  static constexpr int EMAX = ALT ? 16 : ((sizeof(C) == 16 && M == 2) || sizeof(C) == 8 ? 8 : 16);
   static constexpr int E = cmin(EMAX, N / 2);
   static constexpr int T = N / E;  // threads per line, column pass
 #ifndef GPE_ER_F32
 #define GPE_ER_F32 8
 #endif
-  static constexpr int ERMAX = (M == 2) ? (sizeof(C) == 8 ? GPE_ER_F32 : 8) : 16;
+  static constexpr int ERMAX = ALT ? 8 : ((M == 2) ? (sizeof(C) == 8 ? GPE_ER_F32 : 8) : 16);
   static constexpr int ER = cmin(ERMAX, N / 2);
   static constexpr int TR = N / ER;  // threads per line, row pass
   static constexpr int ROWT = 256;
@@ -629,10 +633,10 @@ __device__ __forceinline__ void half_points(typename CT<Real>::T (&x)[M][E], con
 }
 
 // ------------------------------------------------------------------ row pass
-template <typename Real, int LOGN, int M>
-__global__ void __launch_bounds__(LineCfg<Real, M, LOGN>::ROW_THREADS, LineCfg<Real, M, LOGN>::ROW_MINB)
+template <typename Real, int LOGN, int M, int V = 0>
+__global__ void __launch_bounds__(LineCfg<Real, M, LOGN, V>::ROW_THREADS, LineCfg<Real, M, LOGN, V>::ROW_MINB)
 row_kernel(const PassArgs a, const int64_t nlines) {
-  using Cfg = LineCfg<Real, M, LOGN>;
+  using Cfg = LineCfg<Real, M, LOGN, V>;
   using C = typename CT<Real>::T;
   constexpr int N = Cfg::N, E = Cfg::ER, T = Cfg::TR, L = Cfg::L;
   extern __shared__ __align__(16) unsigned char smraw[];
@@ -682,10 +686,10 @@ row_kernel(const PassArgs a, const int64_t nlines) {
 }
 
 // ------------------------------------------------------------------ column pass
-template <typename Real, int LOGN, int M>
-__global__ void __launch_bounds__(LineCfg<Real, M, LOGN>::COL_THREADS, LineCfg<Real, M, LOGN>::COL_MINB)
+template <typename Real, int LOGN, int M, int V = 0>
+__global__ void __launch_bounds__(LineCfg<Real, M, LOGN, V>::COL_THREADS, LineCfg<Real, M, LOGN, V>::COL_MINB)
 col_kernel(const PassArgs a) {
-  using Cfg = LineCfg<Real, M, LOGN>;
+  using Cfg = LineCfg<Real, M, LOGN, V>;
   using C = typename CT<Real>::T;
   constexpr int N = Cfg::N, E = Cfg::E, T = Cfg::T, CC = Cfg::CC;
   extern __shared__ __align__(16) unsigned char smraw[];
@@ -1095,21 +1099,21 @@ static inline int set_smem(K k, size_t bytes) {
   return 0;
 }
 
-template <typename Real, int M, int LOGN>
+template <typename Real, int M, int LOGN, int V = 0>
 int launch_row_n(const PassArgs& a, int64_t nlines, cudaStream_t s) {
-  using Cfg = LineCfg<Real, M, LOGN>;
-  auto k = row_kernel<Real, LOGN, M>;
+  using Cfg = LineCfg<Real, M, LOGN, V>;
+  auto k = row_kernel<Real, LOGN, M, V>;
   int e = set_smem(k, Cfg::ROW_KERNEL_SMEM);
   if (e) return e;
   const int64_t blocks = (nlines + Cfg::L - 1) / Cfg::L;
   k<<<(unsigned)blocks, Cfg::ROW_THREADS, Cfg::ROW_KERNEL_SMEM, s>>>(a, nlines);
   return (int)cudaGetLastError();
 }
-template <typename Real, int M, int LOGN>
+template <typename Real, int M, int LOGN, int V = 0>
 int launch_col_n(const PassArgs& a, cudaStream_t s) {
-  using Cfg = LineCfg<Real, M, LOGN>;
+  using Cfg = LineCfg<Real, M, LOGN, V>;
   if (a.n0 % Cfg::CC) return (int)cudaErrorInvalidValue;
-  auto k = col_kernel<Real, LOGN, M>;
+  auto k = col_kernel<Real, LOGN, M, V>;
   int e = set_smem(k, Cfg::COL_SMEM);
   if (e) return e;
   const int64_t blocks = (int64_t)(a.n0 / Cfg::CC) * a.nouter * a.B;
@@ -1141,13 +1145,27 @@ int launch_line1d_n(const PassArgs& a, cudaStream_t s) {
     default: return (int)cudaErrorInvalidValue;   \
   }
 
-template <typename Real, int M>
+#define GPE_LOGN_SWITCH_V(FN, ...)                  \
+  switch (logn) {                                   \
+    case 4: return FN<Real, M, 4, V>(__VA_ARGS__);    \
+    case 5: return FN<Real, M, 5, V>(__VA_ARGS__);    \
+    case 6: return FN<Real, M, 6, V>(__VA_ARGS__);    \
+    case 7: return FN<Real, M, 7, V>(__VA_ARGS__);    \
+    case 8: return FN<Real, M, 8, V>(__VA_ARGS__);    \
+    case 9: return FN<Real, M, 9, V>(__VA_ARGS__);    \
+    case 10: return FN<Real, M, 10, V>(__VA_ARGS__);  \
+    case 11: return FN<Real, M, 11, V>(__VA_ARGS__);  \
+    case 12: return FN<Real, M, 12, V>(__VA_ARGS__);  \
+    default: return (int)cudaErrorInvalidValue;     \
+  }
+
+template <typename Real, int M, int V = 0>
 int launch_row_t(int logn, const PassArgs& a, int64_t nlines, cudaStream_t s) {
-  GPE_LOGN_SWITCH(launch_row_n, a, nlines, s)
+  GPE_LOGN_SWITCH_V(launch_row_n, a, nlines, s)
 }
-template <typename Real, int M>
+template <typename Real, int M, int V = 0>
 int launch_col_t(int logn, const PassArgs& a, cudaStream_t s) {
-  GPE_LOGN_SWITCH(launch_col_n, a, s)
+  GPE_LOGN_SWITCH_V(launch_col_n, a, s)
 }
 template <typename Real, int M>
 int launch_line1d_t(int logn, const PassArgs& a, cudaStream_t s) {
@@ -1200,9 +1218,13 @@ int launch_norm_t(const PassArgs& a, double* out, cudaStream_t s) {
 }
 
 #define GPE_INSTANTIATE_ROW(REAL, MM) \
-  template int launch_row_t<REAL, MM>(int, const PassArgs&, int64_t, cudaStream_t);
+  template int launch_row_t<REAL, MM, 0>(int, const PassArgs&, int64_t, cudaStream_t);
 #define GPE_INSTANTIATE_COL(REAL, MM) \
-  template int launch_col_t<REAL, MM>(int, const PassArgs&, cudaStream_t);
+  template int launch_col_t<REAL, MM, 0>(int, const PassArgs&, cudaStream_t);
+#define GPE_INSTANTIATE_ROW_V(REAL, MM, VV) \
+  template int launch_row_t<REAL, MM, VV>(int, const PassArgs&, int64_t, cudaStream_t);
+#define GPE_INSTANTIATE_COL_V(REAL, MM, VV) \
+  template int launch_col_t<REAL, MM, VV>(int, const PassArgs&, cudaStream_t);
 #define GPE_INSTANTIATE_PLANE(REAL, MM)                                      \
   template int launch_plane_t<REAL, MM>(int, const PassArgs&, cudaStream_t);  \
   template bool plane_fits_t<REAL, MM>(int);

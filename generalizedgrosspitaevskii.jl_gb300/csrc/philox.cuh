@@ -57,13 +57,19 @@ __device__ __forceinline__ double2 box_muller_f64(uint32_t w0, uint32_t w1) {
   return make_double2(mag * c, mag * s);
 }
 // FP32 variant on the top 24 bits of each word: u1 = (w0>>8 + 1/2) 2^-24.
+// FP32 fields (the truncated-Wigner bulk): the same transform with the hardware
+// approximations of log and sin/cos (absolute error near 2^-21), a few instructions
+// instead of the accurate routines' range reduction.  The angle is taken in [-pi, pi),
+// where the approximation holds: (cos, sin)(2 pi u2) = -(cos, sin)(pi (2 u2 - 1)).  The
+// draws are Gaussian to that accuracy; they are not meant to repeat the FP64 variant
+// bit for bit.
 __device__ __forceinline__ float2 box_muller_f32(uint32_t w0, uint32_t w1) {
   const float u1 = ((float)(w0 >> 8) + 0.5f) * 5.9604644775390625e-8f;
   const float u2 = (float)(w1 >> 8) * 5.9604644775390625e-8f;
-  const float mag = sqrtf(-logf(u1));
+  const float mag = sqrtf(fmaxf(-__logf(u1), 0.0f));  // the approximation may cross 0 near u1 = 1
   float s, c;
-  sincospif(2.0f * u2, &s, &c);
-  return make_float2(mag * c, mag * s);
+  __sincosf(3.14159265358979f * (2.0f * u2 - 1.0f), &s, &c);
+  return make_float2(-mag * c, -mag * s);
 }
 
 template <typename Real> struct BoxMuller;

@@ -89,10 +89,10 @@ class Ensemble:
 
 
 def make_group(N: int, ntraj: int, prm: DampedDrivenParams, nsteps: int, seed: int, dtype=np.complex64,
-               resident: bool = True, noise_seed: Optional[int] = None) -> StrangSplittingIterator:
+               resident: bool = True, noise_seed: Optional[int] = None, variant: int = 0) -> StrangSplittingIterator:
     prob = wigner_problem(N, ntraj, prm, seed, dtype)
     return StrangSplittingIterator(prob, (0.0, nsteps * prm.dt), dt=prm.dt, nsaves=1, rng=noise_seed or seed + 1,
-                                   resident=resident)
+                                   resident=resident, variant=variant)
 
 
 def density_moments(it: StrangSplittingIterator):

@@ -492,7 +492,9 @@ def box_muller_f64(w0, w1):
 
 
 def box_muller_f32(w0, w1):
-    """FP32 variant on the top 24 bits of each word."""
+    """FP32 variant on the top 24 bits of each word, evaluated exactly; the GPU's FP32
+    path uses hardware log / sin / cos approximations (absolute error near 2^-21), so it
+    matches this to that accuracy, not bit for bit."""
     u1 = ((w0 >> np.uint64(8)).astype(np.float32) + np.float32(0.5)) * np.float32(2.0 ** -24)
     u2 = (w1 >> np.uint64(8)).astype(np.float32) * np.float32(2.0 ** -24)
     mag = np.sqrt(-np.log(u1.astype(np.float64)))

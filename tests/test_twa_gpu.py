@@ -132,3 +132,40 @@ def test_momentum_statistics_match_numpy(gpe, lib):
     assert np.allclose(nk, n_ref, rtol=1e-10, atol=1e-14)
     assert np.allclose(G2, G2_ref, rtol=1e-9, atol=1e-13 * np.abs(G2_ref).max())
     assert np.allclose(g2, G2_ref / np.outer(n_ref, n_ref), rtol=1e-8)
+
+
+def test_alternative_tiling_matches_oracle(gpe, oracle, lib):
+    """The second line tiling of FP32 one-component fields (gpe_set_variant 1) against the
+    FP64 oracle on replayed noise (two-pass path, so both passes run the tiling)."""
+    T = twa(gpe)
+    prm = T.DampedDrivenParams()
+    N, B, nsteps = 64, 3, 30
+    prob = T.wigner_problem(N, B, prm, seed=4, dtype=np.complex64)
+    rn = oracle.ReplayNoise(23, (1, B, N, N))
+    xi32 = lambda h: rn(h).astype(np.complex64).astype(np.complex128)
+    it = gpe.init(prob, gpe.StrangSplitting(), (0.0, nsteps * prm.dt), dt=prm.dt, nsaves=1,
+                  noise_replay=lambda h: np.ascontiguousarray(xi32(h)), resident=False, variant=1)
+    ts, res = it.solve()
+    it.close()
+    dV = (prm.L / N) ** 2
+    u0c = c_order(prob.u0[0]).astype(np.complex128)
+    orc = oracle.OracleProblem(u0=(u0c,), lengths=(prm.L, prm.L),
+                               dispersion=lambda k, p: (k[0] ** 2 + k[1] ** 2) / 2 - 0.5j * prm.gamma,
+                               nonlin_g=np.array([[prm.g]]), pump_profile=np.ones((1, N, N), np.complex128),
+                               pump_amp=lambda t: np.array([prm.F]), eta=np.array([math.sqrt(prm.gamma / (2 * dV))]))
+    ots, ores = oracle.solve(orc, (0.0, nsteps * prm.dt), prm.dt, 1, xi_source=xi32)
+    got = c_order(res[0]).astype(np.complex128)
+    assert oracle.rel_l2(got, ores[0]) <= 1e-5
+
+
+def test_variant_needs_fp32_one_component(gpe, lib):
+    """The alternative tiling exists for FP32 one-component fields only; other handles
+    refuse it with GPE_ERR_UNSUPPORTED and keep working."""
+    T = twa(gpe)
+    prm = T.DampedDrivenParams()
+    it = T.make_group(32, 2, prm, 10, seed=1, dtype=np.complex128)
+    assert lib.gpe_set_variant(it.h, 1) == -2
+    assert lib.gpe_set_variant(it.h, 2) == -1
+    assert lib.gpe_set_variant(it.h, 0) == 0
+    it.step(2)
+    it.close()
