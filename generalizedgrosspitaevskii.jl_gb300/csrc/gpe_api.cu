@@ -694,6 +694,10 @@ static PassArgs base_args(gpe_handle* h) {
   a.vtab = h->vtab;
   a.vkind = h->vkind;
   float hl[2];
+  a.dens_mask = 0;
+  for (int j = 0; j < h->M; ++j)
+    for (int l = 0; l < h->M; ++l)
+      if (h->nl_on[j] && (h->g[j][l][0] != 0.0 || h->g[j][l][1] != 0.0)) a.dens_mask |= 1 << l;
   for (int j = 0; j < 2; ++j) {
     a.nl_on[j] = h->nl_on[j];
     a.nl_imag[j] = h->c[j][1] != 0.0;

@@ -33,6 +33,7 @@ struct PassArgs {
   // roundings (gf, cf) and the FP32 remainders (gl, cl) that make (gf + gl) the
   // double-word form, so no pass converts per point.
   int32_t nl_on[2], nl_imag[2];
+  int32_t dens_mask;  // bit l: some active G_j depends on |u_l|^2
   double g[2][2][2];
   double c[2][2];
   float gf[2][2][2], gl[2][2][2];
