@@ -131,3 +131,48 @@ def test_philox_noise_statistics():
     # independent streams per half step and per component
     assert np.abs(np.mean(xi[0] * np.conj(xi[1]))) < 0.02
     assert not np.allclose(O.PhiloxNoise(42, 1, (), (16,))(0), O.PhiloxNoise(42, 1, (), (16,))(1))
+
+
+def test_autotune_picks_fastest_and_caches(gpe, tmp_path, monkeypatch):
+    """The ensemble autotuner (host logic only: the ensemble is faked) times every
+    (path, tiling, chunk) candidate, keeps the fastest, and answers from its cache next time."""
+    import importlib
+    A = importlib.import_module("gpe_gb300.autotune")
+    T = importlib.import_module("gpe_gb300.twa")
+    monkeypatch.setenv("GPE_AUTOTUNE_CACHE", str(tmp_path / "tune.json"))
+    cost = {(True, 0): 5.0, (False, 0): 3.0, (False, 1): 2.0}
+    made = []
+
+    class FakeIt:
+        def __init__(self, resident, variant):
+            self.cfg = (resident, variant)
+
+        def close(self):
+            pass
+
+    class FakeEnsemble:
+        def __init__(self, its):
+            self.cfg = its[0].cfg
+            self.ms = 0.0
+
+        def run(self, nsteps, chunk):
+            self.ms = cost[self.cfg] * nsteps + 100.0 / chunk
+
+        def last_run_ms(self):
+            return self.ms
+
+        def close(self):
+            pass
+
+    monkeypatch.setattr(T, "Ensemble", FakeEnsemble)
+
+    def make(resident, variant):
+        made.append((resident, variant))
+        return FakeIt(resident, variant)
+
+    res, var, chunk, timings = A.tune(make, "k1", chunks=(10, 50, 200), trial_steps=200, variants=(0, 1))
+    assert (res, var, chunk) == (False, 1, 200)
+    assert len(timings) == 9 and len(made) == 9
+    made.clear()
+    assert A.tune(make, "k1", variants=(0, 1))[:3] == (False, 1, 200)
+    assert not made  # answered from the cache
