@@ -180,6 +180,42 @@ def test_noise_philox_matches_restatement(gpe, oracle, lib, fp64):
     assert_close(oracle, res, ores, 1e-10)
 
 
+@pytest.mark.parametrize("resident", [True, False], ids=["resident", "two-pass"])
+def test_noise_philox_fp32_matches_restatement(gpe, oracle, lib, resident):
+    """FP32 one-component fields draw one Philox block for the points x and x + n0/2 of a
+    row (the row pass shares it between them); the draws equal the oracle's restatement
+    up to the FP32 Box-Muller's hardware approximations (~2^-21), far below what a wrong
+    block or word pair would give."""
+    N, L, B = 64, 16.0, 2
+    u0c = np.ones((B, N, N), np.complex128)
+    disp = lambda k, p: (k[0] ** 2 + k[1] ** 2) / 2 - 0.1j
+    eta = 0.25 - 0.1j
+    gkw = dict(u0=(jl(u0c).astype(np.complex64),), lengths=(L, L), dispersion=disp,
+               position_noise_func=lambda u, r, p: eta)
+    orc = oracle.OracleProblem(u0=(u0c,), lengths=(L, L), dispersion=disp, eta=np.array([eta]))
+    seed = 0xC0FFEE
+    xi = oracle.PhiloxNoise(seed, 1, (B,), (N, N), fp32=True)
+    prob = gpe.GrossPitaevskiiProblem(**gkw)
+    ts, res = gpe.solve(prob, gpe.StrangSplitting(), (0.0, 0.2), dt=0.02, nsaves=2, rng=seed, resident=resident)
+    ots, ores = oracle.solve(orc, (0.0, 0.2), 0.02, 2, xi_source=xi)
+    assert_close(oracle, res, ores, 1e-4)
+
+
+def test_noise_philox_fp32_1d_matches_restatement(gpe, oracle, lib):
+    """The same for a batch of 1D lines (the resident line kernel)."""
+    N, L, B = 256, 32.0, 3
+    u0c = np.ones((B, N), np.complex128)
+    disp = lambda k, p: k[0] ** 2 / 2 - 0.1j
+    gkw = dict(u0=(jl(u0c).astype(np.complex64),), lengths=(L,), dispersion=disp,
+               position_noise_func=lambda u, r, p: 0.3)
+    orc = oracle.OracleProblem(u0=(u0c,), lengths=(L,), dispersion=disp, eta=np.array([0.3]))
+    seed = 99
+    ts, res = gpe.solve(gpe.GrossPitaevskiiProblem(**gkw), gpe.StrangSplitting(), (0.0, 0.2), dt=0.02, nsaves=2,
+                        rng=seed)
+    ots, ores = oracle.solve(orc, (0.0, 0.2), 0.02, 2, xi_source=oracle.PhiloxNoise(seed, 1, (B,), (N,), fp32=True))
+    assert_close(oracle, res, ores, 1e-4)
+
+
 @pytest.mark.parametrize("fp64", FP64_MODES)
 def test_1d_bistability_segment(gpe, oracle, lib, fp64):
     """1D driven-dissipative line (the reference's bistability problem), a short
