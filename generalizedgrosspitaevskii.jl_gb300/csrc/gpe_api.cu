@@ -17,6 +17,7 @@
 #include <cstdio>
 #include <cstring>
 #include <string>
+#include <thread>
 #include <vector>
 
 #include "../../include/gpe.h"
@@ -257,11 +258,32 @@ static int build_cis(gpe_handle* h, const double* f, int kind, double delta, dou
   return kind;
 }
 
-static bool all_finite(const double* v, size_t n) {
+// Finiteness of n host values, split over host threads for large inputs (a field of
+// 64 copies of 512^2 points is 33 M values; one thread would dominate the upload).
+template <typename T> static bool all_finite_range(const T* v, size_t n) {
   for (size_t i = 0; i < n; ++i)
     if (!std::isfinite(v[i])) return false;
   return true;
 }
+template <typename T> static bool all_finite_par(const T* v, size_t n) {
+  const size_t kChunk = size_t(1) << 20;
+  if (n < 4 * kChunk) return all_finite_range(v, n);
+  unsigned nt = std::thread::hardware_concurrency();
+  nt = nt == 0 ? 4 : (nt > 16 ? 16 : nt);
+  std::vector<std::thread> pool;
+  std::vector<char> ok(nt, 1);
+  const size_t per = (n + nt - 1) / nt;
+  for (unsigned k = 0; k < nt; ++k) {
+    const size_t lo = k * per, hi = lo + per < n ? lo + per : n;
+    if (lo >= hi) break;
+    pool.emplace_back([&, k, lo, hi] { ok[k] = all_finite_range(v + lo, hi - lo); });
+  }
+  for (auto& th : pool) th.join();
+  for (char c : ok)
+    if (!c) return false;
+  return true;
+}
+static bool all_finite(const double* v, size_t n) { return all_finite_par(v, n); }
 
 extern "C" {
 
@@ -387,21 +409,20 @@ int gpe_set_field(gpe_handle* h, int comp, const void* host) {
   if (rc) return rc;
   if (!host) return fail(h, GPE_ERR_INVALID, "null field");
   const size_t n = (size_t)h->P * h->B;
-  if (h->dtype == GPE_C128) {
-    if (!all_finite((const double*)host, 2 * n)) return fail(h, GPE_ERR_NONFINITE, "field %d has NaN or Inf", comp);
-  } else {
-    const float* f = (const float*)host;
-    for (size_t i = 0; i < 2 * n; ++i)
-      if (!std::isfinite(f[i])) return fail(h, GPE_ERR_NONFINITE, "field %d has NaN or Inf", comp);
-  }
+  const bool finite = h->dtype == GPE_C128 ? all_finite_par((const double*)host, 2 * n)
+                                           : all_finite_par((const float*)host, 2 * n);
+  if (!finite) return fail(h, GPE_ERR_NONFINITE, "field %d has NaN or Inf", comp);
+  CK(h, cudaSetDevice(h->dev));
   if (h->prec == gpe::PREC_DW) {
-    const double* v = (const double*)host;
-    std::vector<float> tmp(4 * n);
-    for (size_t i = 0; i < 2 * n; ++i) split_dw(v[i], &tmp[2 * i]);
-    CK(h, cudaMemcpy(h->u[comp], tmp.data(), n * 16, cudaMemcpyHostToDevice));
+    // FP64 and double-word complex numbers both take 16 bytes: copy the FP64 values and
+    // split them in place on the device
+    CK(h, cudaMemcpyAsync(h->u[comp], host, n * 16, cudaMemcpyHostToDevice, h->stream));
+    LK(h, gpe::launch_f64_to_dw(h->u[comp], h->u[comp], (int64_t)n, h->stream));
+    CK(h, cudaStreamSynchronize(h->stream));
     return GPE_OK;
   }
-  CK(h, cudaMemcpy(h->u[comp], host, n * h->csz, cudaMemcpyHostToDevice));
+  CK(h, cudaMemcpyAsync(h->u[comp], host, n * h->csz, cudaMemcpyHostToDevice, h->stream));
+  CK(h, cudaStreamSynchronize(h->stream));
   return GPE_OK;
 }
 
