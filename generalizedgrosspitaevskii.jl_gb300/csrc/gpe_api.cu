@@ -20,6 +20,8 @@
 #include <thread>
 #include <vector>
 
+#include <nvtx3/nvToolsExt.h>
+
 #include "../../include/gpe.h"
 #include "kernels.h"
 
@@ -169,6 +171,14 @@ static int fail(gpe_handle* h, int code, const char* fmt, ...) {
   } while (0)
 
 static bool is_pow2(int64_t v) { return v > 0 && (v & (v - 1)) == 0; }
+
+// NVTX range over an API call (visible in Nsight timelines; no cost without a tool)
+struct NvtxRange {
+  explicit NvtxRange(const char* name) { nvtxRangePushA(name); }
+  ~NvtxRange() { nvtxRangePop(); }
+  NvtxRange(const NvtxRange&) = delete;
+  NvtxRange& operator=(const NvtxRange&) = delete;
+};
 static int ilog2i(int64_t v) { int r = 0; while ((1ll << r) < v) ++r; return r; }
 
 // FP64 -> double word: hi = fl32(v), lo = fl32(v - hi)
@@ -405,6 +415,7 @@ static int check_comp(gpe_handle* h, int comp) {
 }
 
 int gpe_set_field(gpe_handle* h, int comp, const void* host) {
+  NvtxRange nv("gpe_set_field");
   int rc = check_comp(h, comp);
   if (rc) return rc;
   if (!host) return fail(h, GPE_ERR_INVALID, "null field");
@@ -1135,6 +1146,7 @@ static int replay_graph(gpe_handle* h, int64_t nsteps, int64_t* launches) {
 static int run_common(gpe_handle* h, int64_t nsteps, int64_t save_every, void* out, bool out_is_dev, double* ts_out,
                       const void* xi_host) {
   if (!h) return GPE_ERR_INVALID;
+  NvtxRange nv("gpe_run");
   CK(h, cudaSetDevice(h->dev));
   if (nsteps < 0) return fail(h, GPE_ERR_INVALID, "nsteps must be >= 0");
   if (save_every < 0) return fail(h, GPE_ERR_INVALID, "save_every must be >= 0");
@@ -1285,6 +1297,7 @@ int gpe_set_state(gpe_handle* h, const gpe_state* st) {
 
 int gpe_norm(gpe_handle* h, double* out) {
   if (!h) return GPE_ERR_INVALID;
+  NvtxRange nv("gpe_norm");
   if (!out) return fail(h, GPE_ERR_INVALID, "null output");
   PassArgs a = base_args(h);
   CK(h, cudaMemsetAsync(h->red, 0, 4 * sizeof(double), h->stream));
@@ -1326,6 +1339,7 @@ static int transform_copy(gpe_handle* h) {
 
 int gpe_energy(gpe_handle* h, double* out) {
   if (!h) return GPE_ERR_INVALID;
+  NvtxRange nv("gpe_energy");
   if (!out) return fail(h, GPE_ERR_INVALID, "null output");
   if (h->nl_matrix) return fail(h, GPE_ERR_UNSUPPORTED, "energy is defined for the diagonal nonlinearity families only");
   CK(h, cudaSetDevice(h->dev));
@@ -1388,6 +1402,7 @@ int gpe_set_graph(gpe_handle* h, int64_t steps_per_graph) {
 // Enqueue without waiting: no saves, no replay.  Host bookkeeping (t, steps) advances now.
 int gpe_run_async(gpe_handle* h, int64_t nsteps) {
   if (!h) return GPE_ERR_INVALID;
+  NvtxRange nv("gpe_run_async");
   CK(h, cudaSetDevice(h->dev));
   if (nsteps < 0) return fail(h, GPE_ERR_INVALID, "nsteps must be >= 0");
   if (h->noise == GPE_NOISE_REPLAY) return fail(h, GPE_ERR_INVALID, "replayed noise needs gpe_run_replay");
@@ -1432,6 +1447,7 @@ int gpe_kernel_times(const gpe_handle* h, double* ms, int64_t* n) {
 }
 
 int gpe_spectral_moments(gpe_handle* h, int comp, double* mean_out, double* second_out) {
+  NvtxRange nv("gpe_spectral_moments");
   int rc = check_comp(h, comp);
   if (rc) return rc;
   if (!mean_out) return fail(h, GPE_ERR_INVALID, "null output");
@@ -1524,6 +1540,7 @@ const char* gpe_ensemble_last_error(const gpe_ensemble* e) { return e ? e->err.c
 // steps_per_graph times.
 int gpe_ensemble_run(gpe_ensemble* e, int64_t nsteps, int64_t steps_per_graph) {
   if (!e) return GPE_ERR_INVALID;
+  NvtxRange nv("gpe_ensemble_run");
   if (nsteps < 0 || steps_per_graph < 1 || nsteps % steps_per_graph)
     return efail(e, GPE_ERR_INVALID, "nsteps must be a non-negative multiple of steps_per_graph >= 1");
   gpe_handle* h0 = e->hs[0];
