@@ -414,11 +414,16 @@ __device__ __forceinline__ void half_step(typename CT<Real>::T (&u)[M], const Pa
     }
   }
   C prof[M];
+  // a component that neither G nor V touches takes both pump terms in one product:
+  // (u + pn F) + px F = u + (pn + px) F
+  bool pm[M];
+#pragma unroll
+  for (int j = 0; j < M; ++j) pm[j] = !hasE[j] && a.vkind != TAB_MATRIX;
 #pragma unroll
   for (int j = 0; j < M; ++j) {
     if (a.pprof[j]) {
       prof[j] = a.pprof_cplx ? ldgc((const C*)a.pprof[j] + p) : Prof<Real>::cplx(a.pprof[j], p);
-      u[j] = cadd(u[j], pump_mul(pn[j], prof[j], a.pprof_cplx));
+      if (!pm[j]) u[j] = cadd(u[j], pump_mul(pn[j], prof[j], a.pprof_cplx));
     }
   }
   if (a.vkind == TAB_MATRIX && M == 2) {
@@ -437,7 +442,7 @@ __device__ __forceinline__ void half_step(typename CT<Real>::T (&u)[M], const Pa
   }
 #pragma unroll
   for (int j = 0; j < M; ++j)
-    if (a.pprof[j]) u[j] = cadd(u[j], pump_mul(px[j], prof[j], a.pprof_cplx));
+    if (a.pprof[j]) u[j] = cadd(u[j], pump_mul(pm[j] ? cadd(pn[j], px[j]) : px[j], prof[j], a.pprof_cplx));
   if (a.noise != NOISE_OFF) {
     C xi[M];
     if (xi_pre) {

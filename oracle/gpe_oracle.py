@@ -28,7 +28,9 @@ Supported closure families (the coefficient form the GPU backend accepts):
   ``(M,)`` vector (diagonal) or an ``(M, M)`` matrix per point; it is sampled on the grid
   in FP64 and exponentiated (``cis(-dt*D)``, ``cis(-dt/2*V)``), see src/misc.jl:12-20.
 * nonlinearity: ``G_j(u) = sum_l g[j, l] |u_l|^2 + c[j]`` (complex ``g``, ``c``), or an
-  arbitrary vectorised callable ``G(fields) -> (M, ...)`` returning the diagonal.
+  arbitrary vectorised callable ``G(fields) -> (M, ...)`` returning the diagonal, or
+  (``nonlin_matrix``) a callable returning a 2x2 matrix per point, whose ``cis`` is a
+  matrix exponential (src/kernels.jl:23-25).
 * pump: ``F_m(r, t) = a_m(t) * p_m(r)`` given as the profile array and an amplitude
   callable, or an arbitrary vectorised callable ``F(t) -> (M, *spatial)``.
 * position noise: ``eta_m`` constants (optionally times a real profile) with complex
