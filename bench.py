@@ -226,6 +226,19 @@ def algorithmic_bytes(dtype, B: int):
     return {"row": row, "col": col}
 
 
+def binding_limit(dtype, fp64: str) -> str:
+    """What bounds the passes of this precision, from the committed ncu captures."""
+    if dtype == np.complex128 and fp64 == "native":
+        return ("FP64 pipe: 82-83 % active in both passes (1.2 TFLOP/s FP64 on GB300); "
+                "profiles/polariton512_dw_row_col_passes.md")
+    if dtype == np.complex128:
+        return ("FP32-pipe instruction issue: double-word arithmetic, 2125 + 1340 instructions per point "
+                "(row + column), 72 % / 67 % of issue slots busy, DRAM 8-13 % of peak; "
+                "profiles/polariton512_dw_row_col_passes.md")
+    return ("instruction issue (row: ALU pipe 43 %, 68 % of issue slots) and global-load latency (column); "
+            "profiles/polariton512_f32_row_col_passes.md")
+
+
 def dram_traffic(dtype: str, fp64: str, kernel: str):
     """DRAM bytes per grid point of one launch of `kernel` ("row" / "col"), read from the
     ncu summary in profiles/dram_traffic.md (rows "| precision | pass | bytes |"), or None."""
@@ -350,7 +363,8 @@ def run_gpu(args, rank, world, local_rank):
                      "kernels": {k: {"launches": int(kn[i]), "total_ms": float(kms[i]),
                                      "mean_ms": float(kms[i] / max(kn[i], 1)),
                                      "achieved_gbs": float(ab[k] * P * B / (kms[i] / max(kn[i], 1) * 1e-3) / 1e9)}
-                                 for i, k in enumerate(["row", "col"])}},
+                                 for i, k in enumerate(["row", "col"])},
+                     "binding_limit": binding_limit(dtype, args.fp64)},
         "clocks": clk.summary(),
     }
     if args.anchor_steps > 0:
