@@ -11,6 +11,7 @@
 //                                                              src/strang_splitting.jl:69-90
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <cmath>
 #include <complex>
 #include <cstdarg>
@@ -118,6 +119,8 @@ struct gpe_handle {
   std::vector<cudaEvent_t> ring_ready, ring_done;
   void* xi_buf = nullptr;
   size_t xi_cap = 0;
+  void* conv_buf = nullptr;  // FP64 staging of double-word fields on their way to the host
+  size_t conv_cap = 0;
   double* red = nullptr;  // reduction scratch (4 doubles)
   double last_ms = 0.0;
   int64_t last_launches = 0;
@@ -398,6 +401,7 @@ int gpe_destroy(gpe_handle* h) {
   for (cudaEvent_t e : h->ring_done) cudaEventDestroy(e);
   if (h->cstream) cudaStreamDestroy(h->cstream);
   cudaFree(h->xi_buf);
+  cudaFree(h->conv_buf);
   cudaFree(h->red);
   for (cudaEvent_t e : h->evpool) cudaEventDestroy(e);
   if (h->ev0) cudaEventDestroy(h->ev0);
@@ -437,17 +441,26 @@ int gpe_set_field(gpe_handle* h, int comp, const void* host) {
   return GPE_OK;
 }
 
+static int ensure(gpe_handle* h, void** buf, size_t* cap, size_t bytes);
+
 int gpe_get_field(gpe_handle* h, int comp, void* host) {
   int rc = check_comp(h, comp);
   if (rc) return rc;
   if (!host) return fail(h, GPE_ERR_INVALID, "null destination");
   const size_t n = (size_t)h->P * h->B;
+  CK(h, cudaSetDevice(h->dev));
   CK(h, cudaStreamSynchronize(h->stream));
   if (h->prec == gpe::PREC_DW) {
-    std::vector<float> tmp(4 * n);
-    CK(h, cudaMemcpy(tmp.data(), h->u[comp], n * 16, cudaMemcpyDeviceToHost));
-    double* v = (double*)host;
-    for (size_t i = 0; i < 2 * n; ++i) v[i] = (double)tmp[2 * i] + (double)tmp[2 * i + 1];
+    // rounded to FP64 on the device through a bounded staging buffer, chunk by chunk
+    const size_t chunk = std::min<size_t>(n, size_t(4) << 20);  // complex numbers (64 MiB)
+    rc = ensure(h, &h->conv_buf, &h->conv_cap, chunk * 16);
+    if (rc) return rc;
+    for (size_t o = 0; o < n; o += chunk) {
+      const size_t c = std::min(chunk, n - o);
+      LK(h, gpe::launch_dw_to_f64((const char*)h->u[comp] + o * 16, h->conv_buf, (int64_t)c, h->stream));
+      CK(h, cudaMemcpyAsync((char*)host + o * 16, h->conv_buf, c * 16, cudaMemcpyDeviceToHost, h->stream));
+    }
+    CK(h, cudaStreamSynchronize(h->stream));
     return GPE_OK;
   }
   CK(h, cudaMemcpy(host, h->u[comp], n * h->csz, cudaMemcpyDeviceToHost));

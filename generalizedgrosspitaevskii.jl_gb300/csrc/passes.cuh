@@ -35,13 +35,19 @@ struct LineCfg {
   // pointwise half steps and so keeps fewer points live).  FP32 column passes use 8 so
   // two CTAs share an SM and one's loads overlap the other's FFTs.
   static constexpr bool ALT = V == 1 && sizeof(C) == 8 && M == 1;
-  static constexpr int EMAX = ALT ? 16 : ((sizeof(C) == 16 && M == 2) || sizeof(C) == 8 ? 8 : 16);
+#ifndef GPE_E_W16_M1
+#define GPE_E_W16_M1 16
+#endif
+#ifndef GPE_ER_W16_M1
+#define GPE_ER_W16_M1 16
+#endif
+  static constexpr int EMAX = ALT ? 16 : ((sizeof(C) == 16 && M == 2) || sizeof(C) == 8 ? 8 : GPE_E_W16_M1);
   static constexpr int E = cmin(EMAX, N / 2);
   static constexpr int T = N / E;  // threads per line, column pass
 #ifndef GPE_ER_F32
 #define GPE_ER_F32 8
 #endif
-  static constexpr int ERMAX = ALT ? 8 : ((M == 2) ? (sizeof(C) == 8 ? GPE_ER_F32 : 8) : 16);
+  static constexpr int ERMAX = ALT ? 8 : ((M == 2) ? (sizeof(C) == 8 ? GPE_ER_F32 : 8) : (sizeof(C) == 16 ? GPE_ER_W16_M1 : 16));
   static constexpr int ER = cmin(ERMAX, N / 2);
   static constexpr int TR = N / ER;  // threads per line, row pass
   static constexpr int ROWT = 256;
