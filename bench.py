@@ -129,6 +129,19 @@ class ClockSampler:
                 "reasons": sorted(reasons), "samples": len(sm)}
 
 
+def cpu_model() -> str:
+    """The host CPU's model name (lscpu), or the architecture when it is not reported."""
+    try:
+        out = subprocess.run(["lscpu"], capture_output=True, text=True, timeout=10).stdout
+        for ln in out.splitlines():
+            if ln.lower().startswith("model name"):
+                return ln.split(":", 1)[1].strip()
+    except (OSError, subprocess.SubprocessError):
+        pass
+    import platform
+    return platform.machine()
+
+
 def cpu_baseline(steps_hint: int = 0):
     """FP64 oracle on the host cores: one trajectory of the workload, scipy FFT with all
     threads, steps chosen for ~10 s of work."""
@@ -149,7 +162,7 @@ def cpu_baseline(steps_hint: int = 0):
             break
     el = time.perf_counter() - t0
     P = N_GRID * N_GRID
-    return {"value": P * n / el, "unit": "grid-point-steps/s", "cores": cores, "kind": "port",
+    return {"value": P * n / el, "unit": "grid-point-steps/s", "cores": cores, "cpu": cpu_model(), "kind": "port",
             "sample": f"{n} Strang steps of one 512^2 two-component trajectory, FP64 numpy/scipy.fft "
                       f"with workers={cores}, {el:.1f} s"}
 
@@ -196,7 +209,7 @@ def run_reference(args, rank, world):
             "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * el / args.steps,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
             "config": config_dict(np.complex128, batch_for(np.complex128), world),
-            "cpu_baseline": {"value": v, "unit": "grid-point-steps/s", "cores": cores, "kind": "port",
+            "cpu_baseline": {"value": v, "unit": "grid-point-steps/s", "cores": cores, "cpu": cpu_model(), "kind": "port",
                              "sample": f"each step = one Strang step of one 512^2 two-component trajectory "
                                        f"(FP64 numpy/scipy.fft, workers={cores}); the Julia reference has no "
                                        f"julia binary on this box, so its algorithm runs as the oracle restatement"},
