@@ -52,7 +52,10 @@ struct LineCfg {
   static constexpr int ERMAX = ALT ? 8 : ((M == 2) ? (sizeof(C) == 8 ? GPE_ER_F32 : 8) : (sizeof(C) == 16 ? GPE_ER_W16_M1 : 16));
   static constexpr int ER = cmin(ERMAX, N / 2);
   static constexpr int TR = N / ER;  // threads per line, row pass
-  static constexpr int ROWT = 256;
+#ifndef GPE_ROWT_W16
+#define GPE_ROWT_W16 256
+#endif
+  static constexpr int ROWT = sizeof(C) == 16 ? GPE_ROWT_W16 : 256;
   static constexpr int L = TR >= ROWT ? 1 : ROWT / TR;  // lines per row-pass block
   static constexpr int CCMAX = 128 / (int)sizeof(C);  // columns per tile: one 128-byte row
 #ifndef GPE_COL_TPB_M2
@@ -77,7 +80,10 @@ struct LineCfg {
 #ifndef GPE_COL_MINB_F32
 #define GPE_COL_MINB_F32 2
 #endif
-  static constexpr int COL_MINB_WANT = sizeof(C) == 8 ? GPE_COL_MINB_F32 : 1;
+#ifndef GPE_COL_MINB_W16
+#define GPE_COL_MINB_W16 1
+#endif
+  static constexpr int COL_MINB_WANT = sizeof(C) == 8 ? GPE_COL_MINB_F32 : GPE_COL_MINB_W16;
   static constexpr int COL_THREADS = CC * T;
   static constexpr int COL_MINB = COL_THREADS * COL_MINB_WANT <= 2048 ? COL_MINB_WANT : 1;
   static constexpr size_t ROW_SMEM = (size_t)L * N * sizeof(C);
