@@ -93,3 +93,16 @@ def test_kerr2048_norm_is_conserved(gpe, lib, dtype, fp64, tol):
     n1 = it.norm()[0]
     it.close()
     assert abs(n1 / n0 - 1) <= tol
+
+
+@pytest.mark.parametrize("fp64", ["dw", "native"])
+def test_polariton_full_length_run(gpe, oracle, lib, fp64):
+    """The polariton configuration over its full length (tspan (0, 200), dt 0.05: 4000
+    steps, 100 saves, the pump ramp over the whole span) on a 128^2 grid: the error
+    stays at rounding level over every save, no drift."""
+    gkw, orc = polariton2d(N=128, L=256.0, A=5.0, ramp=200.0)
+    ts, res = gpe.solve(gpe.GrossPitaevskiiProblem(**gkw), gpe.StrangSplitting(), (0.0, 200.0), dt=0.05,
+                        nsaves=100, fp64=fp64)
+    ots, ores = oracle.solve(orc, (0.0, 200.0), 0.05, 100)
+    assert np.array_equal(ts, ots)
+    assert_close(oracle, res, ores, 1e-10)
