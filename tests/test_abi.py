@@ -128,3 +128,14 @@ def test_no_cpu_fallback(gpe, tmp_path):
     L = __import__("gpe_gb300._lib", fromlist=["load"])
     with pytest.raises(RuntimeError, match="no CPU fallback"):
         L.load(tmp_path / "missing.so")
+
+
+def test_c_driver_compiles_and_links(lib, gpe, tmp_path):
+    """The plain-C driver of the reference's plain case (tests/c_abi/kerr_c0.c) builds
+    against include/gpe.h and links against libgpe.so: the ABI is usable without Python."""
+    libdir = Path(lib._name).resolve().parent
+    exe = tmp_path / "kerr_c0"
+    subprocess.run(["gcc", "-O2", "-Wall", "-Werror", "-I", str(ROOT / "include"),
+                    str(ROOT / "tests" / "c_abi" / "kerr_c0.c"), f"-L{libdir}", "-lgpe", "-lm", "-o", str(exe)],
+                   check=True)
+    assert exe.exists()
