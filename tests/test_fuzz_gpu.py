@@ -154,7 +154,7 @@ def run_case(gpe, oracle, seed, dtype, fp64):
         assert_close(oracle, res, ores, fp32_tol(oracle, orc, tspan, cs["dt"], cs["nsaves"], xi=xi), per_save=False)
 
 
-@pytest.mark.parametrize("seed", list(range(12)))
+@pytest.mark.parametrize("seed", list(range(24)))
 @pytest.mark.parametrize("dtype,fp64", [(np.complex128, "dw"), (np.complex128, "native"), (np.complex64, "dw")],
                          ids=["c128-dw", "c128-native", "c64"])
 def test_random_problem(gpe, oracle, lib, seed, dtype, fp64):
