@@ -8,7 +8,7 @@ import math
 import numpy as np
 import pytest
 
-from cases import c_order, jl
+from cases import jl
 from test_parity_gpu import TOL, assert_close, fp32_tol
 
 pytestmark = pytest.mark.gpu
