@@ -34,6 +34,23 @@ static unsigned grid_for(int64_t n) {
   return (unsigned)(b > 152 * 32 ? 152 * 32 : (b < 1 ? 1 : b));
 }
 
+// *flag |= 1 when any of n values (FP64 or FP32) is NaN or Inf
+template <typename T>
+__global__ void nonfinite_kernel(const T* __restrict__ v, int64_t n, int* flag) {
+  bool bad = false;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    bad |= !isfinite(v[i]);
+  if (__syncthreads_or(bad) && threadIdx.x == 0) atomicOr(flag, 1);
+}
+
+int launch_nonfinite(const void* data, int64_t n, int is_f64, int* flag, cudaStream_t s) {
+  if (is_f64)
+    nonfinite_kernel<double><<<grid_for(n), 256, 0, s>>>((const double*)data, n, flag);
+  else
+    nonfinite_kernel<float><<<grid_for(n), 256, 0, s>>>((const float*)data, n, flag);
+  return (int)cudaGetLastError();
+}
+
 int launch_f64_to_dw(const void* src, void* dst, int64_t n, cudaStream_t s) {
   f64_to_dw_kernel<<<grid_for(n), 256, 0, s>>>((const double2*)src, (dwc*)dst, n);
   return (int)cudaGetLastError();

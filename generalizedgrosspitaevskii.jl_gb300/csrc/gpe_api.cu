@@ -418,30 +418,38 @@ static int check_comp(gpe_handle* h, int comp) {
   return GPE_OK;
 }
 
+static int ensure(gpe_handle* h, void** buf, size_t* cap, size_t bytes);
+
 int gpe_set_field(gpe_handle* h, int comp, const void* host) {
   NvtxRange nv("gpe_set_field");
   int rc = check_comp(h, comp);
   if (rc) return rc;
   if (!host) return fail(h, GPE_ERR_INVALID, "null field");
   const size_t n = (size_t)h->P * h->B;
-  const bool finite = h->dtype == GPE_C128 ? all_finite_par((const double*)host, 2 * n)
-                                           : all_finite_par((const float*)host, 2 * n);
-  if (!finite) return fail(h, GPE_ERR_NONFINITE, "field %d has NaN or Inf", comp);
   CK(h, cudaSetDevice(h->dev));
+  // stage the caller's values on the device, check them there, and only then replace the
+  // field: a rejected upload leaves the state as it was
+  const bool f64 = h->dtype == GPE_C128;
+  const size_t bytes = n * (f64 ? 16 : 8);
+  rc = ensure(h, &h->conv_buf, &h->conv_cap, bytes);
+  if (rc) return rc;
+  CK(h, cudaMemcpyAsync(h->conv_buf, host, bytes, cudaMemcpyHostToDevice, h->stream));
+  int* flag = reinterpret_cast<int*>(h->red);
+  CK(h, cudaMemsetAsync(flag, 0, sizeof(int), h->stream));
+  LK(h, gpe::launch_nonfinite(h->conv_buf, (int64_t)(2 * n), f64 ? 1 : 0, flag, h->stream));
+  int bad = 0;
+  CK(h, cudaMemcpyAsync(&bad, flag, sizeof(int), cudaMemcpyDeviceToHost, h->stream));
+  CK(h, cudaStreamSynchronize(h->stream));
+  if (bad) return fail(h, GPE_ERR_NONFINITE, "field %d has NaN or Inf", comp);
   if (h->prec == gpe::PREC_DW) {
-    // FP64 and double-word complex numbers both take 16 bytes: copy the FP64 values and
-    // split them in place on the device
-    CK(h, cudaMemcpyAsync(h->u[comp], host, n * 16, cudaMemcpyHostToDevice, h->stream));
-    LK(h, gpe::launch_f64_to_dw(h->u[comp], h->u[comp], (int64_t)n, h->stream));
-    CK(h, cudaStreamSynchronize(h->stream));
-    return GPE_OK;
+    // FP64 and double-word complex numbers both take 16 bytes: split on the device
+    LK(h, gpe::launch_f64_to_dw(h->conv_buf, h->u[comp], (int64_t)n, h->stream));
+  } else {
+    CK(h, cudaMemcpyAsync(h->u[comp], h->conv_buf, n * h->csz, cudaMemcpyDeviceToDevice, h->stream));
   }
-  CK(h, cudaMemcpyAsync(h->u[comp], host, n * h->csz, cudaMemcpyHostToDevice, h->stream));
   CK(h, cudaStreamSynchronize(h->stream));
   return GPE_OK;
 }
-
-static int ensure(gpe_handle* h, void** buf, size_t* cap, size_t bytes);
 
 int gpe_get_field(gpe_handle* h, int comp, void* host) {
   int rc = check_comp(h, comp);

@@ -102,6 +102,8 @@ int launch_spectral_moments(int prec, const void* uk, int64_t P, int64_t B, doub
 int launch_advance(int64_t* k, int64_t n, cudaStream_t s);
 // FP64 <-> double-word conversion of n complex numbers
 int launch_f64_to_dw(const void* src, void* dst, int64_t n, cudaStream_t s);
+// *flag |= 1 if any of n FP64 (is_f64) or FP32 values is NaN or Inf
+int launch_nonfinite(const void* data, int64_t n, int is_f64, int* flag, cudaStream_t s);
 int launch_dw_to_f64(const void* src, void* dst, int64_t n, cudaStream_t s);
 
 }  // namespace gpe

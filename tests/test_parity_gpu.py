@@ -394,3 +394,21 @@ def test_energy_matches_oracle(gpe, oracle, lib, case, dtype, fp64):
     tol = 1e-10 if dtype == np.complex128 else 1e-5
     scale = np.abs(e_ref).sum()
     assert np.all(np.abs(e_gpu - e_ref) <= tol * scale), (e_gpu, e_ref)
+
+
+@pytest.mark.parametrize("dtype,fp64", PRECISIONS, ids=PREC_IDS)
+def test_nonfinite_upload_is_rejected_and_state_kept(gpe, lib, dtype, fp64):
+    """A field with a NaN is refused (GPE_ERR_NONFINITE) after being staged on the
+    device, and the handle keeps its previous state."""
+    gkw, _ = kerr2d(32, 8.0, -1.0, dtype)
+    it = gpe.init(gpe.GrossPitaevskiiProblem(**gkw), gpe.StrangSplitting(), (0.0, 0.1), dt=0.01, nsaves=1, fp64=fp64)
+    it.step(3)
+    before = it.get_fields()[0].copy()
+    bad = before.copy()
+    bad[5, 7] = np.nan
+    with pytest.raises(Exception, match="NaN or Inf"):
+        it.set_fields((bad,))
+    assert np.array_equal(it.get_fields()[0], before)
+    it.step(1)
+    assert np.all(np.isfinite(it.get_fields()[0]))
+    it.close()
