@@ -382,11 +382,41 @@ def run_gpu(args, rank, world, local_rank):
     }
     if args.anchor_steps > 0:
         line["kerr1024"] = run_kerr1024(pkg, lib, L, local_rank, args.anchor_steps)
+    if args.solve_run:
+        line["polariton_solve"] = run_polariton_solve(pkg, lib, local_rank)
     if not args.no_cpu:
         line["cpu_baseline"] = cpu_baseline()
     if args.twa_steps > 0:
         line["twa"] = run_twa(pkg, args.twa_steps, tune=not args.no_tune)
     print(json.dumps(line), flush=True)
+
+
+def run_polariton_solve(pkg, lib, device):
+    """The polariton configuration exactly as specified, through solve(): one 512^2
+    two-component field, tspan (0, 200), dt 0.05 (4000 steps), nsaves 100 returned to the
+    host (the save ring streams every save out while the next steps run).  Wall-clock
+    time of the whole call (closure sampling, set-up, steps, saves, result assembly) and
+    of the stepping alone; FP64 (double-word) and FP32."""
+    disp, nonl, pump = polariton_closures()
+    out = []
+    for dtype in (np.complex128, np.complex64):
+        z = np.zeros((N_GRID, N_GRID), dtype, order="F")
+        prob = pkg.GrossPitaevskiiProblem((z, z.copy()), (L_BOX, L_BOX), dispersion=disp, nonlinearity=nonl,
+                                          pump=pump)
+        t0 = time.perf_counter()
+        it = pkg.StrangSplittingIterator(prob, (0.0, 200.0), dt=DT, nsaves=100, device=device)
+        t1 = time.perf_counter()
+        ts, res = it.solve()
+        t2 = time.perf_counter()
+        it.close()
+        steps = 4000
+        save_bytes = 100 * 2 * N_GRID * N_GRID * np.dtype(dtype).itemsize
+        out.append({"dtype": "f64-dw" if dtype == np.complex128 else "f32", "steps": steps, "saves": 100,
+                    "setup_s": t1 - t0, "solve_s": t2 - t1, "total_s": t2 - t0,
+                    "point_steps_per_s": N_GRID * N_GRID * steps / (t2 - t1),
+                    "saved_bytes": save_bytes, "result_shape": list(res[0].shape)})
+    return {"workload": "2-component polariton 512x512, one field, tspan (0, 200), dt 0.05, nsaves 100, via solve()",
+            "runs": out}
 
 
 def run_kerr1024(pkg, lib, L, device, steps):
@@ -621,6 +651,8 @@ def main():
     ap.add_argument("--twa-breakdown", action="store_true", help="print per-group TWA step times instead")
     ap.add_argument("--twa-group", type=int, default=0,
                     help="run --steps plain steps of the TWA group on this grid (an ncu capture case)")
+    ap.add_argument("--no-solve-run", dest="solve_run", action="store_false",
+                    help="skip the full-length polariton solve() measurement")
     ap.add_argument("--anchor-steps", type=int, default=200,
                     help="steps of the scalar Kerr 1024^2 FP64 measurement (0 skips it)")
     ap.add_argument("--precision-sweep", action="store_true",
