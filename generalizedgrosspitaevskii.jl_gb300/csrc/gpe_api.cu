@@ -74,6 +74,7 @@ using gpe::PassArgs;
 struct gpe_handle {
   gpe_desc d{};
   int dev = 0;
+  int nsm = 152;  // multiprocessors of dev
   int M = 1, dtype = GPE_C128, ndim = 2;
   int prec = gpe::PREC_DW;   // pass precision: FP64 fields default to double-word passes
   size_t rsz = 8, csz = 16;  // device bytes per real / complex number
@@ -331,6 +332,8 @@ int gpe_create(const gpe_desc* desc, gpe_handle** out) {
   gpe_handle* h = new gpe_handle();
   h->d = *desc;
   h->dev = dev;
+  int nsm = 0;
+  if (cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev) == cudaSuccess && nsm > 0) h->nsm = nsm;
   h->M = desc->ncomp;
   h->dtype = desc->dtype;
   h->ndim = desc->ndim;
@@ -741,6 +744,7 @@ static PassArgs base_args(gpe_handle* h) {
   a.n2 = (int32_t)h->n[2];
   a.P = h->P;
   a.B = h->B;
+  a.nsm = h->nsm;
   for (int m = 0; m < h->M; ++m) a.u[m] = h->u[m];
   a.ktab = h->ktab;
   a.kkind = h->kkind;

@@ -16,6 +16,7 @@ struct PassArgs {
   // geometry: n[0] = x (fastest); P = n0*n1*n2 spatial points; B trajectories
   int32_t n0, n1, n2;
   int64_t P, B;
+  int32_t nsm;  // streaming multiprocessors of the device (launch shapes)
   // fields (M planes of B*P complex numbers in the pass precision)
   void* u[2];
   // optional copy of the real-space state after the first half step of the pass

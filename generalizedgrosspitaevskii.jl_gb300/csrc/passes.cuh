@@ -662,14 +662,15 @@ __device__ __forceinline__ void half_points(typename CT<Real>::T (&x)[M][E], con
 // ------------------------------------------------------------------ row pass
 template <typename Real, int LOGN, int M, int V = 0>
 __global__ void __launch_bounds__(LineCfg<Real, M, LOGN, V>::ROW_THREADS, LineCfg<Real, M, LOGN, V>::ROW_MINB)
-row_kernel(const PassArgs a, const int64_t nlines) {
+row_kernel(const PassArgs a, const int64_t nlines, const int lb) {
+  // lb lines per block (Cfg::L, or fewer when there are too few lines to fill the SMs)
   using Cfg = LineCfg<Real, M, LOGN, V>;
   using C = typename CT<Real>::T;
-  constexpr int N = Cfg::N, E = Cfg::ER, T = Cfg::TR, L = Cfg::L;
+  constexpr int N = Cfg::N, E = Cfg::ER, T = Cfg::TR;
   extern __shared__ __align__(16) unsigned char smraw[];
   C* sm = reinterpret_cast<C*>(smraw);
   const int t = threadIdx.x % T, l = threadIdx.x / T;
-  int64_t line = (int64_t)blockIdx.x * L + l;
+  int64_t line = (int64_t)blockIdx.x * lb + l;
   const bool active = line < nlines;
   if (!active) line = nlines - 1;  // idle lines of the last block compute a copy, store nothing
   const RowLayout<C> lay{sm + l * N};
@@ -692,7 +693,7 @@ row_kernel(const PassArgs a, const int64_t nlines) {
   for (int ph = 0; ph < 4; ++ph) {
     if (ph == 0 || ph == 3) {
       if (ph == 0 ? a.do_ifft : a.do_fft)
-        fft_components<C, N, E, M, RowLayout<C>, Cfg::JOINT>(x, ph == 0, t, lay, tw, L * N);
+        fft_components<C, N, E, M, RowLayout<C>, Cfg::JOINT>(x, ph == 0, t, lay, tw, lb * N);
       continue;
     }
     const int64_t hr = ph == 2 ? a.hB : a.hA;
@@ -1132,8 +1133,14 @@ int launch_row_n(const PassArgs& a, int64_t nlines, cudaStream_t s) {
   auto k = row_kernel<Real, LOGN, M, V>;
   int e = set_smem(k, Cfg::ROW_KERNEL_SMEM);
   if (e) return e;
-  const int64_t blocks = (nlines + Cfg::L - 1) / Cfg::L;
-  k<<<(unsigned)blocks, Cfg::ROW_THREADS, Cfg::ROW_KERNEL_SMEM, s>>>(a, nlines);
+  // fewer lines per block when the default tiling would not give every SM two blocks
+  // (e.g. one 512^2 field: 128 blocks of 4 lines, 512 blocks of one line)
+  int lb = Cfg::L;
+  const int64_t want = 2 * (int64_t)(a.nsm > 0 ? a.nsm : 152);
+  while (lb > 1 && (nlines + lb - 1) / lb < want) lb /= 2;
+  const int64_t blocks = (nlines + lb - 1) / lb;
+  const size_t smem = Cfg::ROW_KERNEL_SMEM / Cfg::L * lb;
+  k<<<(unsigned)blocks, lb * Cfg::TR, smem, s>>>(a, nlines, lb);
   return (int)cudaGetLastError();
 }
 template <typename Real, int M, int LOGN, int V = 0>
