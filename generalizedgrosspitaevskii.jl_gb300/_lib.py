@@ -90,6 +90,7 @@ SIGNATURES = {
     "gpe_set_nonlinearity": (c_int, [H, c_void_p, c_void_p]),
     "gpe_set_matrix_nonlinearity": (c_int, [H, c_void_p, c_void_p]),
     "gpe_set_variant": (c_int, [H, c_int]),
+    "gpe_run_ex": (c_int, [H, c_int64, c_int64, c_void_p, c_void_p, c_int64, c_void_p]),
     "gpe_set_pump": (c_int, [H, c_int, c_void_p, c_int, c_void_p, c_int64]),
     "gpe_set_noise": (c_int, [H, c_int, c_uint64, c_void_p, c_void_p]),
     "gpe_run": (c_int, [H, c_int64, c_int64, c_void_p, c_void_p]),

@@ -825,7 +825,7 @@ constexpr int64_t kSaveRing = 4;
 
 struct SaveRing {
   gpe_handle* h;
-  int64_t nsaves;
+  int64_t comp_stride;  // saves between components in the caller's buffer
   size_t plane_bytes;
   char* out;
   int64_t drained = 0;
@@ -854,7 +854,7 @@ struct SaveRing {
       const int64_t r = drained % kSaveRing;
       CK(h, cudaEventSynchronize(h->ring_done[r]));
       for (int m = 0; m < h->M; ++m)
-        memcpy(out + ((size_t)m * nsaves + drained) * plane_bytes,
+        memcpy(out + ((size_t)m * comp_stride + drained) * plane_bytes,
                (char*)h->pinned + ((size_t)m * kSaveRing + r) * plane_bytes, plane_bytes);
     }
     return GPE_OK;
@@ -1169,7 +1169,7 @@ static int replay_graph(gpe_handle* h, int64_t nsteps, int64_t* launches) {
 }
 
 static int run_common(gpe_handle* h, int64_t nsteps, int64_t save_every, void* out, bool out_is_dev, double* ts_out,
-                      const void* xi_host) {
+                      const void* xi_host, int64_t comp_stride = -1) {
   if (!h) return GPE_ERR_INVALID;
   NvtxRange nv("gpe_run");
   CK(h, cudaSetDevice(h->dev));
@@ -1180,6 +1180,9 @@ static int run_common(gpe_handle* h, int64_t nsteps, int64_t save_every, void* o
                 (long long)save_every);
   const int64_t nsaves = save_every > 0 ? nsteps / save_every : 0;
   if (nsaves > 0 && !out) return fail(h, GPE_ERR_INVALID, "null save buffer");
+  if (comp_stride < 0) comp_stride = nsaves;  // host output: component m, slot s at m*comp_stride + s
+  if (comp_stride < nsaves) return fail(h, GPE_ERR_INVALID, "component stride %lld < %lld saves",
+                                        (long long)comp_stride, (long long)nsaves);
   for (int m = 0; m < h->M; ++m)
     if (h->pprof[m] && h->pcoef_n[m] > 1 && h->pcoef_n[m] < 2 * (h->steps + nsteps) + 1)
       return fail(h, GPE_ERR_INVALID, "pump %d has %lld amplitudes, %lld steps need %lld", m, (long long)h->pcoef_n[m],
@@ -1206,7 +1209,7 @@ static int run_common(gpe_handle* h, int64_t nsteps, int64_t save_every, void* o
                                                                             !(h->d.flags & GPE_FLAG_NO_RESIDENT) &&
                                                                             gpe::plane_fits(h->prec, h->M, h->logn[0]))));
   const bool use_ring = nsaves > kSaveRing && !out_is_dev && !single_launch;
-  SaveRing ring{h, nsaves, plane_bytes, (char*)out};
+  SaveRing ring{h, comp_stride, plane_bytes, (char*)out};
   if (nsaves > 0) {
     if (out_is_dev) {
       save_dev = out;
@@ -1281,9 +1284,16 @@ static int run_common(gpe_handle* h, int64_t nsteps, int64_t save_every, void* o
     const int rc = ring.drain(nsaves);
     if (rc) return rc;
   } else if (nsaves > 0 && !out_is_dev) {
-    CK(h, cudaMemcpy(out, save_dev, (size_t)h->M * nsaves * plane_bytes, cudaMemcpyDeviceToHost));
+    for (int m = 0; m < h->M; ++m)
+      CK(h, cudaMemcpy((char*)out + (size_t)m * comp_stride * plane_bytes, (char*)save_dev + (size_t)m * nsaves * plane_bytes,
+                       (size_t)nsaves * plane_bytes, cudaMemcpyDeviceToHost));
   }
   return GPE_OK;
+}
+
+int gpe_run_ex(gpe_handle* h, int64_t nsteps, int64_t save_every, const void* xi_host, void* out_host,
+               int64_t comp_stride, double* ts_out) {
+  return run_common(h, nsteps, save_every, out_host, false, ts_out, xi_host, comp_stride);
 }
 
 int gpe_run(gpe_handle* h, int64_t nsteps, int64_t save_every, void* out_host, double* ts_out) {

@@ -167,13 +167,18 @@ class StrangSplittingIterator:
             pass
 
     # -- stepping
+    def _replay_xi(self, nsteps: int) -> Optional[np.ndarray]:
+        """The replayed draws of the next nsteps steps, [half][m][batch][p], or None."""
+        if self.noise_replay is None:
+            return None
+        h0 = 2 * self.state().steps
+        return np.concatenate([np.ascontiguousarray(self.noise_replay(h0 + j), dtype=self.dtype).reshape(-1)
+                               for j in range(2 * nsteps)])
+
     def _run(self, nsteps: int, save_every: int, out: Optional[np.ndarray], ts: Optional[np.ndarray]):
         lib, h = self.lib, self.h
-        if self.noise_replay is not None:
-            st = self.state()
-            h0 = 2 * st.steps
-            xi = np.concatenate([np.ascontiguousarray(self.noise_replay(h0 + j), dtype=self.dtype).reshape(-1)
-                                 for j in range(2 * nsteps)])
+        xi = self._replay_xi(nsteps)
+        if xi is not None:
             L.check(lib, h, lib.gpe_run_replay(h, nsteps, save_every, L.ptr(xi), L.ptr(out), L.ptr(ts)))
         else:
             L.check(lib, h, lib.gpe_run(h, nsteps, save_every, L.ptr(out), L.ptr(ts)))
@@ -227,19 +232,22 @@ class StrangSplittingIterator:
         return flat.reshape(cshape).T
 
     def solve(self):
-        """solve! (src/fixed_time_stepping.jl:26-54) -> (ts, result)."""
+        """solve! (src/fixed_time_stepping.jl:26-54) -> (ts, result).  The saves land in
+        place in the result (component stride nsaves + save_start, gpe_run_ex), with u0 in
+        slot 0 when save_start."""
         M, ns, off = self.prob.M, self.nsaves, int(self.save_start)
         plane = self.B * self.P
-        raw = np.empty((M, ns, plane), self.dtype)
+        full = np.empty((M, ns + off, plane), self.dtype)
+        if off:
+            for m in range(M):
+                full[m, 0] = np.asarray(self.prob.u0[m]).ravel(order="F")
         ts = np.empty(ns, np.float64)
-        self._run(ns * self.steps_per_save, self.steps_per_save, raw, ts)
-        res = []
-        for m in range(M):
-            full = np.empty((ns + off, plane), self.dtype)
-            if off:
-                full[0] = np.asarray(self.prob.u0[m]).ravel(order="F")
-            full[off:] = raw[m]
-            res.append(self._as_julia(full, extra=(ns + off,)))
+        nsteps = ns * self.steps_per_save
+        xi = self._replay_xi(nsteps)
+        out = full[0, off:] if ns > 0 else full
+        L.check(self.lib, self.h, self.lib.gpe_run_ex(self.h, nsteps, self.steps_per_save, L.ptr(xi), L.ptr(out),
+                                                      ns + off, L.ptr(ts)))
+        res = [self._as_julia(full[m], extra=(ns + off,)) for m in range(M)]
         self.ts[1:] = ts
         times = self.ts if self.save_start else self.ts[1:]
         return times.copy(), tuple(res)

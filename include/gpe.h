@@ -163,6 +163,12 @@ int gpe_set_noise(gpe_handle* h, int mode, uint64_t seed, const double* eta,
  * out_host may be NULL when save_every == 0. */
 int gpe_run(gpe_handle* h, int64_t nsteps, int64_t save_every, void* out_host,
             double* ts_out);
+/* As gpe_run (xi_host NULL) or gpe_run_replay (xi_host set), with component m, slot s of
+ * the saves at out_host + (m*comp_stride + s) * batch*P complex numbers, comp_stride >=
+ * nsaves: a caller can leave room for the initial state beside the saves (solve's result
+ * holds u0 in slot 0) and receive the run in place.  No counterpart in the reference. */
+int gpe_run_ex(gpe_handle* h, int64_t nsteps, int64_t save_every, const void* xi_host, void* out_host,
+               int64_t comp_stride, double* ts_out);
 /* As gpe_run with out_dev a device buffer of the same layout the caller owns. */
 int gpe_run_dev(gpe_handle* h, int64_t nsteps, int64_t save_every, void* out_dev,
                 double* ts_out);
