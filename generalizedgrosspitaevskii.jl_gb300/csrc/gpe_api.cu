@@ -44,14 +44,23 @@ template <typename Real> int launch_mat_t(const PassArgs&, cudaStream_t);
   if (dtype == PREC_DW) return M == 1 ? FN<DWR, 1>(__VA_ARGS__) : FN<DWR, 2>(__VA_ARGS__);        \
   return M == 1 ? FN<float, 1>(__VA_ARGS__) : FN<float, 2>(__VA_ARGS__);
 
-// variant 1 (alternative line tiling) exists for FP32 one-component fields only
+// variant 1 (alternative line tiling) exists for FP32 one-component fields only;
+// variant 2 (fine tiling) for every precision and component count
+#define GPE_DISPATCH_V2(FN, ...)                                                                        \
+  if (variant == 2) {                                                                                   \
+    if (dtype == PREC_F64) return M == 1 ? FN<double, 1, 2>(__VA_ARGS__) : FN<double, 2, 2>(__VA_ARGS__); \
+    if (dtype == PREC_DW) return M == 1 ? FN<DWR, 1, 2>(__VA_ARGS__) : FN<DWR, 2, 2>(__VA_ARGS__);       \
+    return M == 1 ? FN<float, 1, 2>(__VA_ARGS__) : FN<float, 2, 2>(__VA_ARGS__);                         \
+  }
 int launch_row(int dtype, int M, int logn, const PassArgs& a, int64_t nl, cudaStream_t s, int variant) {
+  GPE_DISPATCH_V2(launch_row_t, logn, a, nl, s)
   if (variant == 1 && dtype == PREC_F32 && M == 1) return launch_row_t<float, 1, 1>(logn, a, nl, s);
   if (dtype == PREC_F64) return M == 1 ? launch_row_t<double, 1, 0>(logn, a, nl, s) : launch_row_t<double, 2, 0>(logn, a, nl, s);
   if (dtype == PREC_DW) return M == 1 ? launch_row_t<DWR, 1, 0>(logn, a, nl, s) : launch_row_t<DWR, 2, 0>(logn, a, nl, s);
   return M == 1 ? launch_row_t<float, 1, 0>(logn, a, nl, s) : launch_row_t<float, 2, 0>(logn, a, nl, s);
 }
 int launch_col(int dtype, int M, int logn, const PassArgs& a, cudaStream_t s, int variant) {
+  GPE_DISPATCH_V2(launch_col_t, logn, a, s)
   if (variant == 1 && dtype == PREC_F32 && M == 1) return launch_col_t<float, 1, 1>(logn, a, s);
   if (dtype == PREC_F64) return M == 1 ? launch_col_t<double, 1, 0>(logn, a, s) : launch_col_t<double, 2, 0>(logn, a, s);
   if (dtype == PREC_DW) return M == 1 ? launch_col_t<DWR, 1, 0>(logn, a, s) : launch_col_t<DWR, 2, 0>(logn, a, s);
@@ -106,7 +115,7 @@ struct gpe_handle {
   double g[2][2][2] = {};
   double c[2][2] = {};
   int nl_on[2] = {0, 0};
-  int variant = 0;  // line tiling of the two-pass passes (gpe_set_variant)
+  int variant = -1;  // line tiling of the two-pass passes (gpe_set_variant); -1 = by size
   int nl_matrix = 0;
   double* nlm = nullptr;  // device copy of the matrix nonlinearity coefficients
   double t = 0.0;
@@ -175,6 +184,10 @@ static int fail(gpe_handle* h, int code, const char* fmt, ...) {
   } while (0)
 
 static bool is_pow2(int64_t v) { return v > 0 && (v & (v - 1)) == 0; }
+
+// Fields of at most this many points (all trajectories) take the fine line tiling unless
+// a variant was set: the default leaves most of the GPU idle there (one 512^2 field).
+constexpr int64_t kFinePoints = int64_t(1) << 19;
 
 // NVTX range over an API call (visible in Nsight timelines; no cost without a tool)
 struct NvtxRange {
@@ -736,6 +749,11 @@ struct TimedLaunch {
 };
 
 // Fill the coefficient part of the pass arguments.
+static int pass_variant(const gpe_handle* h) {
+  if (h->variant >= 0) return h->variant;
+  return h->P * h->B <= kFinePoints ? 2 : 0;
+}
+
 static PassArgs base_args(gpe_handle* h) {
   PassArgs a;
   memset(&a, 0, sizeof a);
@@ -1060,7 +1078,7 @@ static int enqueue_steps(gpe_handle* h, int64_t nsteps, int64_t save_every, void
   r.hB = -1;
   {
     TimedLaunch tl(h, 0);
-    LK(h, gpe::launch_row(h->prec, h->M, h->logn[0], r, nrows, h->stream, h->variant));
+    LK(h, gpe::launch_row(h->prec, h->M, h->logn[0], r, nrows, h->stream, pass_variant(h)));
   }
   ++nl;
   std::vector<std::pair<PassArgs, int>> cols;  // (args, log2 line length)
@@ -1095,7 +1113,7 @@ static int enqueue_steps(gpe_handle* h, int64_t nsteps, int64_t save_every, void
   for (int64_t s = 0; s < nsteps; ++s) {
     for (auto& cp : cols) {
       TimedLaunch tl(h, 1);
-      LK(h, gpe::launch_col(h->prec, h->M, cp.second, cp.first, h->stream, h->variant));
+      LK(h, gpe::launch_col(h->prec, h->M, cp.second, cp.first, h->stream, pass_variant(h)));
       ++nl;
     }
     const bool last = (s == nsteps - 1);
@@ -1116,7 +1134,7 @@ static int enqueue_steps(gpe_handle* h, int64_t nsteps, int64_t save_every, void
     }
     {
       TimedLaunch tl(h, 0);
-      LK(h, gpe::launch_row(h->prec, h->M, h->logn[0], rr, nrows, h->stream, h->variant));
+      LK(h, gpe::launch_row(h->prec, h->M, h->logn[0], rr, nrows, h->stream, pass_variant(h)));
     }
     if (saving && ring) {
       const int rc = ring->after(si);
@@ -1410,7 +1428,7 @@ int gpe_energy(gpe_handle* h, double* out) {
 
 int gpe_set_variant(gpe_handle* h, int variant) {
   if (!h) return GPE_ERR_INVALID;
-  if (variant < 0 || variant > 1) return fail(h, GPE_ERR_INVALID, "variant %d: expected 0 or 1", variant);
+  if (variant < -1 || variant > 2) return fail(h, GPE_ERR_INVALID, "variant %d: expected -1, 0, 1 or 2", variant);
   if (variant == 1 && !(h->prec == gpe::PREC_F32 && h->M == 1))
     return fail(h, GPE_ERR_UNSUPPORTED, "variant 1 exists for FP32 one-component fields only");
   if (variant != h->variant) {

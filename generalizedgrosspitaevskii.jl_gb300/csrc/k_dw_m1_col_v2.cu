@@ -1,0 +1,6 @@
+// Instantiates the fine-tiling col kernels (V = 2: 4 points a thread) for double-word FP64
+// fields with 1 component(s), used when a field is too small to fill the GPU.
+#include "passes.cuh"
+namespace gpe {
+GPE_INSTANTIATE_COL_V(DWR, 1, 2)
+}  // namespace gpe

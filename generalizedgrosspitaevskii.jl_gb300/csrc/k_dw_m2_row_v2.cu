@@ -1,0 +1,6 @@
+// Instantiates the fine-tiling row kernels (V = 2: 4 points a thread) for double-word FP64
+// fields with 2 component(s), used when a field is too small to fill the GPU.
+#include "passes.cuh"
+namespace gpe {
+GPE_INSTANTIATE_ROW_V(DWR, 2, 2)
+}  // namespace gpe

@@ -35,6 +35,9 @@ struct LineCfg {
   // pointwise half steps and so keeps fewer points live).  FP32 column passes use 8 so
   // two CTAs share an SM and one's loads overlap the other's FFTs.
   static constexpr bool ALT = V == 1 && sizeof(C) == 8 && M == 1;
+  // V=2: fine tiling for fields too small to fill the GPU (4 points a thread in both
+  // passes: twice the threads of the default at the price of more radix-4 stages)
+  static constexpr bool FINE = V == 2;
 // one-component 16-byte lines: 8 points a thread in both passes (1024^2 Kerr, 16 copies:
 // 1.141 ms per step against 1.174 ms with 16 / 16, 1.154 with 8 / 16, 1.156 with 16 / 8)
 #ifndef GPE_E_W16_M1
@@ -43,13 +46,13 @@ struct LineCfg {
 #ifndef GPE_ER_W16_M1
 #define GPE_ER_W16_M1 8
 #endif
-  static constexpr int EMAX = ALT ? 16 : ((sizeof(C) == 16 && M == 2) || sizeof(C) == 8 ? 8 : GPE_E_W16_M1);
+  static constexpr int EMAX = FINE ? 4 : ALT ? 16 : ((sizeof(C) == 16 && M == 2) || sizeof(C) == 8 ? 8 : GPE_E_W16_M1);
   static constexpr int E = cmin(EMAX, N / 2);
   static constexpr int T = N / E;  // threads per line, column pass
 #ifndef GPE_ER_F32
 #define GPE_ER_F32 8
 #endif
-  static constexpr int ERMAX = ALT ? 8 : ((M == 2) ? (sizeof(C) == 8 ? GPE_ER_F32 : 8) : (sizeof(C) == 16 ? GPE_ER_W16_M1 : 16));
+  static constexpr int ERMAX = FINE ? 4 : ALT ? 8 : ((M == 2) ? (sizeof(C) == 8 ? GPE_ER_F32 : 8) : (sizeof(C) == 16 ? GPE_ER_W16_M1 : 16));
   static constexpr int ER = cmin(ERMAX, N / 2);
   static constexpr int TR = N / ER;  // threads per line, row pass
 #ifndef GPE_ROWT_W16

@@ -67,9 +67,9 @@ class StrangSplittingIterator:
 
     def __init__(self, prob: GrossPitaevskiiProblem, tspan, *, dt, nsaves, save_start=True, rng=None,
                  noise_replay: Optional[Callable] = None, total_steps: Optional[int] = None,
-                 device: int = -1, fp64: str = "dw", resident: bool = True, variant: int = 0):
+                 device: int = -1, fp64: str = "dw", resident: bool = True, variant: Optional[int] = None):
         self.lib = L.load()
-        self.variant = int(variant)
+        self.variant = variant
         self.prob = prob
         self.nsaves = int(nsaves)
         self.save_start = bool(save_start)
@@ -112,8 +112,8 @@ class StrangSplittingIterator:
     def _configure(self, rng):
         prob, lib, h = self.prob, self.lib, self.h
         M = prob.M
-        if self.variant:
-            L.check(lib, h, lib.gpe_set_variant(h, self.variant))
+        if self.variant is not None:
+            L.check(lib, h, lib.gpe_set_variant(h, int(self.variant)))
         for m in range(M):
             L.check(lib, h, lib.gpe_set_field(h, m, L.ptr(prob.u0[m])))
         dg, rg = direct_grid(prob), reciprocal_grid(prob)
@@ -255,7 +255,7 @@ class StrangSplittingIterator:
 
 def init(prob: GrossPitaevskiiProblem, alg: StrangSplitting, tspan, *, dt, nsaves, show_progress=False,
          progress=None, save_start=True, workgroup_size=(), rng=None, noise_replay=None, fp64="dw", device=-1,
-         resident=True, variant=0):
+         resident=True, variant=None):
     """init(prob, StrangSplitting(), tspan; dt, nsaves, ...) (src/strang_splitting.jl:32-67).
     show_progress / progress / workgroup_size are accepted for signature parity and
     have no effect: the backend picks its own launch shapes.  Extra keywords: ``rng``
@@ -263,7 +263,8 @@ def init(prob: GrossPitaevskiiProblem, alg: StrangSplitting, tspan, *, dt, nsave
     noise), ``fp64`` ("dw": ComplexF64 fields advanced in double-word arithmetic on the
     FP32 pipes, the default; "native": FP64 instructions), ``device`` (CUDA ordinal),
     ``resident`` (False forces the two-pass HBM path for small square 2D grids),
-    ``variant`` (line tiling of the two-pass passes, see gpe_set_variant)."""
+    ``variant`` (line tiling of the two-pass passes, see gpe_set_variant; None lets the
+    library choose by field size)."""
     if not isinstance(alg, StrangSplitting):
         raise TypeError("the only algorithm is StrangSplitting()")
     return StrangSplittingIterator(prob, tspan, dt=dt, nsaves=nsaves, save_start=save_start, rng=rng,

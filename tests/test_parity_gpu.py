@@ -412,3 +412,34 @@ def test_nonfinite_upload_is_rejected_and_state_kept(gpe, lib, dtype, fp64):
     it.step(1)
     assert np.all(np.isfinite(it.get_fields()[0]))
     it.close()
+
+
+@pytest.mark.parametrize("dtype,fp64", PRECISIONS, ids=PREC_IDS)
+@pytest.mark.parametrize("variant", [0, 2], ids=["default-tiling", "fine-tiling"])
+@pytest.mark.parametrize("case", ["kerr", "polariton", "3d"])
+def test_line_tilings_match_oracle(gpe, oracle, lib, case, variant, dtype, fp64):
+    """Both line tilings of the two-pass passes (forced with gpe_set_variant) against the
+    oracle, for one- and two-component 2D fields and a 3D grid."""
+    if case == "kerr":
+        gkw, orc = kerr2d(128, 8.0, -2.0, dtype)
+        tspan, dt, ns = (0.0, 0.1), 0.005, 4
+    elif case == "polariton":
+        gkw, orc = polariton2d(N=128, L=256.0, A=5.0, ramp=20.0, dtype=dtype)
+        tspan, dt, ns = (0.0, 2.0), 0.05, 4
+    else:
+        L = (8.0, 6.0, 5.0)
+        X, Y, Z = oracle.mesh(oracle.grids(L, (32, 16, 16))[0])
+        u0c = np.exp(-(X - 4) ** 2 - (Y - 3) ** 2 - (Z - 2.5) ** 2 + 0.2j * X).astype(np.complex128)
+        disp = lambda k, p: (k[0] ** 2 + k[1] ** 2 + k[2] ** 2) / 2
+        gkw = dict(u0=(jl(u0c).astype(dtype),), lengths=L, dispersion=disp,
+                   nonlinearity=lambda u, p: 1.3 * np.abs(u[0]) ** 2)
+        orc = oracle.OracleProblem(u0=(u0c,), lengths=L, dispersion=disp, nonlin_g=np.array([[1.3]]))
+        tspan, dt, ns = (0.0, 0.1), 0.01, 2
+    prob = gpe.GrossPitaevskiiProblem(**gkw)
+    ts, res = gpe.solve(prob, gpe.StrangSplitting(), tspan, dt=dt, nsaves=ns, fp64=fp64, resident=False,
+                        variant=variant)
+    ots, ores = oracle.solve(orc, tspan, dt, ns)
+    if dtype == np.complex128:
+        assert_close(oracle, res, ores, TOL[dtype])
+    else:
+        assert_close(oracle, res, ores, fp32_tol(oracle, orc, tspan, dt, ns), per_save=False)
