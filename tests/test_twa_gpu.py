@@ -160,12 +160,16 @@ def test_alternative_tiling_matches_oracle(gpe, oracle, lib):
 
 def test_variant_needs_fp32_one_component(gpe, lib):
     """The alternative tiling exists for FP32 one-component fields only; other handles
-    refuse it with GPE_ERR_UNSUPPORTED and keep working."""
+    refuse it with GPE_ERR_UNSUPPORTED and keep working.  The fine tiling (2) and the
+    choice by size (-1) exist everywhere; other values are invalid."""
     T = twa(gpe)
     prm = T.DampedDrivenParams()
     it = T.make_group(32, 2, prm, 10, seed=1, dtype=np.complex128)
     assert lib.gpe_set_variant(it.h, 1) == -2
-    assert lib.gpe_set_variant(it.h, 2) == -1
+    assert lib.gpe_set_variant(it.h, 3) == -1
+    assert lib.gpe_set_variant(it.h, -2) == -1
+    assert lib.gpe_set_variant(it.h, 2) == 0
+    assert lib.gpe_set_variant(it.h, -1) == 0
     assert lib.gpe_set_variant(it.h, 0) == 0
     it.step(2)
     it.close()
