@@ -185,9 +185,11 @@ static int fail(gpe_handle* h, int code, const char* fmt, ...) {
 
 static bool is_pow2(int64_t v) { return v > 0 && (v & (v - 1)) == 0; }
 
-// Fields of at most this many points (all trajectories) take the fine line tiling unless
-// a variant was set: the default leaves most of the GPU idle there (one 512^2 field).
-constexpr int64_t kFinePoints = int64_t(1) << 19;
+// Two-component fields of at most this many points (all trajectories) take the fine line
+// tiling unless a variant was set.  Measured per step, one 512^2 two-component field:
+// 53.3 / 22.6 us fine against 55.3 / 26.7 us default (double-word / FP32); at 2^19 points
+// and for one-component fields the default tiling is faster.
+constexpr int64_t kFinePoints = int64_t(1) << 18;
 
 // NVTX range over an API call (visible in Nsight timelines; no cost without a tool)
 struct NvtxRange {
@@ -751,7 +753,7 @@ struct TimedLaunch {
 // Fill the coefficient part of the pass arguments.
 static int pass_variant(const gpe_handle* h) {
   if (h->variant >= 0) return h->variant;
-  return h->P * h->B <= kFinePoints ? 2 : 0;
+  return h->M == 2 && h->P * h->B <= kFinePoints ? 2 : 0;
 }
 
 static PassArgs base_args(gpe_handle* h) {

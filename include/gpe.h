@@ -204,8 +204,8 @@ int gpe_set_graph(gpe_handle* h, int64_t steps_per_graph);
 /* Line tiling of the two-pass passes: 0, the default tiling; 1, the alternative tiling of
  * FP32 one-component fields (8 points a thread along x, 16 along y/z instead of 16 and 8);
  * 2, the fine tiling (4 points a thread in both passes: twice the threads, for fields too
- * small to fill the GPU); -1 (the initial setting), 2 for fields of at most 2^19 points
- * over all trajectories and 0 above.  Tilings agree to rounding, not bit for bit.  Set it
+ * small to fill the GPU); -1 (the initial setting), 2 for two-component fields of at most
+ * 2^18 points over all trajectories and 0 otherwise.  Tilings agree to rounding, not bit for bit.  Set it
  * before capturing graphs or ensembles that include the handle.  No counterpart in the
  * reference (the choice an autotuner makes per grid size). */
 int gpe_set_variant(gpe_handle* h, int variant);
