@@ -16,6 +16,9 @@ e2e        : the same through the C ABI with host buffers: H2D of the state from
 roofline   : dominant kernel, algorithmic bytes per launch / its mean event-timed
              duration, against the measured HBM copy bandwidth
 cpu_baseline: the FP64 oracle (scipy FFT, all host threads) on a bounded sample
+plain_gpu  : the plain GPU split step on the same workload (cuFFT transforms + unfused
+             torch elementwise kernels, the reference's step order): its rate, the rate
+             of its transforms alone, and the fused passes' speed-up over both
 --impl reference: the reference's algorithm on the host cores (the Julia reference
              cannot run here; its restatement in oracle/ is the reference arm)
 """
@@ -347,6 +350,12 @@ def run_gpu(args, rank, world, local_rank):
     e2e_value = P * B * args.steps * world / e2e_s
     state_bytes = 2 * B * P * np.dtype(dtype).itemsize
     it.close()
+    plain = None
+    if args.plain_steps > 0:
+        plain = run_plain_gpu(dtype, B, args.plain_steps, 3, local_rank, value / world)
+        if dtype == np.complex128 and args.fp64 == "dw" and rank == 0:
+            plain["rel_l2_fused_vs_plain_f64"] = plain_vs_fused_rel_l2(pkg, local_rank)
+            plain["rel_l2_case"] = "one pumped 512^2 field from u = 0, 200 steps, fused double-word vs plain FP64"
 
     if rank != 0:
         return
@@ -380,6 +389,8 @@ def run_gpu(args, rank, world, local_rank):
                      "binding_limit": binding_limit(dtype, args.fp64)},
         "clocks": clk.summary(),
     }
+    if plain is not None:
+        line["plain_gpu"] = plain
     if args.anchor_steps > 0:
         line["kerr1024"] = run_kerr1024(pkg, lib, L, local_rank, args.anchor_steps)
     if args.solve_run:
@@ -414,7 +425,8 @@ def run_polariton_solve(pkg, lib, device):
         out.append({"dtype": "f64-dw" if dtype == np.complex128 else "f32", "steps": steps, "saves": 100,
                     "setup_s": t1 - t0, "solve_s": t2 - t1, "total_s": t2 - t0,
                     "point_steps_per_s": N_GRID * N_GRID * steps / (t2 - t1),
-                    "saved_bytes": save_bytes, "result_shape": list(res[0].shape)})
+                    "saved_bytes": save_bytes, "result_shape": list(res[0].shape),
+                    "plain_gpu_ms_per_step": plain_single_field_ms(dtype, device)})
     return {"workload": "2-component polariton 512x512, one field, tspan (0, 200), dt 0.05, nsaves 100, via solve()",
             "runs": out}
 
@@ -448,6 +460,162 @@ def run_kerr1024(pkg, lib, L, device, steps):
                     "l2": "field L2-resident (16 MiB)" if B == 1 else "256 MiB of fields, streamed from HBM"})
     return {"workload": "scalar Kerr 1024x1024 FP64, L=32, G=|u|^2, dt=0.005 (80 algorithmic B per point-step)",
             "runs": out}
+
+
+def expm2_np(A):
+    """exp(A) for a field of 2x2 complex matrices A[i, j][...] (closed form: e^{tr/2}
+    [cosh(s) I + sinh(s)/s (A - tr/2 I)], s^2 = ((a-d)/2)^2 + bc, series for sinh(s)/s
+    near s = 0)."""
+    ht = (A[0][0] + A[1][1]) / 2
+    hd = (A[0][0] - A[1][1]) / 2
+    s = np.sqrt(hd * hd + A[0][1] * A[1][0])
+    small = np.abs(s) < 1e-3
+    s2 = s * s
+    shs = np.where(small, 1 + s2 / 6 + s2 * s2 / 120, np.sinh(s) / np.where(small, 1.0, s))
+    e = np.exp(ht)
+    ch = np.cosh(s)
+    return [[e * (ch + shs * (A[0][0] - ht)), e * shs * A[0][1]], [e * shs * A[1][0], e * (ch + shs * (A[1][1] - ht))]]
+
+
+class PlainSplitStep:
+    """The plain GPU form of the reference's Strang step for the polariton workload, the
+    comparator of the fused passes: cuFFT transforms (torch.fft.fft2 over every component
+    and copy at once) and the per-point work as separate elementwise torch operations, in
+    the reference's order (src/strang_splitting.jl:69-90): at each half-step time the pump
+    is evaluated over the whole grid into the `next` buffer after `now` takes the old one
+    (src/misc.jl:22-42), then u <- cis(-dt/2 G(u)) (u + dt/4 F_now) + dt/4 F_next
+    (src/kernels.jl:37-54); between the half steps the 2x2 table exp(-i dt D(k)) (built in
+    FP64 on the host, src/misc.jl:14-20) is applied per k between the forward and the
+    normalised inverse transform.  State: torch tensor (2, B, N, N), [component][copy][y][x]."""
+
+    def __init__(self, N: int, L: float, B: int, dtype, device, u0=None, dt: float = DT, prm=None):
+        import torch
+        self.torch = torch
+        p = prm or POL
+        self.p, self.dt, self.N, self.B = p, dt, N, B
+        c64 = dtype == np.complex64
+        self.cdt = torch.complex64 if c64 else torch.complex128
+        rdt = torch.float32 if c64 else torch.float64
+        x = np.arange(N) * (L / N)
+        k = 2 * np.pi * np.fft.fftfreq(N, L / N)
+        KY, KX = np.meshgrid(k, k, indexing="ij")
+        Y, X = np.meshgrid(x, x, indexing="ij")
+        k2 = KX ** 2 + KY ** 2
+        one = np.ones_like(k2)
+        D = [[p["hbar"] * k2 / (2 * p["m"]) - p["dc"] - 1j * p["gc"], p["Om"] * one],
+             [p["Om"] * one, (-p["dx"] - 1j * p["gx"]) * one]]
+        E = expm2_np([[-1j * dt * D[i][j] for j in range(2)] for i in range(2)])
+        dev = torch.device(device)
+        self.T = [[torch.tensor(E[i][j], dtype=self.cdt, device=dev) for j in range(2)] for i in range(2)]
+        prof = np.exp(-((X - L / 2) ** 2 + (Y - L / 2) ** 2) / p["w"] ** 2)
+        self.prof = torch.tensor(prof, dtype=rdt, device=dev)
+        self.u = (torch.zeros((2, B, N, N), dtype=self.cdt, device=dev) if u0 is None
+                  else torch.tensor(np.asarray(u0), dtype=self.cdt, device=dev))
+        self.t = 0.0
+        self.nxt = self.prof * self.amp(0.0)  # init evaluates F(t0) into `next`
+        self.now = torch.empty_like(self.nxt)
+
+    def amp(self, t: float) -> float:
+        return self.p["A"] * min(t / self.p["ramp"], 1.0)
+
+    def half(self, t_pump: float):
+        torch = self.torch
+        self.now, self.nxt = self.nxt, self.now
+        torch.mul(self.prof, self.amp(t_pump), out=self.nxt)
+        dth = self.dt / 2
+        u0, u1 = self.u[0], self.u[1]
+        u0.add_(self.now, alpha=dth / 2)   # G_0 = 0: cis(0) (u + dt/4 F_now) + dt/4 F_next
+        u0.add_(self.nxt, alpha=dth / 2)
+        dens = torch.view_as_real(u1).square().sum(-1)
+        u1.mul_(torch.exp(dens.mul(-1j * dth * self.p["g"])))
+
+    def diffusion(self):
+        torch = self.torch
+        U = torch.fft.fft2(self.u)
+        V = torch.empty_like(U)
+        for i in range(2):
+            torch.mul(self.T[i][0], U[0], out=V[i])
+            V[i].addcmul_(self.T[i][1], U[1])
+        self.u = torch.fft.ifft2(V)
+
+    def step(self, n: int = 1):
+        for _ in range(n):
+            self.t = self.t + self.dt
+            self.half(self.t + self.dt / 2)
+            self.diffusion()
+            self.half(self.t + self.dt)
+
+    def fft_only(self, n: int = 1):
+        """The transforms of n steps alone (forward and inverse of both components)."""
+        torch = self.torch
+        for _ in range(n):
+            self.u = torch.fft.ifft2(torch.fft.fft2(self.u))
+
+
+def run_plain_gpu(dtype, B: int, steps: int, warmup: int, device: int, fused_value: float):
+    """Times the plain cuFFT form (PlainSplitStep) on the same workload and batch as the
+    fused passes: whole steps, and the transforms alone (a lower bound for any split step
+    built on cuFFT), CUDA events on torch's stream, inputs larger than L2."""
+    import torch
+    dev = f"cuda:{device}"
+    ps = PlainSplitStep(N_GRID, L_BOX, B, dtype, dev)
+    ev = [torch.cuda.Event(enable_timing=True) for _ in range(4)]
+    ps.step(warmup)
+    torch.cuda.synchronize()
+    ev[0].record()
+    ps.step(steps)
+    ev[1].record()
+    ps.fft_only(warmup)
+    ev[2].record()
+    ps.fft_only(steps)
+    ev[3].record()
+    torch.cuda.synchronize()
+    ms = ev[0].elapsed_time(ev[1]) / steps
+    ms_fft = ev[2].elapsed_time(ev[3]) / steps
+    P = N_GRID * N_GRID
+    v, vf = P * B / (ms * 1e-3), P * B / (ms_fft * 1e-3)
+    del ps
+    torch.cuda.empty_cache()
+    return {"impl": "plain GPU split step: cuFFT (torch.fft.fft2 / ifft2 over both components and all copies) "
+                    "and unfused torch elementwise kernels for the pump evaluation, half steps and 2x2 table",
+            "dtype": "f64" if dtype == np.complex128 else "f32", "batch": B, "steps": steps,
+            "ms_per_step": ms, "value": v, "unit": "grid-point-steps/s",
+            "fft_only_ms_per_step": ms_fft, "fft_only_value": vf,
+            "speedup": fused_value / v, "speedup_vs_fft_only": fused_value / vf}
+
+
+def plain_single_field_ms(dtype, device: int, steps: int = 200) -> float:
+    """ms per step of the plain cuFFT form on one 512^2 polariton field (no saves)."""
+    import torch
+    ps = PlainSplitStep(N_GRID, L_BOX, 1, dtype, f"cuda:{device}")
+    ps.step(10)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    e0.record()
+    ps.step(steps)
+    e1.record()
+    torch.cuda.synchronize()
+    del ps
+    return e0.elapsed_time(e1) / steps
+
+
+def plain_vs_fused_rel_l2(pkg, device: int, steps: int = 200):
+    """rel L2 between the plain cuFFT form in FP64 and the fused double-word passes after
+    `steps` steps of one pumped polariton field from u = 0."""
+    import torch
+    disp, nonl, pump = polariton_closures()
+    z = np.zeros((N_GRID, N_GRID), np.complex128, order="F")
+    prob = pkg.GrossPitaevskiiProblem((z, z.copy()), (L_BOX, L_BOX), dispersion=disp, nonlinearity=nonl, pump=pump)
+    it = pkg.StrangSplittingIterator(prob, (0.0, steps * DT), dt=DT, nsaves=1, device=device)
+    it.step(steps)
+    got = np.stack([np.ascontiguousarray(f.T) for f in it.get_fields()])
+    it.close()
+    ps = PlainSplitStep(N_GRID, L_BOX, 1, np.complex128, f"cuda:{device}")
+    ps.step(steps)
+    ref = ps.u[:, 0].cpu().numpy()
+    del ps
+    torch.cuda.empty_cache()
+    return float(np.linalg.norm(got - ref) / max(np.linalg.norm(ref), 1e-300))
 
 
 TWA_GROUPS = [(64, 342), (128, 341), (256, 341)]  # 1024 trajectories over three grids
@@ -653,6 +821,8 @@ def main():
                     help="run --steps plain steps of the TWA group on this grid (an ncu capture case)")
     ap.add_argument("--no-solve-run", dest="solve_run", action="store_false",
                     help="skip the full-length polariton solve() measurement")
+    ap.add_argument("--plain-steps", type=int, default=20,
+                    help="steps of the plain cuFFT split step timed beside the fused passes (0 skips it)")
     ap.add_argument("--anchor-steps", type=int, default=200,
                     help="steps of the scalar Kerr 1024^2 FP64 measurement (0 skips it)")
     ap.add_argument("--precision-sweep", action="store_true",
