@@ -25,6 +25,8 @@ GPE_C128 = 0
 GPE_C64 = 1
 GPE_FLAG_FP64_NATIVE = 1
 GPE_FLAG_NO_RESIDENT = 2
+GPE_FLAG_NO_TMA = 4
+GPE_FLAG_TMA = 8
 GPE_TABLE_NONE, GPE_TABLE_SCALAR, GPE_TABLE_DIAG, GPE_TABLE_MATRIX = 0, 1, 2, 3
 GPE_NOISE_OFF, GPE_NOISE_PHILOX, GPE_NOISE_REPLAY = 0, 1, 2
 
@@ -104,6 +106,7 @@ SIGNATURES = {
     "gpe_set_graph": (c_int, [H, c_int64]),
     "gpe_run_async": (c_int, [H, c_int64]),
     "gpe_wait": (c_int, [H]),
+    "gpe_selftest_wait": (c_int, [c_int, c_int, c_int64]),
     "gpe_ensemble_create": (c_int, [c_void_p, c_int, POINTER(c_void_p)]),
     "gpe_ensemble_run": (c_int, [c_void_p, c_int64, c_int64]),
     "gpe_ensemble_destroy": (c_int, [c_void_p]),

@@ -1,7 +1,9 @@
 // convert.cu -- small device utilities: FP64 <-> double-word conversion of complex
-// arrays, and the step-counter advance that ends a captured chunk of steps.
+// arrays, the step-counter advance that ends a captured chunk of steps, and the probe of
+// the bounded mbarrier wait.
 #include "dw.cuh"
 #include "kernels.h"
+#include "tma.cuh"
 
 namespace gpe {
 
@@ -22,6 +24,27 @@ __global__ void dw_to_f64_kernel(const dwc* __restrict__ src, double2* __restric
 
 __global__ void advance_kernel(int64_t* k, int64_t n) {
   if (threadIdx.x == 0 && blockIdx.x == 0) *k += n;
+}
+
+// One CTA waits on an mbarrier of one expected arrival, with the same bounded wait the
+// TMA column pass uses.  arrive = 0: nothing arrives, so the wait runs out after limit_ns
+// and the kernel stores 1 in *status; arrive = 1: thread 0 arrives first and the wait
+// completes at once.
+__global__ void wait_probe_kernel(int arrive, uint64_t limit_ns, int32_t* status) {
+  __shared__ uint64_t bar;
+  if (threadIdx.x == 0) {
+    mbar_init(&bar, 1);
+    mbar_init_fence();
+  }
+  __syncthreads();
+  if (arrive && threadIdx.x == 0) asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_addr(&bar)) : "memory");
+  const bool ok = mbar_wait(&bar, 0, limit_ns);
+  if (__syncthreads_or(!ok) && threadIdx.x == 0) atomicExch(status, 1);
+}
+
+int launch_wait_probe(int arrive, uint64_t limit_ns, int32_t* status, cudaStream_t s) {
+  wait_probe_kernel<<<1, 32, 0, s>>>(arrive, limit_ns, status);
+  return (int)cudaGetLastError();
 }
 
 int launch_advance(int64_t* k, int64_t n, cudaStream_t s) {

@@ -132,6 +132,9 @@ struct gpe_handle {
   void* conv_buf = nullptr;  // FP64 staging of double-word fields on their way to the host
   size_t conv_cap = 0;
   double* red = nullptr;  // reduction scratch (4 doubles)
+  // status word in mapped host memory: a kernel whose bounded wait ran out stores 1
+  int32_t* hstat = nullptr;
+  int32_t* dstat = nullptr;
   double last_ms = 0.0;
   int64_t last_launches = 0;
   // per-launch timing (gpe_set_timing)
@@ -384,6 +387,12 @@ int gpe_create(const gpe_desc* desc, gpe_handle** out) {
     fail(nullptr, GPE_ERR_NOMEM, "cudaMalloc failed: %s", cudaGetErrorString(e));
     return bail(GPE_ERR_NOMEM);
   }
+  if ((e = cudaHostAlloc((void**)&h->hstat, sizeof(int32_t), cudaHostAllocMapped)) != cudaSuccess ||
+      (e = cudaHostGetDevicePointer((void**)&h->dstat, h->hstat, 0)) != cudaSuccess) {
+    fail(nullptr, GPE_ERR_NOMEM, "mapped status word: %s", cudaGetErrorString(e));
+    return bail(GPE_ERR_NOMEM);
+  }
+  *h->hstat = 0;
   // twiddles w_N^k = exp(-2 pi i k / N) per axis, built in FP64
   for (int a = 0; a < h->ndim; ++a) {
     const int64_t N = h->n[a];
@@ -421,6 +430,7 @@ int gpe_destroy(gpe_handle* h) {
   cudaFree(h->xi_buf);
   cudaFree(h->conv_buf);
   cudaFree(h->red);
+  if (h->hstat) cudaFreeHost(h->hstat);
   for (cudaEvent_t e : h->evpool) cudaEventDestroy(e);
   if (h->ev0) cudaEventDestroy(h->ev0);
   if (h->ev1) cudaEventDestroy(h->ev1);
@@ -765,6 +775,8 @@ static PassArgs base_args(gpe_handle* h) {
   a.P = h->P;
   a.B = h->B;
   a.nsm = h->nsm;
+  a.col_tma = (h->d.flags & GPE_FLAG_NO_TMA) ? 0 : (h->d.flags & GPE_FLAG_TMA) ? 1 : 2;
+  a.status = h->dstat;
   for (int m = 0; m < h->M; ++m) a.u[m] = h->u[m];
   a.ktab = h->ktab;
   a.kkind = h->kkind;
@@ -1188,6 +1200,14 @@ static int replay_graph(gpe_handle* h, int64_t nsteps, int64_t* launches) {
   return GPE_OK;
 }
 
+// A device wait that ran out of time left 1 in the status word: report it once.
+static int take_status(gpe_handle* h) {
+  if (!h->hstat || !*(volatile int32_t*)h->hstat) return GPE_OK;
+  *(volatile int32_t*)h->hstat = 0;
+  return fail(h, GPE_ERR_TIMEOUT, "a device wait exceeded its limit (a TMA tile did not arrive); the results of this "
+                                  "run are not valid");
+}
+
 static int run_common(gpe_handle* h, int64_t nsteps, int64_t save_every, void* out, bool out_is_dev, double* ts_out,
                       const void* xi_host, int64_t comp_stride = -1) {
   if (!h) return GPE_ERR_INVALID;
@@ -1276,6 +1296,7 @@ static int run_common(gpe_handle* h, int64_t nsteps, int64_t save_every, void* o
   }
   CK(h, cudaEventRecord(h->ev1, h->stream));
   CK(h, cudaEventSynchronize(h->ev1));
+  if (int rc = take_status(h)) return rc;
   float ms = 0.f;
   cudaEventElapsedTime(&ms, h->ev0, h->ev1);
   h->last_ms = ms;
@@ -1376,6 +1397,7 @@ static int transform_copy(gpe_handle* h) {
   f.ktab = nullptr;
   f.noise = 0;
   f.hA = f.hB = -1;
+  f.col_tma = 0;  // diagnostics: plain loads, no device wait
   PassArgs r = f;
   r.tw = h->tw[0];
   r.do_fft = 1;
@@ -1486,7 +1508,23 @@ int gpe_wait(gpe_handle* h) {
   CK(h, cudaSetDevice(h->dev));
   CK(h, cudaStreamSynchronize(h->stream));
   CK(h, cudaGetLastError());
-  return GPE_OK;
+  return take_status(h);
+}
+
+int gpe_selftest_wait(int device, int arrive, int64_t limit_ns) {
+  if (limit_ns < 0) return GPE_ERR_INVALID;
+  if (cudaSetDevice(device < 0 ? 0 : device) != cudaSuccess) return GPE_ERR_CUDA;
+  int32_t *hs = nullptr, *ds = nullptr;
+  if (cudaHostAlloc((void**)&hs, sizeof(int32_t), cudaHostAllocMapped) != cudaSuccess) return GPE_ERR_NOMEM;
+  int rc = GPE_OK;
+  *hs = 0;
+  if (cudaHostGetDevicePointer((void**)&ds, hs, 0) != cudaSuccess ||
+      gpe::launch_wait_probe(arrive ? 1 : 0, (uint64_t)limit_ns, ds, 0) != 0 || cudaDeviceSynchronize() != cudaSuccess)
+    rc = GPE_ERR_CUDA;
+  else if (*(volatile int32_t*)hs)
+    rc = GPE_ERR_TIMEOUT;
+  cudaFreeHost(hs);
+  return rc;
 }
 
 int gpe_set_timing(gpe_handle* h, int on) {
@@ -1655,6 +1693,8 @@ int gpe_ensemble_run(gpe_ensemble* e, int64_t nsteps, int64_t steps_per_graph) {
   cudaEventRecord(e->ev1, h0->stream);
   const cudaError_t es = cudaEventSynchronize(e->ev1);
   if (es != cudaSuccess) return efail(e, GPE_ERR_CUDA, cudaGetErrorString(es));
+  for (gpe_handle* h : e->hs)
+    if (take_status(h)) return efail(e, GPE_ERR_TIMEOUT, "a device wait exceeded its limit in a group");
   float ms = 0.f;
   cudaEventElapsedTime(&ms, e->ev0, e->ev1);
   e->last_ms = ms;

@@ -72,6 +72,11 @@ struct PassArgs {
   // columns at outer index o (offset o*ostride) of trajectory b
   int64_t ld, ostride, nouter;
   int32_t col_fwd, col_inv;
+  // TMA staging of 2D column tiles: 0 never, 1 wherever the shape and shared memory
+  // allow, 2 by the measured rule (one-component lines of at most 512 points)
+  int32_t col_tma;
+  // host-mapped status word: a device wait that ran out of time stores 1 here
+  int32_t* status;
 };
 
 // Pass precisions: native FP64, FP32, double-word FP64 on the FP32 pipes.
@@ -99,6 +104,9 @@ int launch_energy_sums(int prec, int M, const void* const* uk, const void* const
 // the matrix (1/B) sum_b nb[b][k] nb[b][k']
 int launch_spectral_moments(int prec, const void* uk, int64_t P, int64_t B, double* nb, double* mean, double* second,
                             cudaStream_t s);
+// bounded-wait probe: one CTA waits on an mbarrier that (arrive = 0) nothing completes;
+// *status = 1 when the wait ran out after limit_ns
+int launch_wait_probe(int arrive, uint64_t limit_ns, int32_t* status, cudaStream_t s);
 // *k += n on the device (end of a captured chunk of n steps)
 int launch_advance(int64_t* k, int64_t n, cudaStream_t s);
 // FP64 <-> double-word conversion of n complex numbers

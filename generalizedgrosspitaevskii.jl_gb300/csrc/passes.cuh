@@ -16,6 +16,12 @@
 #include "fft.cuh"
 #include "kernels.h"
 #include "philox.cuh"
+#include "tma.cuh"
+
+#include <cudaTypedefs.h>
+
+#include <algorithm>
+#include <climits>
 
 namespace gpe {
 
@@ -717,32 +723,18 @@ row_kernel(const PassArgs a, const int64_t nlines, const int lb) {
 }
 
 // ------------------------------------------------------------------ column pass
-template <typename Real, int LOGN, int M, int V = 0>
-__global__ void __launch_bounds__(LineCfg<Real, M, LOGN, V>::COL_THREADS, LineCfg<Real, M, LOGN, V>::COL_MINB)
-col_kernel(const PassArgs a) {
+// The work on one tile held in registers: FFT_y, the k-space table, iFFT_y (one FFT
+// instance: the phase loop is not unrolled).  sp0: spatial index of this thread's first
+// point, step: index distance between its points.
+template <typename Real, int LOGN, int M, int V>
+__device__ __forceinline__ void col_tile_work(typename CT<Real>::T (&x)[M][LineCfg<Real, M, LOGN, V>::E],
+                                              const PassArgs& a, int t,
+                                              const ColLayout<typename CT<Real>::T, LineCfg<Real, M, LOGN, V>::CC>& lay,
+                                              int64_t sp0, int64_t step) {
   using Cfg = LineCfg<Real, M, LOGN, V>;
   using C = typename CT<Real>::T;
-  constexpr int N = Cfg::N, E = Cfg::E, T = Cfg::T, CC = Cfg::CC;
-  extern __shared__ __align__(16) unsigned char smraw[];
-  C* sm = reinterpret_cast<C*>(smraw);
-  const int c = threadIdx.x % CC, t = threadIdx.x / CC;
-  int64_t tile = blockIdx.x;
-  const int64_t ntx = a.n0 / CC;
-  const int64_t xt = tile % ntx;
-  tile /= ntx;
-  const int64_t o = tile % a.nouter;
-  const int64_t b = tile / a.nouter;
-  const int64_t sp0 = o * a.ostride + xt * CC + c + (int64_t)t * a.ld;
-  const int64_t g0 = b * a.P + sp0;
-  const int64_t step = (int64_t)T * a.ld;
-  const ColLayout<C, CC> lay{sm + c};
+  constexpr int N = Cfg::N, E = Cfg::E, CC = Cfg::CC;
   const C* tw = (const C*)a.tw;
-  C x[M][E];
-#pragma unroll
-  for (int m = 0; m < M; ++m)
-#pragma unroll
-    for (int i = 0; i < E; ++i) x[m][i] = ((const C*)a.u[m])[g0 + step * i];
-  // phases: 0 forward FFT_y, 1 k-space table, 2 inverse FFT_y (one FFT instance)
 #pragma unroll 1
   for (int ph = 0; ph < 3; ++ph) {
     if (ph != 1) {
@@ -762,10 +754,125 @@ col_kernel(const PassArgs a) {
       }
     }
   }
+}
+
+template <typename Real, int LOGN, int M, int V = 0>
+__global__ void __launch_bounds__(LineCfg<Real, M, LOGN, V>::COL_THREADS, LineCfg<Real, M, LOGN, V>::COL_MINB)
+col_kernel(const PassArgs a) {
+  using Cfg = LineCfg<Real, M, LOGN, V>;
+  using C = typename CT<Real>::T;
+  constexpr int E = Cfg::E, T = Cfg::T, CC = Cfg::CC;
+  extern __shared__ __align__(16) unsigned char smraw[];
+  C* sm = reinterpret_cast<C*>(smraw);
+  const int c = threadIdx.x % CC, t = threadIdx.x / CC;
+  int64_t tile = blockIdx.x;
+  const int64_t ntx = a.n0 / CC;
+  const int64_t xt = tile % ntx;
+  tile /= ntx;
+  const int64_t o = tile % a.nouter;
+  const int64_t b = tile / a.nouter;
+  const int64_t sp0 = o * a.ostride + xt * CC + c + (int64_t)t * a.ld;
+  const int64_t g0 = b * a.P + sp0;
+  const int64_t step = (int64_t)T * a.ld;
+  const ColLayout<C, CC> lay{sm + c};
+  C x[M][E];
+#pragma unroll
+  for (int m = 0; m < M; ++m)
+#pragma unroll
+    for (int i = 0; i < E; ++i) x[m][i] = ((const C*)a.u[m])[g0 + step * i];
+  col_tile_work<Real, LOGN, M, V>(x, a, t, lay, sp0, step);
 #pragma unroll
   for (int m = 0; m < M; ++m)
 #pragma unroll
     for (int i = 0; i < E; ++i) ((C*)a.u[m])[g0 + step * i] = x[m][i];
+}
+
+// Shared-memory plan of the TMA column pass: the FFT exchange, then the staging buffer
+// (1024-byte aligned) holding one tile of every component as TMA writes it (rows of CC
+// points, dense), then the mbarrier.  SLACK covers the alignment of the dynamic base.
+template <typename Real, int M, int LOGN>
+struct ColTmaCfg {
+  using Cfg = LineCfg<Real, M, LOGN, 0>;
+  using C = typename CT<Real>::T;
+  static constexpr int N = Cfg::N, CC = Cfg::CC;
+  static constexpr int XF = CC * (int)sizeof(C) / 4;  // floats per tile row (box width)
+  static constexpr int BOXR = N < 256 ? N : 256;      // rows per box
+  static constexpr size_t EXCH = (Cfg::COL_SMEM + 1023) / 1024 * 1024;
+  static constexpr size_t STAGE = (size_t)M * N * CC * sizeof(C);
+  static constexpr size_t SLACK = 1024;
+  static constexpr size_t SMEM = SLACK + EXCH + STAGE + 16;
+  static constexpr bool OK = XF % 4 == 0 && SMEM <= 227 * 1024 && STAGE < (1u << 20);
+};
+
+// Persistent 2D column pass with TMA staging: CTA k takes tiles k, k + grid, ...; while
+// it transforms one tile, the copy engine brings the next into the staging buffer.
+// tm[m] maps component m as a 2D array of B*n1 rows of n0 points (counted in floats).
+template <typename Real, int LOGN, int M>
+__global__ void __launch_bounds__(LineCfg<Real, M, LOGN, 0>::COL_THREADS, LineCfg<Real, M, LOGN, 0>::COL_MINB)
+col_kernel_tma(const PassArgs a, const __grid_constant__ CUtensorMap tm0, const __grid_constant__ CUtensorMap tm1) {
+  using Cfg = LineCfg<Real, M, LOGN, 0>;
+  using TC = ColTmaCfg<Real, M, LOGN>;
+  using C = typename CT<Real>::T;
+  constexpr int N = Cfg::N, E = Cfg::E, T = Cfg::T, CC = Cfg::CC;
+  extern __shared__ __align__(16) unsigned char smraw[];
+  unsigned char* base = smraw + ((1024u - (smem_addr(smraw) & 1023u)) & 1023u);
+  C* sm = reinterpret_cast<C*>(base);
+  C* stg = reinterpret_cast<C*>(base + TC::EXCH);
+  uint64_t* bar = reinterpret_cast<uint64_t*>(base + TC::EXCH + TC::STAGE);
+  const int c = threadIdx.x % CC, t = threadIdx.x / CC;
+  const int64_t ntx = a.n0 / CC;
+  const int64_t ntiles = ntx * a.B;
+  const int64_t step = (int64_t)T * a.ld;
+  const ColLayout<C, CC> lay{sm + c};
+  auto issue = [&](int64_t tile) {
+    const int64_t xt = tile % ntx, b = tile / ntx;
+    mbar_arrive_expect_tx(bar, (uint32_t)TC::STAGE);
+#pragma unroll
+    for (int m = 0; m < M; ++m)
+#pragma unroll
+      for (int j = 0; j < N / TC::BOXR; ++j)
+        tma_load_2d(stg + ((size_t)m * N + (size_t)j * TC::BOXR) * CC, m == 0 ? &tm0 : &tm1, (int32_t)(xt * TC::XF),
+                    (int32_t)(b * a.n1 + j * TC::BOXR), bar);
+  };
+  if (threadIdx.x == 0) {
+    mbar_init(bar, 1);
+    mbar_init_fence();
+  }
+  __syncthreads();
+  int64_t tile = blockIdx.x;
+  if (threadIdx.x == 0 && tile < ntiles) issue(tile);
+  uint32_t parity = 0;
+  for (; tile < ntiles; tile += gridDim.x) {
+    const bool got = mbar_wait(bar, parity, kWaitLimitNs);
+    if (__syncthreads_or(!got)) {
+      // the tile never arrived: report, and leave only once the copy engine is done
+      // with this CTA's shared memory (again a bounded wait)
+      if (threadIdx.x == 0 && a.status) atomicExch(a.status, 1);
+      if (threadIdx.x == 0) mbar_wait(bar, parity, kWaitLimitNs);
+      __syncthreads();
+      return;
+    }
+    parity ^= 1u;
+    C x[M][E];
+#pragma unroll
+    for (int m = 0; m < M; ++m)
+#pragma unroll
+      for (int i = 0; i < E; ++i) x[m][i] = stg[((size_t)m * N + t + T * i) * CC + c];
+    // staging consumed: the copy engine's writes of the next tile are ordered after these
+    // reads only through the proxy fence (a barrier alone orders ordinary accesses)
+    fence_proxy_async_smem();
+    __syncthreads();
+    const int64_t nxt = tile + gridDim.x;
+    if (nxt < ntiles && threadIdx.x == 0) issue(nxt);
+    const int64_t xt = tile % ntx, b = tile / ntx;
+    const int64_t sp0 = xt * CC + c + (int64_t)t * a.ld;
+    const int64_t g0 = b * a.P + sp0;
+    col_tile_work<Real, LOGN, M, 0>(x, a, t, lay, sp0, step);
+#pragma unroll
+    for (int m = 0; m < M; ++m)
+#pragma unroll
+      for (int i = 0; i < E; ++i) ((C*)a.u[m])[g0 + step * i] = x[m][i];
+  }
 }
 
 // ------------------------------------------------------------------ 1D resident
@@ -1146,10 +1253,83 @@ int launch_row_n(const PassArgs& a, int64_t nlines, cudaStream_t s) {
   k<<<(unsigned)blocks, lb * Cfg::TR, smem, s>>>(a, nlines, lb);
   return (int)cudaGetLastError();
 }
+// cuTensorMapEncodeTiled from the driver, looked up once through the runtime (no link
+// against libcuda); null when the driver does not provide it
+inline PFN_cuTensorMapEncodeTiled_v12000 tensor_map_encoder() {
+  static PFN_cuTensorMapEncodeTiled_v12000 fn = [] {
+    void* p = nullptr;
+    cudaDriverEntryPointQueryResult q{};
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) != cudaSuccess ||
+        q != cudaDriverEntryPointSuccess)
+      p = nullptr;
+    return reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(p);
+  }();
+  return fn;
+}
+
+// Tensor map of one component for the TMA column pass: rows of `row_floats` floats,
+// `rows` rows, box of box_x floats by box_y rows, no swizzle.
+inline bool encode_rows_map(CUtensorMap* tm, const void* base, uint64_t row_floats, uint64_t rows, uint32_t box_x,
+                            uint32_t box_y) {
+  auto enc = tensor_map_encoder();
+  if (!enc || ((uintptr_t)base & 15) || (row_floats * 4) % 16) return false;
+  const cuuint64_t dims[2] = {row_floats, rows};
+  const cuuint64_t strides[1] = {row_floats * 4};
+  const cuuint32_t box[2] = {box_x, box_y};
+  const cuuint32_t es[2] = {1, 1};
+  return enc(tm, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, const_cast<void*>(base), dims, strides, box, es,
+             CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+             CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
+
+// TMA column pass for a 2D field (lines along y of length N = n1, stride n0); returns
+// -1 when this shape does not take it (the caller then launches col_kernel)
+template <typename Real, int M, int LOGN>
+int launch_col_tma_n(const PassArgs& a, cudaStream_t s) {
+  using Cfg = LineCfg<Real, M, LOGN, 0>;
+  using TC = ColTmaCfg<Real, M, LOGN>;
+  using C = typename CT<Real>::T;
+  if constexpr (!TC::OK) {
+    return -1;
+  } else {
+    if (a.nouter != 1 || a.ld != a.n0 || a.n1 != Cfg::N || a.n0 % Cfg::CC || a.B * (int64_t)a.n1 > INT32_MAX) return -1;
+    // measured on GB300 (ms per column pass, plain -> TMA): one component 0.139 -> 0.135
+    // (256^2 x 341, FP32), 0.107 -> 0.104 (512^2 x 16, double-word), 0.193 -> 0.191 (512^2
+    // x 64, FP32); two components 0.796 -> 0.817 (512^2 x 64, double-word), 0.412 -> 0.479
+    // (512^2 x 128, FP32, one CTA per SM instead of two); 1024-point FP32 lines 0.214 -> 0.221
+    if (a.col_tma == 2 && (M != 1 || Cfg::N > 512)) return -1;
+    CUtensorMap tm[2];
+    const uint64_t row_floats = (uint64_t)a.n0 * sizeof(C) / 4;
+    for (int m = 0; m < M; ++m)
+      if (!encode_rows_map(&tm[m], a.u[m], row_floats, (uint64_t)a.B * a.n1, TC::XF, TC::BOXR)) return -1;
+    if (M == 1) tm[1] = tm[0];
+    auto k = col_kernel_tma<Real, LOGN, M>;
+    int e = set_smem(k, TC::SMEM);
+    if (e) return e;
+    static int per_sm = 0;  // resident CTAs per SM (one value per instantiation)
+    if (per_sm == 0) {
+      int v = 0;
+      if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&v, k, Cfg::COL_THREADS, TC::SMEM) != cudaSuccess || v < 1)
+        v = 1;
+      per_sm = v;
+    }
+    const int64_t ntiles = (int64_t)(a.n0 / Cfg::CC) * a.B;
+    const int64_t grid = std::min<int64_t>(ntiles, (int64_t)per_sm * (a.nsm > 0 ? a.nsm : 152));
+    k<<<(unsigned)grid, Cfg::COL_THREADS, TC::SMEM, s>>>(a, tm[0], tm[1]);
+    return (int)cudaGetLastError();
+  }
+}
+
 template <typename Real, int M, int LOGN, int V = 0>
 int launch_col_n(const PassArgs& a, cudaStream_t s) {
   using Cfg = LineCfg<Real, M, LOGN, V>;
   if (a.n0 % Cfg::CC) return (int)cudaErrorInvalidValue;
+  if constexpr (V == 0) {
+    if (a.col_tma) {
+      const int r = launch_col_tma_n<Real, M, LOGN>(a, s);
+      if (r >= 0) return r;
+    }
+  }
   auto k = col_kernel<Real, LOGN, M, V>;
   int e = set_smem(k, Cfg::COL_SMEM);
   if (e) return e;

@@ -67,7 +67,8 @@ class StrangSplittingIterator:
 
     def __init__(self, prob: GrossPitaevskiiProblem, tspan, *, dt, nsaves, save_start=True, rng=None,
                  noise_replay: Optional[Callable] = None, total_steps: Optional[int] = None,
-                 device: int = -1, fp64: str = "dw", resident: bool = True, variant: Optional[int] = None):
+                 device: int = -1, fp64: str = "dw", resident: bool = True, variant: Optional[int] = None,
+                 tma: Optional[bool] = None):
         self.lib = L.load()
         self.variant = variant
         self.prob = prob
@@ -97,7 +98,8 @@ class StrangSplittingIterator:
         d.device = device
         if fp64 not in ("dw", "native"):
             raise ValueError("fp64 must be 'dw' (double-word on the FP32 pipes) or 'native'")
-        d.flags = (L.GPE_FLAG_FP64_NATIVE if fp64 == "native" else 0) | (0 if resident else L.GPE_FLAG_NO_RESIDENT)
+        d.flags = ((L.GPE_FLAG_FP64_NATIVE if fp64 == "native" else 0) | (0 if resident else L.GPE_FLAG_NO_RESIDENT)
+                   | (0 if tma is None else L.GPE_FLAG_TMA if tma else L.GPE_FLAG_NO_TMA))
         h = ctypes.c_void_p()
         rc = self.lib.gpe_create(ctypes.byref(d), ctypes.byref(h))
         L.check(self.lib, None, rc)
@@ -255,7 +257,7 @@ class StrangSplittingIterator:
 
 def init(prob: GrossPitaevskiiProblem, alg: StrangSplitting, tspan, *, dt, nsaves, show_progress=False,
          progress=None, save_start=True, workgroup_size=(), rng=None, noise_replay=None, fp64="dw", device=-1,
-         resident=True, variant=None):
+         resident=True, variant=None, tma=None):
     """init(prob, StrangSplitting(), tspan; dt, nsaves, ...) (src/strang_splitting.jl:32-67).
     show_progress / progress / workgroup_size are accepted for signature parity and
     have no effect: the backend picks its own launch shapes.  Extra keywords: ``rng``
@@ -264,12 +266,13 @@ def init(prob: GrossPitaevskiiProblem, alg: StrangSplitting, tspan, *, dt, nsave
     FP32 pipes, the default; "native": FP64 instructions), ``device`` (CUDA ordinal),
     ``resident`` (False forces the two-pass HBM path for small square 2D grids),
     ``variant`` (line tiling of the two-pass passes, see gpe_set_variant; None lets the
-    library choose by field size)."""
+    library choose by field size), ``tma`` (TMA staging of 2D column tiles: True wherever
+    it fits, False never, None by the library's measured rule)."""
     if not isinstance(alg, StrangSplitting):
         raise TypeError("the only algorithm is StrangSplitting()")
     return StrangSplittingIterator(prob, tspan, dt=dt, nsaves=nsaves, save_start=save_start, rng=rng,
                                    noise_replay=noise_replay, fp64=fp64, device=device, resident=resident,
-                                   variant=variant)
+                                   variant=variant, tma=tma)
 
 
 def solve(prob: GrossPitaevskiiProblem, alg: StrangSplitting, tspan, **kwargs):

@@ -89,10 +89,11 @@ class Ensemble:
 
 
 def make_group(N: int, ntraj: int, prm: DampedDrivenParams, nsteps: int, seed: int, dtype=np.complex64,
-               resident: bool = True, noise_seed: Optional[int] = None, variant: int = 0) -> StrangSplittingIterator:
+               resident: bool = True, noise_seed: Optional[int] = None, variant: int = 0,
+               tma: Optional[bool] = None) -> StrangSplittingIterator:
     prob = wigner_problem(N, ntraj, prm, seed, dtype)
     return StrangSplittingIterator(prob, (0.0, nsteps * prm.dt), dt=prm.dt, nsaves=1, rng=noise_seed or seed + 1,
-                                   resident=resident, variant=variant)
+                                   resident=resident, variant=variant, tma=tma)
 
 
 def density_moments(it: StrangSplittingIterator):

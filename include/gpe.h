@@ -59,6 +59,15 @@ extern "C" {
  * component, 16-byte types up to 64x64) run every step of a gpe_run call in one resident
  * launch, one CTA per trajectory.  This flag forces the two-pass HBM path instead. */
 #define GPE_FLAG_NO_RESIDENT 2
+/* 2D column passes can stage each tile of columns into shared memory with the tensor
+ * memory accelerator (cp.async.bulk.tensor), the next tile landing while the current one
+ * is transformed.  By default they do so for one-component lines of at most 512 points
+ * (measured faster there; two-component tiles are faster with plain per-thread loads).
+ * GPE_FLAG_NO_TMA keeps plain loads everywhere; GPE_FLAG_TMA stages wherever the shape
+ * and shared memory allow.  A tile that does not arrive within 1 s makes the run return
+ * GPE_ERR_TIMEOUT. */
+#define GPE_FLAG_NO_TMA 4
+#define GPE_FLAG_TMA 8
 
 /* table kinds: what the user closure returned per grid point */
 #define GPE_TABLE_NONE 0
@@ -213,6 +222,12 @@ int gpe_set_variant(gpe_handle* h, int variant);
  * gpe_wait blocks until they are done. */
 int gpe_run_async(gpe_handle* h, int64_t nsteps);
 int gpe_wait(gpe_handle* h);
+
+/* Probe of the bounded device wait the TMA column pass relies on: one CTA waits on an
+ * mbarrier with limit_ns as its limit.  arrive = 0: nothing completes the barrier, the
+ * wait runs out and the call returns GPE_ERR_TIMEOUT with the context still usable;
+ * arrive = 1: the barrier completes and the call returns GPE_OK. */
+int gpe_selftest_wait(int device, int arrive, int64_t limit_ns);
 /* Several handles (e.g. trajectory groups on grids of different sizes) advanced together
  * by ONE captured CUDA graph: each handle's chunk of steps_per_graph steps runs on its own
  * stream inside the graph (small square grids as one resident launch, larger ones as
