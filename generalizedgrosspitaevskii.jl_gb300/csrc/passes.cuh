@@ -21,6 +21,7 @@
 #include <cudaTypedefs.h>
 
 #include <algorithm>
+#include <atomic>
 #include <climits>
 
 namespace gpe {
@@ -1306,12 +1307,15 @@ int launch_col_tma_n(const PassArgs& a, cudaStream_t s) {
     auto k = col_kernel_tma<Real, LOGN, M>;
     int e = set_smem(k, TC::SMEM);
     if (e) return e;
-    static int per_sm = 0;  // resident CTAs per SM (one value per instantiation)
+    // resident CTAs per SM, queried once per instantiation (the kernel's registers and
+    // shared memory decide it, not the field)
+    static std::atomic<int> per_sm_cache{0};
+    int per_sm = per_sm_cache.load(std::memory_order_relaxed);
     if (per_sm == 0) {
-      int v = 0;
-      if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&v, k, Cfg::COL_THREADS, TC::SMEM) != cudaSuccess || v < 1)
-        v = 1;
-      per_sm = v;
+      if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k, Cfg::COL_THREADS, TC::SMEM) != cudaSuccess ||
+          per_sm < 1)
+        per_sm = 1;
+      per_sm_cache.store(per_sm, std::memory_order_relaxed);
     }
     const int64_t ntiles = (int64_t)(a.n0 / Cfg::CC) * a.B;
     const int64_t grid = std::min<int64_t>(ntiles, (int64_t)per_sm * (a.nsm > 0 ? a.nsm : 152));
