@@ -788,6 +788,57 @@ def run_twa_breakdown(args):
     print(json.dumps({"metric": "TWA per-group step time", "groups": out}), flush=True)
 
 
+def run_pass_breakdown(args):
+    """Where the row pass spends its time: the same passes on problems that drop one
+    term at a time (noise, pump, nonlinearity), event-timed per launch over 50 steps.
+    Trajectory group: 256^2 x 341 one-component FP32 fields (D = |k|^2/2 - 0.1i, G =
+    0.01|u|^2, constant pump 1, noise 0.3); polariton: 512^2 two-component fields (the
+    benchmark's 2x2 dispersion and G, Gaussian photon pump), 128 copies in FP32 and 64
+    in double-word FP64.  One JSON line."""
+    import __graft_entry__ as G
+    gpe = G.load_package()
+    L = sys.modules["gpe_gb300._lib"]
+
+    def timed(prob, dt):
+        it = gpe.StrangSplittingIterator(prob, (0.0, 1000 * dt), dt=dt, nsaves=1, device=0, resident=False, rng=5)
+        it.step(5)
+        lib = it.lib
+        L.check(lib, it.h, lib.gpe_set_timing(it.h, 1))
+        L.check(lib, it.h, lib.gpe_run(it.h, 50, 0, None, None))
+        kms = np.zeros(3)
+        kn = np.zeros(3, np.int64)
+        L.check(lib, it.h, lib.gpe_kernel_times(it.h, L.ptr(kms), L.ptr(kn)))
+        it.close()
+        return {"row_ms": float(kms[0] / kn[0]), "col_ms": float(kms[1] / kn[1])}
+
+    rng = np.random.default_rng(0)
+    out = []
+    N, B = 256, 341
+    u0 = np.asfortranarray((1 + 0.3 * (rng.standard_normal((N, N, B)) + 1j * rng.standard_normal((N, N, B))))
+                           .astype(np.complex64))
+    nl = lambda u, p: 0.01 * np.abs(u[0]) ** 2
+    cases = [("all terms", dict(nonlinearity=nl, pump=lambda r, p, t: 1.0 + 0 * r[0],
+                                position_noise_func=lambda u, r, p: 0.3)),
+             ("no noise", dict(nonlinearity=nl, pump=lambda r, p, t: 1.0 + 0 * r[0])),
+             ("no noise, no pump", dict(nonlinearity=nl)),
+             ("transforms only", dict())]
+    for name, kw in cases:
+        prob = gpe.GrossPitaevskiiProblem((u0,), (64.0, 64.0), dispersion=lambda k, p: (k[0] ** 2 + k[1] ** 2) / 2 - 0.1j,
+                                          **kw)
+        out.append({"workload": "256^2 x 341, one component, FP32", "case": name, **timed(prob, 0.02)})
+    disp, nonl, pump = polariton_closures()
+    for dtype, B2 in ((np.complex64, 128), (np.complex128, 64)):
+        z = [np.asfortranarray((0.1 * (rng.standard_normal((N_GRID, N_GRID, B2)) + 1j * rng.standard_normal(
+            (N_GRID, N_GRID, B2)))).astype(dtype)) for _ in range(2)]
+        pump_now = lambda r, p, t: pump(r, p, 100.0)  # a constant amplitude, half the ramp's end value
+        for name, kw in (("all terms", dict(nonlinearity=nonl, pump=pump_now)), ("no pump", dict(nonlinearity=nonl)),
+                         ("transforms only", dict())):
+            prob = gpe.GrossPitaevskiiProblem(tuple(z), (L_BOX, L_BOX), dispersion=disp, **kw)
+            out.append({"workload": f"polariton 512^2 x {B2}, " + ("FP32" if dtype == np.complex64 else "double-word"),
+                        "case": name, **timed(prob, DT)})
+    print(json.dumps({"metric": "pass time by term", "runs": out}), flush=True)
+
+
 def run_twa_group_steps(args):
     """A handful of plain steps of one TWA group (the capture case for ncu)."""
     import __graft_entry__ as G
@@ -817,6 +868,8 @@ def main():
                     help="steps of the batched truncated-Wigner ensemble measurement (0 skips it)")
     ap.add_argument("--no-tune", action="store_true", help="skip the ensemble autotuner")
     ap.add_argument("--twa-breakdown", action="store_true", help="print per-group TWA step times instead")
+    ap.add_argument("--pass-breakdown", action="store_true",
+                    help="print the row / column pass times of problems that drop one term at a time")
     ap.add_argument("--twa-group", type=int, default=0,
                     help="run --steps plain steps of the TWA group on this grid (an ncu capture case)")
     ap.add_argument("--no-solve-run", dest="solve_run", action="store_false",
@@ -853,6 +906,10 @@ def main():
     if args.twa_group:
         if rank == 0:
             run_twa_group_steps(args)
+        return
+    if args.pass_breakdown:
+        if rank == 0:
+            run_pass_breakdown(args)
         return
     if args.impl == "reference":
         run_reference(args, rank, world)
