@@ -802,6 +802,9 @@ def run_pass_breakdown(args):
     def timed(prob, dt):
         it = gpe.StrangSplittingIterator(prob, (0.0, 1000 * dt), dt=dt, nsaves=1, device=0, resident=False, rng=5)
         it.step(5)
+        if args.pass_case >= 0:  # one case, a few steps: a capture for ncu
+            it.close()
+            return {}
         lib = it.lib
         L.check(lib, it.h, lib.gpe_set_timing(it.h, 1))
         L.check(lib, it.h, lib.gpe_run(it.h, 50, 0, None, None))
@@ -822,10 +825,15 @@ def run_pass_breakdown(args):
              ("no noise", dict(nonlinearity=nl, pump=lambda r, p, t: 1.0 + 0 * r[0])),
              ("no noise, no pump", dict(nonlinearity=nl)),
              ("transforms only", dict())]
-    for name, kw in cases:
+    for ci, (name, kw) in enumerate(cases):
+        if args.pass_case >= 0 and ci != args.pass_case:
+            continue
         prob = gpe.GrossPitaevskiiProblem((u0,), (64.0, 64.0), dispersion=lambda k, p: (k[0] ** 2 + k[1] ** 2) / 2 - 0.1j,
                                           **kw)
         out.append({"workload": "256^2 x 341, one component, FP32", "case": name, **timed(prob, 0.02)})
+    if args.pass_case >= 0:
+        print(json.dumps({"metric": "pass time by term", "runs": out}), flush=True)
+        return
     disp, nonl, pump = polariton_closures()
     for dtype, B2 in ((np.complex64, 128), (np.complex128, 64)):
         z = [np.asfortranarray((0.1 * (rng.standard_normal((N_GRID, N_GRID, B2)) + 1j * rng.standard_normal(
@@ -870,6 +878,8 @@ def main():
     ap.add_argument("--twa-breakdown", action="store_true", help="print per-group TWA step times instead")
     ap.add_argument("--pass-breakdown", action="store_true",
                     help="print the row / column pass times of problems that drop one term at a time")
+    ap.add_argument("--pass-case", type=int, default=-1,
+                    help="with --pass-breakdown: run only trajectory case K (0-3) for a few steps, untimed")
     ap.add_argument("--twa-group", type=int, default=0,
                     help="run --steps plain steps of the TWA group on this grid (an ncu capture case)")
     ap.add_argument("--no-solve-run", dest="solve_run", action="store_false",
