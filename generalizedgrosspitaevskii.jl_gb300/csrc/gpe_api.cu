@@ -93,6 +93,7 @@ struct gpe_handle {
   double dV = 1.0;
   cudaStream_t stream = nullptr;
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+  cudaEvent_t ev_ext = nullptr;  // orders the handle's stream after the legacy default stream
   void* u[2] = {nullptr, nullptr};
   void* tw[3] = {nullptr, nullptr, nullptr};
   void* ktab = nullptr;
@@ -434,6 +435,7 @@ int gpe_destroy(gpe_handle* h) {
   for (cudaEvent_t e : h->evpool) cudaEventDestroy(e);
   if (h->ev0) cudaEventDestroy(h->ev0);
   if (h->ev1) cudaEventDestroy(h->ev1);
+  if (h->ev_ext) cudaEventDestroy(h->ev_ext);
   if (h->stream) cudaStreamDestroy(h->stream);
   delete h;
   return GPE_OK;
@@ -503,10 +505,22 @@ int gpe_get_field(gpe_handle* h, int comp, void* host) {
   return GPE_OK;
 }
 
+// Caller-owned device buffers are usually written and read by work on the device's
+// legacy default stream (PyTorch's default).  The handle's stream does not synchronise
+// with it, so copies to or from such a buffer first wait for the work queued there.
+static int after_legacy_stream(gpe_handle* h) {
+  if (!h->ev_ext) CK(h, cudaEventCreateWithFlags(&h->ev_ext, cudaEventDisableTiming));
+  CK(h, cudaEventRecord(h->ev_ext, cudaStreamLegacy));
+  CK(h, cudaStreamWaitEvent(h->stream, h->ev_ext, 0));
+  return GPE_OK;
+}
+
 int gpe_set_field_dev(gpe_handle* h, int comp, const void* dev) {
   int rc = check_comp(h, comp);
   if (rc) return rc;
   if (!dev) return fail(h, GPE_ERR_INVALID, "null field");
+  CK(h, cudaSetDevice(h->dev));
+  if ((rc = after_legacy_stream(h))) return rc;
   if (h->prec == gpe::PREC_DW) {
     LK(h, gpe::launch_f64_to_dw(dev, h->u[comp], h->P * h->B, h->stream));
   } else {
@@ -520,6 +534,8 @@ int gpe_get_field_dev(gpe_handle* h, int comp, void* dev) {
   int rc = check_comp(h, comp);
   if (rc) return rc;
   if (!dev) return fail(h, GPE_ERR_INVALID, "null destination");
+  CK(h, cudaSetDevice(h->dev));
+  if ((rc = after_legacy_stream(h))) return rc;
   if (h->prec == gpe::PREC_DW) {
     LK(h, gpe::launch_dw_to_f64(h->u[comp], dev, h->P * h->B, h->stream));
   } else {
@@ -1252,6 +1268,7 @@ static int run_common(gpe_handle* h, int64_t nsteps, int64_t save_every, void* o
   SaveRing ring{h, comp_stride, plane_bytes, (char*)out};
   if (nsaves > 0) {
     if (out_is_dev) {
+      if (int rc = after_legacy_stream(h)) return rc;
       save_dev = out;
     } else {
       const int64_t slots = use_ring ? kSaveRing : nsaves;

@@ -120,7 +120,10 @@ const char* gpe_version(void);
  * batch*P complex numbers of the handle's precision, layout [batch][z][y][x]. */
 int gpe_set_field(gpe_handle* h, int comp, const void* host);
 int gpe_get_field(gpe_handle* h, int comp, void* host);
-/* Same with device pointers the caller owns (e.g. a torch tensor's data_ptr()). */
+/* Same with device pointers the caller owns (e.g. a torch tensor's data_ptr()).  The
+ * copy waits for the work already queued on the device's legacy default stream (where
+ * PyTorch writes and reads by default); a caller that fills or reads the buffer on
+ * another stream synchronises that stream first. */
 int gpe_set_field_dev(gpe_handle* h, int comp, const void* dev);
 int gpe_get_field_dev(gpe_handle* h, int comp, void* dev);
 
