@@ -152,6 +152,16 @@ struct gpe_handle {
   int64_t kval = 0;
   cudaGraphExec_t gexec = nullptr;
   int64_t glaunches = 0;
+  // every setter that changes what the passes read (tables, coefficients, pump, noise,
+  // tiling, RNG key) bumps gen; a captured graph holds the kernel arguments of the
+  // generation it was captured in and is recaptured when gen moves on
+  int64_t gen = 0;
+  int64_t gexec_gen = -1;
+  // save chunks as graphs (one per ring slot): save_every steps between two saves, the
+  // last row pass writing the save into its slot; key (steps, save buffer, gen)
+  cudaGraphExec_t sgexec[4] = {nullptr, nullptr, nullptr, nullptr};
+  int64_t sg_steps = 0, sg_gen = -1, sg_launches = 0;
+  void* sg_buf = nullptr;
   // energy diagnostics: transformed copy of the state, FP64 D and V samples on the device
   void* escr[2] = {nullptr, nullptr};
   double2* dsamp = nullptr;
@@ -436,6 +446,9 @@ int gpe_destroy(gpe_handle* h) {
   if (h->ev0) cudaEventDestroy(h->ev0);
   if (h->ev1) cudaEventDestroy(h->ev1);
   if (h->ev_ext) cudaEventDestroy(h->ev_ext);
+  if (h->gexec) cudaGraphExecDestroy(h->gexec);
+  for (cudaGraphExec_t& g : h->sgexec)
+    if (g) cudaGraphExecDestroy(g);
   if (h->stream) cudaStreamDestroy(h->stream);
   delete h;
   return GPE_OK;
@@ -563,6 +576,7 @@ static int store_ktable(gpe_handle* h, const std::vector<cd>& tab, int kind) {
 
 int gpe_set_dispersion(gpe_handle* h, const double* D, int kind) {
   if (!h) return GPE_ERR_INVALID;
+  ++h->gen;
   int rc = check_kind(h, kind);
   if (rc) return rc;
   if (!D) return fail(h, GPE_ERR_INVALID, "null dispersion");
@@ -580,6 +594,7 @@ int gpe_set_dispersion(gpe_handle* h, const double* D, int kind) {
 
 int gpe_set_ktable(gpe_handle* h, const double* table, int kind) {
   if (!h) return GPE_ERR_INVALID;
+  ++h->gen;
   int rc = check_kind(h, kind);
   if (rc) return rc;
   if (!table) return fail(h, GPE_ERR_INVALID, "null table");
@@ -612,6 +627,7 @@ static int store_vtable(gpe_handle* h, const std::vector<cd>& tab, int kind) {
 
 int gpe_set_potential(gpe_handle* h, const double* V, int kind) {
   if (!h) return GPE_ERR_INVALID;
+  ++h->gen;
   int rc = check_kind(h, kind);
   if (rc) return rc;
   if (!V) return fail(h, GPE_ERR_INVALID, "null potential");
@@ -628,6 +644,7 @@ int gpe_set_potential(gpe_handle* h, const double* V, int kind) {
 
 int gpe_set_vtable(gpe_handle* h, const double* table, int kind) {
   if (!h) return GPE_ERR_INVALID;
+  ++h->gen;
   int rc = check_kind(h, kind);
   if (rc) return rc;
   if (!table) return fail(h, GPE_ERR_INVALID, "null table");
@@ -641,6 +658,7 @@ int gpe_set_vtable(gpe_handle* h, const double* table, int kind) {
 
 int gpe_set_nonlinearity(gpe_handle* h, const double* g, const double* c) {
   if (!h) return GPE_ERR_INVALID;
+  ++h->gen;
   const int M = h->M;
   double gg[2][2][2] = {}, cc[2][2] = {};
   if (g) {
@@ -669,6 +687,7 @@ int gpe_set_nonlinearity(gpe_handle* h, const double* g, const double* c) {
 
 int gpe_set_matrix_nonlinearity(gpe_handle* h, const double* g, const double* c) {
   if (!h) return GPE_ERR_INVALID;
+  ++h->gen;
   if (h->M != 2) return fail(h, GPE_ERR_UNSUPPORTED, "the matrix nonlinearity needs two components");
   if (!g) return fail(h, GPE_ERR_INVALID, "null coefficients");
   if (!all_finite(g, 16) || (c && !all_finite(c, 8))) return fail(h, GPE_ERR_NONFINITE, "nonlinearity has NaN or Inf");
@@ -687,6 +706,7 @@ int gpe_set_matrix_nonlinearity(gpe_handle* h, const double* g, const double* c)
 }
 
 int gpe_set_pump(gpe_handle* h, int comp, const double* profile, int profile_complex, const double* amp, int64_t n_amp) {
+  if (h) ++h->gen;
   int rc = check_comp(h, comp);
   if (rc) return rc;
   cudaFree(h->pprof[comp]);
@@ -735,6 +755,7 @@ int gpe_set_pump(gpe_handle* h, int comp, const double* profile, int profile_com
 
 int gpe_set_noise(gpe_handle* h, int mode, uint64_t seed, const double* eta, const double* eta_profile) {
   if (!h) return GPE_ERR_INVALID;
+  ++h->gen;
   if (mode != GPE_NOISE_OFF && mode != GPE_NOISE_PHILOX && mode != GPE_NOISE_REPLAY)
     return fail(h, GPE_ERR_INVALID, "bad noise mode %d", mode);
   for (int m = 0; m < 2; ++m) { cudaFree(h->etaprof[m]); h->etaprof[m] = nullptr; }
@@ -870,6 +891,7 @@ static int ensure(gpe_handle* h, void** buf, size_t* cap, size_t bytes) {
 // slot's copy before overwriting it.  Device memory for saves stays kSaveRing slots
 // however many saves the run has.
 constexpr int64_t kSaveRing = 4;
+static_assert(sizeof(gpe_handle::sgexec) / sizeof(cudaGraphExec_t) == kSaveRing, "one save-chunk graph per ring slot");
 
 struct SaveRing {
   gpe_handle* h;
@@ -1043,8 +1065,13 @@ static int enqueue_matrix_steps(gpe_handle* h, PassArgs a, int64_t k0, int64_t n
   return GPE_OK;
 }
 
+// entry / final: emit the run's opening row pass (the first step's leading half step and
+// FFT_x) and close it with the last step's trailing half step in real space; without
+// them the steps continue a run (graph-captured save chunks).  k0: first step index
+// (default: the handle's step count).
 static int enqueue_steps(gpe_handle* h, int64_t nsteps, int64_t save_every, void* save_dev, int64_t nsaves_total,
-                         const void* xi_dev, int64_t* launches, bool relative = false, SaveRing* ring = nullptr) {
+                         const void* xi_dev, int64_t* launches, bool relative = false, SaveRing* ring = nullptr,
+                         bool entry = true, bool final_pass = true, int64_t k0_at = -1) {
   PassArgs a = base_args(h);
   if (h->nl_matrix) {
     a.xi = xi_dev;
@@ -1054,7 +1081,7 @@ static int enqueue_steps(gpe_handle* h, int64_t nsteps, int64_t save_every, void
     return enqueue_matrix_steps(h, a, k0m, nsteps, save_every, save_dev, nsaves_total, launches, ring);
   }
   // relative: step indices count from the value in h->kdev (graph capture)
-  const int64_t k0 = relative ? 0 : h->steps;
+  const int64_t k0 = relative ? 0 : (k0_at >= 0 ? k0_at : h->steps);
   if (relative) a.kbase = h->kdev;
   a.xi = xi_dev;
   a.xi_h0 = 2 * k0;  // replayed xi are indexed from this run's first half step
@@ -1100,17 +1127,17 @@ static int enqueue_steps(gpe_handle* h, int64_t nsteps, int64_t save_every, void
   // 2D / 3D: entry row pass, then (column pass(es), row pass) per step.  3D column
   // passes: FFT_y, then FFT_z * table * iFFT_z, then iFFT_y.
   const int64_t nrows = h->P / h->n[0] * h->B;
-  PassArgs r = a;
-  r.tw = h->tw[0];
-  r.do_ifft = 0;
-  r.do_fft = 1;
-  r.hA = 2 * k0;
-  r.hB = -1;
-  {
+  if (entry) {
+    PassArgs r = a;
+    r.tw = h->tw[0];
+    r.do_ifft = 0;
+    r.do_fft = 1;
+    r.hA = 2 * k0;
+    r.hB = -1;
     TimedLaunch tl(h, 0);
     LK(h, gpe::launch_row(h->prec, h->M, h->logn[0], r, nrows, h->stream, pass_variant(h)));
+    ++nl;
   }
-  ++nl;
   std::vector<std::pair<PassArgs, int>> cols;  // (args, log2 line length)
   if (h->ndim == 2) {
     PassArgs c = a;
@@ -1146,7 +1173,7 @@ static int enqueue_steps(gpe_handle* h, int64_t nsteps, int64_t save_every, void
       LK(h, gpe::launch_col(h->prec, h->M, cp.second, cp.first, h->stream, pass_variant(h)));
       ++nl;
     }
-    const bool last = (s == nsteps - 1);
+    const bool last = final_pass && (s == nsteps - 1);
     PassArgs rr = a;
     rr.tw = h->tw[0];
     rr.do_ifft = 1;
@@ -1190,7 +1217,11 @@ static int capture_chunk(gpe_handle* h, cudaStream_t st, int64_t* launches) {
 
 static int ensure_graph(gpe_handle* h) {
   if (!h->kdev) CK(h, cudaMalloc((void**)&h->kdev, sizeof(int64_t)));
-  if (h->gexec) return GPE_OK;
+  if (h->gexec && h->gexec_gen == h->gen) return GPE_OK;
+  if (h->gexec) {
+    cudaGraphExecDestroy(h->gexec);
+    h->gexec = nullptr;
+  }
   cudaGraph_t g = nullptr;
   CK(h, cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
   int64_t nl = 0;
@@ -1205,6 +1236,77 @@ static int ensure_graph(gpe_handle* h) {
   cudaGraphDestroy(g);
   if (ei != cudaSuccess) return fail(h, GPE_ERR_CUDA, "graph instantiate failed: %s", cudaGetErrorString(ei));
   h->glaunches = nl;
+  h->gexec_gen = h->gen;
+  return GPE_OK;
+}
+
+// Save chunks as graphs, one per ring slot: save_every steps continuing a run (no opening
+// or closing pass), the last row pass writing its save into the slot and going on into
+// the next step; the kernels read the chunk's first step index from kdev, which the
+// chunk advances at its end.
+static int ensure_save_graphs(gpe_handle* h, int64_t save_every) {
+  if (!h->kdev) CK(h, cudaMalloc((void**)&h->kdev, sizeof(int64_t)));
+  if (h->sgexec[0] && h->sg_steps == save_every && h->sg_gen == h->gen && h->sg_buf == h->save_buf) return GPE_OK;
+  for (cudaGraphExec_t& g : h->sgexec)
+    if (g) {
+      cudaGraphExecDestroy(g);
+      g = nullptr;
+    }
+  const size_t plane_bytes = (size_t)h->P * h->B * h->csz;
+  for (int r = 0; r < kSaveRing; ++r) {
+    cudaGraph_t g = nullptr;
+    CK(h, cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
+    h->capturing = 1;
+    int64_t nl = 0;
+    int rc = enqueue_steps(h, save_every, save_every, (char*)h->save_buf + r * plane_bytes, kSaveRing, nullptr, &nl,
+                           true, nullptr, false, false);
+    if (rc == GPE_OK && gpe::launch_advance(h->kdev, save_every, h->stream) != 0)
+      rc = fail(h, GPE_ERR_CUDA, "step-counter advance failed");
+    h->capturing = 0;
+    const cudaError_t ec = cudaStreamEndCapture(h->stream, &g);
+    if (rc || ec != cudaSuccess) {
+      if (g) cudaGraphDestroy(g);
+      return rc ? rc : fail(h, GPE_ERR_CUDA, "save-chunk capture failed: %s", cudaGetErrorString(ec));
+    }
+    const cudaError_t ei = cudaGraphInstantiate(&h->sgexec[r], g, 0);
+    cudaGraphDestroy(g);
+    if (ei != cudaSuccess) return fail(h, GPE_ERR_CUDA, "save-chunk instantiate failed: %s", cudaGetErrorString(ei));
+    h->sg_launches = nl + 1;
+  }
+  h->sg_steps = save_every;
+  h->sg_gen = h->gen;
+  h->sg_buf = h->save_buf;
+  return GPE_OK;
+}
+
+// A run whose saves stream through the ring, one graph launch per save chunk: the
+// opening row pass, chunks 0 .. nsaves-2 as graphs, then the last chunk launched directly
+// with the closing pass.  The passes and their order are those of the direct launches,
+// so the results are identical; the launch gaps between the passes of a chunk go.
+static int run_saves_graphed(gpe_handle* h, int64_t nsteps, int64_t save_every, SaveRing& ring, int64_t* launches) {
+  const int64_t nsaves = nsteps / save_every;
+  int rc = ensure_save_graphs(h, save_every);
+  if (rc) return rc;
+  int64_t nl = 0, total = 0;
+  rc = enqueue_steps(h, 0, 0, nullptr, 0, nullptr, &nl, false, nullptr, true, false);  // opening pass
+  if (rc) return rc;
+  total += nl;
+  h->kval = h->steps;
+  CK(h, cudaMemcpyAsync(h->kdev, &h->kval, sizeof(int64_t), cudaMemcpyHostToDevice, h->stream));
+  for (int64_t si = 0; si + 1 < nsaves; ++si) {
+    if ((rc = ring.before(si))) return rc;
+    CK(h, cudaGraphLaunch(h->sgexec[si % kSaveRing], h->stream));
+    if ((rc = ring.after(si))) return rc;
+    total += h->sg_launches;
+  }
+  const int64_t si = nsaves - 1;
+  if ((rc = ring.before(si))) return rc;
+  const size_t plane_bytes = (size_t)h->P * h->B * h->csz;
+  rc = enqueue_steps(h, save_every, save_every, (char*)h->save_buf + (si % kSaveRing) * plane_bytes, kSaveRing, nullptr,
+                     &nl, false, nullptr, false, true, h->steps + si * save_every);
+  if (rc) return rc;
+  if ((rc = ring.after(si))) return rc;
+  *launches = total + nl;
   return GPE_OK;
 }
 
@@ -1306,6 +1408,9 @@ static int run_common(gpe_handle* h, int64_t nsteps, int64_t save_every, void* o
   if (graph) {
     int rc = replay_graph(h, nsteps, &launches);
     if (rc) return rc;
+  } else if (use_ring && !xi_host && !h->nl_matrix && !h->timing) {
+    int rc = run_saves_graphed(h, nsteps, save_every, ring, &launches);
+    if (rc) return rc;
   } else {
     int rc = enqueue_steps(h, nsteps, save_every, save_dev, use_ring ? kSaveRing : nsaves,
                            xi_host ? h->xi_buf : nullptr, &launches, false, use_ring ? &ring : nullptr);
@@ -1384,6 +1489,7 @@ int gpe_set_state(gpe_handle* h, const gpe_state* st) {
   if (!std::isfinite(st->t) || st->steps < 0) return fail(h, GPE_ERR_INVALID, "bad state");
   h->t = st->t;
   h->steps = st->steps;
+  if (st->seed != h->seed) ++h->gen;  // the key is a kernel argument; step indices are not
   h->seed = st->seed;
   return GPE_OK;
 }
@@ -1469,6 +1575,7 @@ int gpe_energy(gpe_handle* h, double* out) {
 
 int gpe_set_variant(gpe_handle* h, int variant) {
   if (!h) return GPE_ERR_INVALID;
+  ++h->gen;
   if (variant < -1 || variant > 2) return fail(h, GPE_ERR_INVALID, "variant %d: expected -1, 0, 1 or 2", variant);
   if (variant == 1 && !(h->prec == gpe::PREC_F32 && h->M == 1))
     return fail(h, GPE_ERR_UNSUPPORTED, "variant 1 exists for FP32 one-component fields only");
@@ -1484,6 +1591,7 @@ int gpe_set_variant(gpe_handle* h, int variant) {
 
 int gpe_set_graph(gpe_handle* h, int64_t steps_per_graph) {
   if (!h) return GPE_ERR_INVALID;
+  ++h->gen;
   if (steps_per_graph < 0) return fail(h, GPE_ERR_INVALID, "steps_per_graph must be >= 0");
   if (h->gexec) {
     cudaGraphExecDestroy(h->gexec);
@@ -1600,6 +1708,7 @@ struct gpe_ensemble {
   int64_t launches_per_graph = 0;
   double last_ms = 0.0;
   int64_t last_launches = 0;
+  std::vector<int64_t> gens;  // the handles' setter generations the graph was captured in
   std::string err;
 };
 
@@ -1659,7 +1768,9 @@ int gpe_ensemble_run(gpe_ensemble* e, int64_t nsteps, int64_t steps_per_graph) {
     for (int m = 0; m < h->M; ++m)
       if (h->pprof[m] && h->pcoef_n[m] > 1 && h->pcoef_n[m] < 2 * (h->steps + nsteps) + 1)
         return efail(e, GPE_ERR_INVALID, "a pump has too few amplitudes for this run");
-  if (e->gexec && e->gsteps != steps_per_graph) {
+  bool stale = e->gexec && e->gsteps != steps_per_graph;
+  for (size_t i = 0; e->gexec && i < e->hs.size(); ++i) stale = stale || e->gens[i] != e->hs[i]->gen;
+  if (stale) {
     cudaGraphExecDestroy(e->gexec);
     e->gexec = nullptr;
   }
@@ -1698,6 +1809,8 @@ int gpe_ensemble_run(gpe_ensemble* e, int64_t nsteps, int64_t steps_per_graph) {
     if (ei != cudaSuccess) return efail(e, GPE_ERR_CUDA, cudaGetErrorString(ei));
     e->gsteps = steps_per_graph;
     e->launches_per_graph = total;
+    e->gens.clear();
+    for (gpe_handle* h : e->hs) e->gens.push_back(h->gen);
   }
   for (gpe_handle* h : e->hs) {
     h->kval = h->steps;
