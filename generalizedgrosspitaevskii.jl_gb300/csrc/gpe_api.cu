@@ -162,6 +162,9 @@ struct gpe_handle {
   cudaGraphExec_t sgexec[4] = {nullptr, nullptr, nullptr, nullptr};
   int64_t sg_steps = 0, sg_gen = -1, sg_launches = 0;
   void* sg_buf = nullptr;
+  // runs without saves: chunks of kRunChunk steps continuing the run, as one graph
+  cudaGraphExec_t cgexec = nullptr;
+  int64_t cg_gen = -1, cg_launches = 0;
   // energy diagnostics: transformed copy of the state, FP64 D and V samples on the device
   void* escr[2] = {nullptr, nullptr};
   double2* dsamp = nullptr;
@@ -449,6 +452,7 @@ int gpe_destroy(gpe_handle* h) {
   if (h->gexec) cudaGraphExecDestroy(h->gexec);
   for (cudaGraphExec_t& g : h->sgexec)
     if (g) cudaGraphExecDestroy(g);
+  if (h->cgexec) cudaGraphExecDestroy(h->cgexec);
   if (h->stream) cudaStreamDestroy(h->stream);
   delete h;
   return GPE_OK;
@@ -1310,6 +1314,54 @@ static int run_saves_graphed(gpe_handle* h, int64_t nsteps, int64_t save_every, 
   return GPE_OK;
 }
 
+// Runs without saves: the opening row pass, then chunks of kRunChunk steps as one graph
+// (continuing the run, step indices from kdev), then the remaining 1 .. kRunChunk steps
+// launched directly with the closing pass.  Same passes in the same order as direct
+// launches, so the same results; fewer launch gaps between the passes of small fields.
+constexpr int64_t kRunChunk = 32;
+
+static int run_chunks_graphed(gpe_handle* h, int64_t nsteps, int64_t* launches) {
+  if (!h->kdev) CK(h, cudaMalloc((void**)&h->kdev, sizeof(int64_t)));
+  if (h->cgexec && h->cg_gen != h->gen) {
+    cudaGraphExecDestroy(h->cgexec);
+    h->cgexec = nullptr;
+  }
+  if (!h->cgexec) {
+    cudaGraph_t g = nullptr;
+    CK(h, cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
+    h->capturing = 1;
+    int64_t nl = 0;
+    int rc = enqueue_steps(h, kRunChunk, 0, nullptr, 0, nullptr, &nl, true, nullptr, false, false);
+    if (rc == GPE_OK && gpe::launch_advance(h->kdev, kRunChunk, h->stream) != 0)
+      rc = fail(h, GPE_ERR_CUDA, "step-counter advance failed");
+    h->capturing = 0;
+    const cudaError_t ec = cudaStreamEndCapture(h->stream, &g);
+    if (rc || ec != cudaSuccess) {
+      if (g) cudaGraphDestroy(g);
+      return rc ? rc : fail(h, GPE_ERR_CUDA, "chunk capture failed: %s", cudaGetErrorString(ec));
+    }
+    const cudaError_t ei = cudaGraphInstantiate(&h->cgexec, g, 0);
+    cudaGraphDestroy(g);
+    if (ei != cudaSuccess) return fail(h, GPE_ERR_CUDA, "chunk instantiate failed: %s", cudaGetErrorString(ei));
+    h->cg_launches = nl + 1;
+    h->cg_gen = h->gen;
+  }
+  int64_t nl = 0, total = 0;
+  int rc = enqueue_steps(h, 0, 0, nullptr, 0, nullptr, &nl, false, nullptr, true, false);  // opening pass
+  if (rc) return rc;
+  total += nl;
+  const int64_t nchunks = (nsteps - 1) / kRunChunk;
+  h->kval = h->steps;
+  CK(h, cudaMemcpyAsync(h->kdev, &h->kval, sizeof(int64_t), cudaMemcpyHostToDevice, h->stream));
+  for (int64_t c = 0; c < nchunks; ++c) CK(h, cudaGraphLaunch(h->cgexec, h->stream));
+  total += nchunks * h->cg_launches;
+  const int64_t done = nchunks * kRunChunk;
+  rc = enqueue_steps(h, nsteps - done, 0, nullptr, 0, nullptr, &nl, false, nullptr, false, true, h->steps + done);
+  if (rc) return rc;
+  *launches = total + nl;
+  return GPE_OK;
+}
+
 static int replay_graph(gpe_handle* h, int64_t nsteps, int64_t* launches) {
   h->kval = h->steps;
   CK(h, cudaMemcpyAsync(h->kdev, &h->kval, sizeof(int64_t), cudaMemcpyHostToDevice, h->stream));
@@ -1410,6 +1462,9 @@ static int run_common(gpe_handle* h, int64_t nsteps, int64_t save_every, void* o
     if (rc) return rc;
   } else if (use_ring && !xi_host && !h->nl_matrix && !h->timing) {
     int rc = run_saves_graphed(h, nsteps, save_every, ring, &launches);
+    if (rc) return rc;
+  } else if (nsaves == 0 && nsteps > 2 * kRunChunk && !xi_host && !h->nl_matrix && !h->timing && !single_launch) {
+    int rc = run_chunks_graphed(h, nsteps, &launches);
     if (rc) return rc;
   } else {
     int rc = enqueue_steps(h, nsteps, save_every, save_dev, use_ring ? kSaveRing : nsaves,

@@ -70,3 +70,24 @@ def test_setter_between_graphed_solves(gpe, lib):
     it.close()
     for a, b in zip(res1, res2):
         assert np.array_equal(np.array(a), np.array(b))
+
+
+@pytest.mark.parametrize("name", ["polariton-dw", "noise-f32", "3d-dw"])
+@pytest.mark.parametrize("nsteps", [65, 100, 129])
+def test_run_chunk_graphs_match_direct_launches(gpe, lib, name, nsteps):
+    """Runs without saves longer than two chunks go through the chunk graph."""
+    (_, prob, tspan, dt, nsaves, kw), = [c for c in cases(gpe) if c[0] == name]
+    out = []
+    for direct in (False, True):
+        it = gpe.init(prob, gpe.StrangSplitting(), (0.0, (nsteps + 5) * dt), dt=dt, nsaves=1, **kw)
+        if direct:
+            lib.gpe_set_timing(it.h, 1)
+        it.step(3)
+        it.step(nsteps)
+        if not direct:
+            assert it.last_run_launches() > 0
+        out.append([np.array(f) for f in it.get_fields()])
+        it.close()
+    for a, b in zip(*out):
+        assert np.isfinite(a).all()
+        assert np.array_equal(a, b)
