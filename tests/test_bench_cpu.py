@@ -42,8 +42,8 @@ def test_algorithmic_bytes_and_traffic_lookup():
     assert ab["row"] == 64 + 8 / 64 and ab["col"] == 64 + 64 / 64
     ab = bench.algorithmic_bytes(np.complex64, 128)
     assert ab["row"] == 32 + 4 / 128 and ab["col"] == 32 + 32 / 128
-    # the committed ncu summary holds per-point DRAM bytes of both passes, double-word and FP32
-    for dt, fp in (("c128", "dw"), ("c64", "dw")):
+    # the committed ncu summary holds per-point DRAM bytes of both passes in every precision
+    for dt, fp in (("c128", "dw"), ("c128", "native"), ("c64", "dw")):
         for k in ("row", "col"):
             v = bench.dram_traffic(dt, fp, k)
             assert v is not None and 0 < v < 200, (dt, fp, k, v)
