@@ -1287,12 +1287,11 @@ static int ensure_save_graphs(gpe_handle* h, int64_t save_every) {
 // opening row pass, chunks 0 .. nsaves-2 as graphs, then the last chunk launched directly
 // with the closing pass.  The passes and their order are those of the direct launches,
 // so the results are identical; the launch gaps between the passes of a chunk go.
+// (the chunk graphs are ready: ensure_save_graphs)
 static int run_saves_graphed(gpe_handle* h, int64_t nsteps, int64_t save_every, SaveRing& ring, int64_t* launches) {
   const int64_t nsaves = nsteps / save_every;
-  int rc = ensure_save_graphs(h, save_every);
-  if (rc) return rc;
   int64_t nl = 0, total = 0;
-  rc = enqueue_steps(h, 0, 0, nullptr, 0, nullptr, &nl, false, nullptr, true, false);  // opening pass
+  int rc = enqueue_steps(h, 0, 0, nullptr, 0, nullptr, &nl, false, nullptr, true, false);  // opening pass
   if (rc) return rc;
   total += nl;
   h->kval = h->steps;
@@ -1320,7 +1319,7 @@ static int run_saves_graphed(gpe_handle* h, int64_t nsteps, int64_t save_every, 
 // launches, so the same results; fewer launch gaps between the passes of small fields.
 constexpr int64_t kRunChunk = 32;
 
-static int run_chunks_graphed(gpe_handle* h, int64_t nsteps, int64_t* launches) {
+static int ensure_chunk_graph(gpe_handle* h) {
   if (!h->kdev) CK(h, cudaMalloc((void**)&h->kdev, sizeof(int64_t)));
   if (h->cgexec && h->cg_gen != h->gen) {
     cudaGraphExecDestroy(h->cgexec);
@@ -1346,6 +1345,11 @@ static int run_chunks_graphed(gpe_handle* h, int64_t nsteps, int64_t* launches) 
     h->cg_launches = nl + 1;
     h->cg_gen = h->gen;
   }
+  return GPE_OK;
+}
+
+// (the chunk graph is ready: ensure_chunk_graph)
+static int run_chunks_graphed(gpe_handle* h, int64_t nsteps, int64_t* launches) {
   int64_t nl = 0, total = 0;
   int rc = enqueue_steps(h, 0, 0, nullptr, 0, nullptr, &nl, false, nullptr, true, false);  // opening pass
   if (rc) return rc;
@@ -1451,8 +1455,22 @@ static int run_common(gpe_handle* h, int64_t nsteps, int64_t save_every, void* o
   }
   h->evkind.clear();
   const bool graph = h->gsteps > 0 && save_every == 0 && !xi_host && nsteps % h->gsteps == 0;
+  // save chunks / step chunks as graphs (not with per-launch timing, replayed noise or
+  // the matrix family); captured before the run's start event, so capture time is not
+  // counted as run time
+  const bool direct_ok = !xi_host && !h->nl_matrix && !h->timing;
+  const bool gsaves = !graph && use_ring && direct_ok;
+  const bool gchunks = !graph && !gsaves && nsaves == 0 && nsteps > 2 * kRunChunk && direct_ok && !single_launch;
   if (graph) {
     int rc = ensure_graph(h);
+    if (rc) return rc;
+  }
+  if (gsaves) {
+    int rc = ensure_save_graphs(h, save_every);
+    if (rc) return rc;
+  }
+  if (gchunks) {
+    int rc = ensure_chunk_graph(h);
     if (rc) return rc;
   }
   CK(h, cudaEventRecord(h->ev0, h->stream));
@@ -1460,10 +1478,10 @@ static int run_common(gpe_handle* h, int64_t nsteps, int64_t save_every, void* o
   if (graph) {
     int rc = replay_graph(h, nsteps, &launches);
     if (rc) return rc;
-  } else if (use_ring && !xi_host && !h->nl_matrix && !h->timing) {
+  } else if (gsaves) {
     int rc = run_saves_graphed(h, nsteps, save_every, ring, &launches);
     if (rc) return rc;
-  } else if (nsaves == 0 && nsteps > 2 * kRunChunk && !xi_host && !h->nl_matrix && !h->timing && !single_launch) {
+  } else if (gchunks) {
     int rc = run_chunks_graphed(h, nsteps, &launches);
     if (rc) return rc;
   } else {
