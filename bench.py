@@ -325,16 +325,19 @@ def run_gpu(args, rank, world, local_rank):
     value = P * B * args.steps * world / (ms_clean * 1e-3)
 
     # ---- end to end through the C ABI with host buffers
+    # the state in and the result out both live in pinned host memory
     try:
         import torch
-        pinned = [torch.zeros(B * P * 2, dtype=torch.float64 if dtype == np.complex128 else torch.float32).pin_memory()
-                  for _ in range(2)]
+        rt = torch.float64 if dtype == np.complex128 else torch.float32
+        pinned = [torch.zeros(B * P * 2, dtype=rt).pin_memory() for _ in range(2)]
         hbufs = [pb.numpy().view(dtype) for pb in pinned]
+        out_pinned = torch.empty(2 * B * P * 2, dtype=rt).pin_memory()
+        out = out_pinned.numpy().view(dtype).reshape(2, 1, B * P)
     except Exception:
         hbufs = [np.zeros(B * P, dtype) for _ in range(2)]
+        out = np.empty((2, 1, B * P), dtype)
     for m in range(2):
         hbufs[m][:] = 0
-    out = np.empty((2, 1, B * P), dtype)
     barrier()
     t0 = time.perf_counter()
     for m in range(2):
