@@ -106,6 +106,7 @@ struct gpe_handle {
   int vskind = GPE_TABLE_NONE;
   void* pprof[2] = {nullptr, nullptr};
   int pprof_cplx = 0;
+  int pump_uniform = 0;  // bit m: component m's profile is one value everywhere, folded into its coefficients
   std::vector<cd> pprof_host[2];
   void* pcoef[2] = {nullptr, nullptr};  // (dt/4) a(t_h) per half-step boundary, pass precision
   int64_t pcoef_n[2] = {0, 0};
@@ -719,6 +720,7 @@ int gpe_set_pump(gpe_handle* h, int comp, const double* profile, int profile_com
   h->pcoef[comp] = nullptr;
   h->pcoef_n[comp] = 0;
   h->pprof_host[comp].clear();
+  h->pump_uniform &= ~(1 << comp);
   if (!profile) return GPE_OK;
   if (!amp || n_amp < 1) return fail(h, GPE_ERR_INVALID, "pump needs at least one amplitude");
   const size_t P = (size_t)h->P;
@@ -727,10 +729,17 @@ int gpe_set_pump(gpe_handle* h, int comp, const double* profile, int profile_com
   std::vector<cd>& ph = h->pprof_host[comp];
   ph.resize(P);
   for (size_t p = 0; p < P; ++p) ph[p] = profile_complex ? cd(profile[2 * p], profile[2 * p + 1]) : cd(profile[p], 0.0);
+  // a profile with one value c everywhere (a uniform drive, e.g. F = 1 of the
+  // truncated-Wigner example) is folded into the coefficients: the passes then apply
+  // (dt/4) a(t) c without a per-point profile load
+  bool uniform = true;
+  for (size_t p = 1; p < P && uniform; ++p) uniform = ph[p] == ph[0];
+  h->pump_uniform = uniform ? (h->pump_uniform | (1 << comp)) : (h->pump_uniform & ~(1 << comp));
   {
     // (dt/4) a(t_h): the delta/2 = dt/4 factor of src/kernels.jl:45-46, formed in FP64
     std::vector<cd> coef((size_t)n_amp);
-    for (int64_t i = 0; i < n_amp; ++i) coef[(size_t)i] = 0.25 * h->d.dt * cd(amp[2 * i], amp[2 * i + 1]);
+    const cd fold = uniform ? ph[0] : cd(1.0, 0.0);
+    for (int64_t i = 0; i < n_amp; ++i) coef[(size_t)i] = 0.25 * h->d.dt * cd(amp[2 * i], amp[2 * i + 1]) * fold;
     rc = upload_complex(h, &h->pcoef[comp], coef.data(), (size_t)n_amp);
     if (rc) return rc;
     h->pcoef_n[comp] = n_amp;
@@ -853,6 +862,7 @@ static PassArgs base_args(gpe_handle* h) {
     a.etaprof[m] = h->etaprof[m];
   }
   a.pprof_cplx = h->pprof_cplx;
+  a.pump_uniform = h->pump_uniform;
   a.nlm = h->nl_matrix ? h->nlm : nullptr;
   a.noise = h->noise;
   a.seed_lo = (uint32_t)h->seed;

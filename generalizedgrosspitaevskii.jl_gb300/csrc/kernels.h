@@ -47,6 +47,7 @@ struct PassArgs {
   // coefficients (dt/4) a_m(t_h), both stored in the pass precision
   const void* pprof[2];
   int32_t pprof_cplx;
+  int32_t pump_uniform;  // bit m: profile m is 1 everywhere (its value is in the coefficients)
   const void* pcoef[2];
   int64_t pcoef_n[2];
   // noise: -i sqrt(dt/2) eta_m (host-formed) [* eta profile] * xi

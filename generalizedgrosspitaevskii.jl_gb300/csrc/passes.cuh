@@ -226,6 +226,11 @@ template <typename C> __device__ __forceinline__ C czero() {
   memset(&z, 0, sizeof z);
   return z;
 }
+// 1 + 0i in the pass precision
+__device__ __forceinline__ float2 cunit_(float2*) { return make_float2(1.0f, 0.0f); }
+__device__ __forceinline__ double2 cunit_(double2*) { return make_double2(1.0, 0.0); }
+__device__ __forceinline__ dwc cunit_(dwc*) { return mk(dw{1.0f, 0.0f}, dw{0.0f, 0.0f}); }
+template <typename C> __device__ __forceinline__ C cunit() { return cunit_((C*)nullptr); }
 
 // Pump coefficients (dt/4) a(t_h) and (dt/4) a(t_{h+1}) for half step h.
 template <typename Real, int M>
@@ -451,7 +456,8 @@ __device__ __forceinline__ void half_step(typename CT<Real>::T (&u)[M], const Pa
 #pragma unroll
   for (int j = 0; j < M; ++j) {
     if (a.pprof[j]) {
-      prof[j] = a.pprof_cplx ? ldgc((const C*)a.pprof[j] + p) : Prof<Real>::cplx(a.pprof[j], p);
+      prof[j] = ((a.pump_uniform >> j) & 1) ? cunit<C>()
+                : a.pprof_cplx ? ldgc((const C*)a.pprof[j] + p) : Prof<Real>::cplx(a.pprof[j], p);
       if (!pm[j]) u[j] = cadd(u[j], pump_mul(pn[j], prof[j], a.pprof_cplx));
     }
   }
@@ -1123,7 +1129,8 @@ __device__ __forceinline__ void matrix_half_step(typename CT<Real>::T (&u)[2], c
 #pragma unroll
   for (int j = 0; j < 2; ++j) {
     if (a.pprof[j]) {
-      prof[j] = a.pprof_cplx ? ldgc((const C*)a.pprof[j] + p) : Prof<Real>::cplx(a.pprof[j], p);
+      prof[j] = ((a.pump_uniform >> j) & 1) ? cunit<C>()
+                : a.pprof_cplx ? ldgc((const C*)a.pprof[j] + p) : Prof<Real>::cplx(a.pprof[j], p);
       u[j] = cadd(u[j], pump_mul(pn[j], prof[j], a.pprof_cplx));
     }
   }
