@@ -714,6 +714,13 @@ int gpe_set_pump(gpe_handle* h, int comp, const double* profile, int profile_com
   if (h) ++h->gen;
   int rc = check_comp(h, comp);
   if (rc) return rc;
+  const size_t P = (size_t)h->P;
+  // check everything before touching the handle: a refused call keeps the old pump
+  if (profile) {
+    if (!amp || n_amp < 1) return fail(h, GPE_ERR_INVALID, "pump needs at least one amplitude");
+    if (!all_finite(profile, profile_complex ? 2 * P : P)) return fail(h, GPE_ERR_NONFINITE, "pump profile has NaN or Inf");
+    if (!all_finite(amp, 2 * (size_t)n_amp)) return fail(h, GPE_ERR_NONFINITE, "pump amplitude has NaN or Inf");
+  }
   cudaFree(h->pprof[comp]);
   h->pprof[comp] = nullptr;
   cudaFree(h->pcoef[comp]);
@@ -722,10 +729,6 @@ int gpe_set_pump(gpe_handle* h, int comp, const double* profile, int profile_com
   h->pprof_host[comp].clear();
   h->pump_uniform &= ~(1 << comp);
   if (!profile) return GPE_OK;
-  if (!amp || n_amp < 1) return fail(h, GPE_ERR_INVALID, "pump needs at least one amplitude");
-  const size_t P = (size_t)h->P;
-  if (!all_finite(profile, profile_complex ? 2 * P : P)) return fail(h, GPE_ERR_NONFINITE, "pump profile has NaN or Inf");
-  if (!all_finite(amp, 2 * (size_t)n_amp)) return fail(h, GPE_ERR_NONFINITE, "pump amplitude has NaN or Inf");
   std::vector<cd>& ph = h->pprof_host[comp];
   ph.resize(P);
   for (size_t p = 0; p < P; ++p) ph[p] = profile_complex ? cd(profile[2 * p], profile[2 * p + 1]) : cd(profile[p], 0.0);
@@ -771,16 +774,20 @@ int gpe_set_noise(gpe_handle* h, int mode, uint64_t seed, const double* eta, con
   ++h->gen;
   if (mode != GPE_NOISE_OFF && mode != GPE_NOISE_PHILOX && mode != GPE_NOISE_REPLAY)
     return fail(h, GPE_ERR_INVALID, "bad noise mode %d", mode);
+  // check everything before touching the handle: a refused call keeps the old noise
+  if (mode != GPE_NOISE_OFF) {
+    if (!eta) return fail(h, GPE_ERR_INVALID, "noise needs eta");
+    if (!all_finite(eta, 2 * h->M)) return fail(h, GPE_ERR_NONFINITE, "eta has NaN or Inf");
+    if (eta_profile && !all_finite(eta_profile, (size_t)h->M * h->P))
+      return fail(h, GPE_ERR_NONFINITE, "eta profile has NaN or Inf");
+  }
   for (int m = 0; m < 2; ++m) { cudaFree(h->etaprof[m]); h->etaprof[m] = nullptr; }
   h->noise = mode;
   h->seed = seed;
   memset(h->eta, 0, sizeof h->eta);
   if (mode == GPE_NOISE_OFF) return GPE_OK;
-  if (!eta) return fail(h, GPE_ERR_INVALID, "noise needs eta");
-  if (!all_finite(eta, 2 * h->M)) return fail(h, GPE_ERR_NONFINITE, "eta has NaN or Inf");
   for (int m = 0; m < h->M; ++m) { h->eta[m][0] = eta[2 * m]; h->eta[m][1] = eta[2 * m + 1]; }
   if (eta_profile) {
-    if (!all_finite(eta_profile, (size_t)h->M * h->P)) return fail(h, GPE_ERR_NONFINITE, "eta profile has NaN or Inf");
     for (int m = 0; m < h->M; ++m) {
       int rc = upload_real(h, &h->etaprof[m], eta_profile + (size_t)m * h->P, (size_t)h->P);
       if (rc) return rc;

@@ -112,6 +112,33 @@ def test_bad_calls_leave_the_handle_working(gpe, lib):
     assert np.array_equal(got, want)
 
 
+def test_refused_setters_keep_the_old_settings(gpe, lib):
+    """A refused pump or noise call leaves the previous pump / noise in place: the run
+    afterwards equals the run of a handle that never saw the bad call."""
+    L = gpe._lib
+    amp = np.zeros(2 * 41)
+    amp[0::2] = 0.7
+    eta = np.array([0.05, 0.0])
+    outs = []
+    for bad in (False, True):
+        rc, h = create(lib, L)
+        configure(lib, L, h)
+        assert lib.gpe_set_pump(h, 0, np.ones(N * N).ctypes.data, 0, amp.ctypes.data, 41) == L.GPE_OK
+        assert lib.gpe_set_noise(h, L.GPE_NOISE_PHILOX, 9, eta.ctypes.data, None) == L.GPE_OK
+        if bad:
+            nan_amp = amp.copy()
+            nan_amp[4] = np.nan
+            assert lib.gpe_set_pump(h, 0, np.ones(N * N).ctypes.data, 0, nan_amp.ctypes.data, 41) == L.GPE_ERR_NONFINITE
+            assert lib.gpe_set_pump(h, 0, np.ones(N * N).ctypes.data, 0, None, 0) == L.GPE_ERR_INVALID
+            assert lib.gpe_set_noise(h, L.GPE_NOISE_PHILOX, 3, None, None) == L.GPE_ERR_INVALID
+            assert lib.gpe_set_noise(h, L.GPE_NOISE_PHILOX, 3, np.array([np.inf, 0]).ctypes.data,
+                                     None) == L.GPE_ERR_NONFINITE
+        assert lib.gpe_run(h, 20, 0, None, None) == L.GPE_OK
+        outs.append(field(lib, h))
+        lib.gpe_destroy(h)
+    assert np.array_equal(outs[0], outs[1])
+
+
 def test_pump_amplitudes_must_cover_the_run(gpe, lib):
     L = gpe._lib
     rc, h = create(lib, L)
