@@ -643,7 +643,7 @@ def run_twa(pkg, steps: int, tune: bool):
             k = A.key(N, 1, "c64", B, A.gpu_name())
             resident, variant, chunk_n, _ = A.tune(
                 lambda r, v, N=N, B=B: T.make_group(N, B, prm, 400, seed=N, resident=r, variant=v), k,
-                trial_steps=200, variants=(0, 1))
+                trial_steps=200, variants=(0, 1), resident_ok=A.resident_fits(N, 1, 8))
             choices[f"{N}x{N}"] = {"resident": resident, "variant": variant, "steps_per_graph": chunk_n}
             tuned_chunks.append(chunk_n)
         its.append(T.make_group(N, B, prm, steps + 400, seed=N, resident=resident, variant=variant))

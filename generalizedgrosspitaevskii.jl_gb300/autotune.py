@@ -60,19 +60,28 @@ def key(N: int, M: int, dtype: str, ntraj: int, gpu: str) -> str:
     return f"{gpu}|N{N}|M{M}|{dtype}|B{ntraj}"
 
 
+def resident_fits(N: int, M: int, complex_bytes: int) -> bool:
+    """Whether an N x N field of M components (complex_bytes per value) runs in the
+    resident plane kernel: its whole trajectory must fit in 200 KiB of shared memory
+    (the library's rule for square 2D grids of 16..128 points a side)."""
+    return 16 <= N <= 128 and M * N * N * complex_bytes <= 200 * 1024
+
+
 def tune(make_iterator: Callable[[bool, int], object], k: str, chunks: Iterable[int] = CANDIDATE_CHUNKS,
-         trial_steps: int = 200, force: bool = False, variants: Iterable[int] = (0,)) -> Tuple[bool, int, int, dict]:
+         trial_steps: int = 200, force: bool = False, variants: Iterable[int] = (0,),
+         resident_ok: bool = True) -> Tuple[bool, int, int, dict]:
     """Pick (resident, variant, steps_per_graph) for one group.  make_iterator(resident,
     variant) builds a fresh iterator for the group; ``variants`` are the line tilings to
-    try on the two-pass path.  Returns (resident, variant, steps_per_graph, timings)."""
+    try on the two-pass path; ``resident_ok`` False leaves the resident kernel out (the
+    grid does not fit it).  Returns (resident, variant, steps_per_graph, timings)."""
     db = _load()
     if not force and k in db and "variant" in db[k]:
         r = db[k]
-        return bool(r["resident"]), int(r["variant"]), int(r["steps_per_graph"]), r.get("timings", {})
+        return bool(r["resident"]) and resident_ok, int(r["variant"]), int(r["steps_per_graph"]), r.get("timings", {})
     from .twa import Ensemble
     timings = {}
     best = None
-    candidates = [(True, 0)] + [(False, v) for v in variants]
+    candidates = ([(True, 0)] if resident_ok else []) + [(False, v) for v in variants]
     for resident, variant in candidates:
         for chunk in chunks:
             if trial_steps % chunk:

@@ -176,3 +176,47 @@ def test_autotune_picks_fastest_and_caches(gpe, tmp_path, monkeypatch):
     made.clear()
     assert A.tune(make, "k1", variants=(0, 1))[:3] == (False, 1, 200)
     assert not made  # answered from the cache
+
+
+def test_autotune_leaves_out_a_resident_kernel_that_does_not_fit(gpe, tmp_path, monkeypatch):
+    """Grids too large for the resident plane kernel are tuned over the two-pass tilings
+    only, and a cached answer never claims the resident kernel for them."""
+    import importlib
+    A = importlib.import_module("gpe_gb300.autotune")
+    T = importlib.import_module("gpe_gb300.twa")
+    monkeypatch.setenv("GPE_AUTOTUNE_CACHE", str(tmp_path / "tune.json"))
+    assert A.resident_fits(128, 1, 8) and A.resident_fits(64, 2, 16)
+    assert not A.resident_fits(256, 1, 8) and not A.resident_fits(128, 2, 16) and not A.resident_fits(8, 1, 8)
+    made = []
+
+    class FakeIt:
+        def __init__(self, resident, variant):
+            self.cfg = (resident, variant)
+
+        def close(self):
+            pass
+
+    class FakeEnsemble:
+        def __init__(self, its):
+            self.cfg = its[0].cfg
+
+        def run(self, nsteps, chunk):
+            self.ms = (1.0 if self.cfg[0] else 2.0) * nsteps  # a "resident" run that would win
+
+        def last_run_ms(self):
+            return self.ms
+
+        def close(self):
+            pass
+
+    monkeypatch.setattr(T, "Ensemble", FakeEnsemble)
+
+    def make(resident, variant):
+        made.append((resident, variant))
+        return FakeIt(resident, variant)
+
+    res, var, chunk, _ = A.tune(make, "k256", chunks=(50,), trial_steps=200, variants=(0,), resident_ok=False)
+    assert res is False and all(not r for r, _ in made)
+    # a cache entry from a tuner that did try it is not trusted for a grid that cannot fit
+    A.tune(make, "kfits", chunks=(50,), trial_steps=200, variants=(0,))
+    assert A.tune(make, "kfits", chunks=(50,), variants=(0,), resident_ok=False)[0] is False
