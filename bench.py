@@ -317,6 +317,7 @@ def run_gpu(args, rank, world, local_rank):
     # the event-bracketed run above has per-launch events; time a clean run for value
     L.check(lib, h, lib.gpe_run(h, args.steps, 0, None, None))
     ms_clean = lib.gpe_last_run_ms(h)
+    launches = lib.gpe_last_run_launches(h)  # the kernels of the run that `value` times
     if dist:
         import torch
         t = torch.tensor([ms_clean], device=f"cuda:{local_rank}")
