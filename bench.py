@@ -303,21 +303,20 @@ def run_gpu(args, rank, world, local_rank):
             dist.barrier()
 
     # ---- device-resident throughput (value), per-kernel events on
-    L.check(lib, h, lib.gpe_set_timing(h, 1))
-    barrier()
+    # clocks sampled over both runs: the per-launch-event run (kernel times for the
+    # roofline) and the clean run that `value` times
     with ClockSampler(local_rank) as clk:
+        L.check(lib, h, lib.gpe_set_timing(h, 1))
+        barrier()
         L.check(lib, h, lib.gpe_run(h, args.steps, 0, None, None))
-    barrier()
-    ms = lib.gpe_last_run_ms(h)
-    launches = lib.gpe_last_run_launches(h)
-    kms = np.zeros(3)
-    kn = np.zeros(3, np.int64)
-    L.check(lib, h, lib.gpe_kernel_times(h, L.ptr(kms), L.ptr(kn)))
-    L.check(lib, h, lib.gpe_set_timing(h, 0))
-    # the event-bracketed run above has per-launch events; time a clean run for value
-    L.check(lib, h, lib.gpe_run(h, args.steps, 0, None, None))
-    ms_clean = lib.gpe_last_run_ms(h)
-    launches = lib.gpe_last_run_launches(h)  # the kernels of the run that `value` times
+        barrier()
+        kms = np.zeros(3)
+        kn = np.zeros(3, np.int64)
+        L.check(lib, h, lib.gpe_kernel_times(h, L.ptr(kms), L.ptr(kn)))
+        L.check(lib, h, lib.gpe_set_timing(h, 0))
+        L.check(lib, h, lib.gpe_run(h, args.steps, 0, None, None))
+        ms_clean = lib.gpe_last_run_ms(h)
+        launches = lib.gpe_last_run_launches(h)  # the kernels of the run that `value` times
     if dist:
         import torch
         t = torch.tensor([ms_clean], device=f"cuda:{local_rank}")
