@@ -445,6 +445,11 @@ int gpe_destroy(gpe_handle* h) {
   cudaFree(h->xi_buf);
   cudaFree(h->conv_buf);
   cudaFree(h->red);
+  cudaFree(h->kdev);
+  cudaFree(h->escr[0]);
+  cudaFree(h->escr[1]);
+  cudaFree(h->dsamp);
+  cudaFree(h->vsamp);
   if (h->hstat) cudaFreeHost(h->hstat);
   for (cudaEvent_t e : h->evpool) cudaEventDestroy(e);
   if (h->ev0) cudaEventDestroy(h->ev0);
