@@ -139,8 +139,9 @@ __device__ __forceinline__ float rexp(float x) { return expf(x); }
 
 // Double-word sin/cos.  |x| <= 1/8: cos = 1 - x^2/2 + x^4/24 + tail, sin = x (1 - x^2/6 +
 // x^4/120 + tail) with the double-word leading terms and the tails (below 6e-9 and
-// 8e-10) summed in FP32, which keeps the result within a few units of 2^-48.  Larger
-// angles go through the FP64 routine.
+// 8e-10) summed in FP32, which keeps the result within a few units of 2^-48 (for
+// |x| <= 2^-6 the x^4 terms join the FP32 tails).  Larger angles go through the FP64
+// routine.
 __device__ __forceinline__ void dw_sincos(dw x, dw& s, dw& c) {
   if (fabsf(x.h) <= 0.125f) {
     const dw x2 = dw_mul(x, x);
@@ -148,6 +149,16 @@ __device__ __forceinline__ void dw_sincos(dw x, dw& s, dw& c) {
     const float t3 = t * t * t;
     const float tc = t3 * (-1.0f / 720 + t * (1.0f / 40320 + t * (-1.0f / 3628800 + t * (1.0f / 479001600))));
     const float ts = t3 * (-1.0f / 5040 + t * (1.0f / 362880 + t * (-1.0f / 39916800 + t * (1.0f / 6227020800.0f))));
+    if (t <= 0x1p-12f) {
+      // |x| <= 2^-6: x^4/24 <= 2.5e-9 and x^4/120 <= 5e-10, so FP32 carries them (and
+      // the tails) to well inside 2^-48 absolute; only 1 - x^2/2 and 1 - x^2/6 need
+      // double-word sums
+      c = dw_add(dw_add({1.0f, 0.0f}, {-0.5f * x2.h, -0.5f * x2.l}), {t * t * (1.0f / 24) + tc, 0.0f});
+      dw ss = dw_add({1.0f, 0.0f}, dw_neg(dw_mul(x2, {dwh(1.0 / 6), dwl(1.0 / 6)})));
+      ss = dw_add(ss, {t * t * (1.0f / 120) + ts, 0.0f});
+      s = dw_mul(x, ss);
+      return;
+    }
     const dw q = dw_mul(x2, x2);
     // every partial sum stays within [0.99, 1] (x^2 <= 1/64): no cancellation, so the
     // sloppy double-word sum keeps its relative bound
