@@ -243,10 +243,19 @@ __device__ __forceinline__ double2 cunit_(double2*) { return make_double2(1.0, 0
 __device__ __forceinline__ dwc cunit_(dwc*) { return mk(dw{1.0f, 0.0f}, dw{0.0f, 0.0f}); }
 template <typename C> __device__ __forceinline__ C cunit() { return cunit_((C*)nullptr); }
 
-// Pump coefficients (dt/4) a(t_h) and (dt/4) a(t_{h+1}) for half step h.
+// whether half_step applies component j's two pump terms as one (no E multiplies it)
+__device__ __forceinline__ bool pump_merged(const PassArgs& a, int j) {
+  return !a.nl_on[j] && a.vkind == TAB_NONE;
+}
+
+// Pump coefficients (dt/4) a(t_h) and (dt/4) a(t_{h+1}) for half step h.  merge: a
+// component that neither G nor V touches takes both pump terms in one product,
+// (u + pn F) + px F = u + (pn + px) F, so px carries the sum (formed once here, not per
+// point) and half_step applies it alone (the matrix family's half step applies pn and px
+// on either side of its exponential and does not merge).
 template <typename Real, int M>
 __device__ __forceinline__ void load_pump(const PassArgs& a, int64_t h, typename CT<Real>::T (&pn)[M],
-                                          typename CT<Real>::T (&px)[M]) {
+                                          typename CT<Real>::T (&px)[M], bool merge = false) {
   using C = typename CT<Real>::T;
 #pragma unroll
   for (int j = 0; j < M; ++j) {
@@ -255,6 +264,7 @@ __device__ __forceinline__ void load_pump(const PassArgs& a, int64_t h, typename
       const C* pc = (const C*)a.pcoef[j];
       pn[j] = n == 1 ? ldgc(pc) : ldgc(pc + (h < n ? h : n - 1));
       px[j] = n == 1 ? pn[j] : ldgc(pc + (h + 1 < n ? h + 1 : n - 1));
+      if (merge && pump_merged(a, j)) px[j] = cadd(pn[j], px[j]);
     } else {
       pn[j] = czero<C>();
       px[j] = pn[j];
@@ -399,11 +409,18 @@ __device__ __forceinline__ void half_step(typename CT<Real>::T (&u)[M], const Pa
     for (int j = 0; j < M; ++j) {
       hasE[j] = a.nl_on[j] != 0;
       if (hasE[j]) {
+        // sum of the nonzero terms, starting from the first one when c_j is zero (the
+        // usual case) rather than adding it to zero
         dw gr = {a.cf[j][0], a.cl[j][0]};
+        bool empty = a.cf[j][0] == 0.0f && a.cl[j][0] == 0.0f;
 #pragma unroll
         for (int l = 0; l < M; ++l)
-          if (a.gf[j][l][0] != 0.0f || a.gl[j][l][0] != 0.0f)
-            gr = dw_add_acc(gr, dw_mul({a.gf[j][l][0], a.gl[j][l][0]}, dens[l]));
+          if (a.gf[j][l][0] != 0.0f || a.gl[j][l][0] != 0.0f) {
+            const dw term = dw_mul({a.gf[j][l][0], a.gl[j][l][0]}, dens[l]);
+            if (empty) gr = term;
+            else gr = dw_add_acc(gr, term);
+            empty = false;
+          }
         dw s, c;
         dw_sincos(dw_mul(dth, gr), s, c);
         if (a.nl_imag[j]) {
@@ -463,7 +480,7 @@ __device__ __forceinline__ void half_step(typename CT<Real>::T (&u)[M], const Pa
   // (u + pn F) + px F = u + (pn + px) F
   bool pm[M];
 #pragma unroll
-  for (int j = 0; j < M; ++j) pm[j] = !hasE[j] && a.vkind != TAB_MATRIX;
+  for (int j = 0; j < M; ++j) pm[j] = pump_merged(a, j);  // = !hasE[j] && vkind != MATRIX
 #pragma unroll
   for (int j = 0; j < M; ++j) {
     if (a.pprof[j]) {
@@ -488,7 +505,7 @@ __device__ __forceinline__ void half_step(typename CT<Real>::T (&u)[M], const Pa
   }
 #pragma unroll
   for (int j = 0; j < M; ++j)
-    if (a.pprof[j]) u[j] = cadd(u[j], pump_mul(pm[j] ? cadd(pn[j], px[j]) : px[j], prof[j], a.pprof_cplx));
+    if (a.pprof[j]) u[j] = cadd(u[j], pump_mul(px[j], prof[j], a.pprof_cplx));  // px: pn + px when merged
   if (a.noise != NOISE_OFF) {
     C xi[M];
     if (xi_pre) {
@@ -613,7 +630,7 @@ __device__ __forceinline__ void half_points(typename CT<Real>::T (&x)[M][E], con
                                             int64_t b, int64_t h) {
   using C = typename CT<Real>::T;
   C pn[M], px[M];
-  load_pump<Real, M>(a, h, pn, px);
+  load_pump<Real, M>(a, h, pn, px, true);
 // FP32 points per trip of the half-step loop: 2 measured fastest on the 512^2 polariton
 // row pass (0.61 ms against 0.68 ms with all 8 unrolled, whose code spills out of the
 // instruction cache, and 0.64 ms with 1)
@@ -1112,7 +1129,7 @@ __global__ void __launch_bounds__(256) nl_only_kernel(const PassArgs a) {
       for (int half = 0; half < 2; ++half) {
         const int64_t h = 2 * (step0 + s) + half;
         C pn[M], px[M];
-        load_pump<Real, M>(a, h, pn, px);
+        load_pump<Real, M>(a, h, pn, px, true);
         half_step<Real, M>(v, a, p, b, h, pn, px);
       }
       if (a.save_every > 0 && ((s + 1) % a.save_every) == 0) {
