@@ -248,8 +248,8 @@ def binding_limit(dtype, fp64: str) -> str:
         return ("FP64 pipe: 82-83 % active in both passes (1.2 TFLOP/s FP64 on GB300); "
                 "profiles/polariton512_dw_row_col_passes.md")
     if dtype == np.complex128:
-        return ("FP32-pipe instruction issue: double-word arithmetic, 2088 + 1341 instructions per point "
-                "(row + column), 71 % / 69 % of issue slots busy, DRAM 8-14 % of peak; "
+        return ("FP32-pipe instruction issue: double-word arithmetic, 1929 + 1341 instructions per point "
+                "(row + column), 70 % / 69 % of issue slots busy, DRAM 9-14 % of peak; "
                 "profiles/polariton512_dw_row_col_passes.md")
     return ("instruction issue (row: ALU pipe 43 %, 68 % of issue slots) and global-load latency (column); "
             "profiles/polariton512_f32_row_col_passes.md")
