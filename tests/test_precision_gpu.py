@@ -1,0 +1,43 @@
+"""Long-run accuracy of the FP64 modes on 2D Kerr over 1000 steps against the FP64
+oracle.  The defocusing packet (g = +1) stays smooth: both modes stay far inside the
+1e-10 parity bar.  The self-focusing packet (g = -2, norm just above the collapse
+threshold) amplifies every difference in rounding, the oracle's own FFT order included:
+there the double-word mode is held to its unit roundoff against native FP64 (2^-48
+against 2^-53, a factor 32), i.e. within 64x of native FP64's distance to the oracle."""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+N, LB, DT, NSTEPS = 256, 32.0, 0.005, 1000
+
+
+def run(gpe, oracle, g):
+    dg, _ = oracle.grids((LB, LB), (N, N))
+    X, Y = oracle.mesh(dg)
+    u0c = np.exp(-((X - 16) ** 2 + (Y - 16) ** 2) / 4.0).astype(np.complex128)
+    disp = lambda k, p: (k[0] ** 2 + k[1] ** 2) / 2
+    orc = oracle.OracleProblem(u0=(u0c,), lengths=(LB, LB), dispersion=disp, nonlin_g=np.array([[g]]))
+    _, ores = oracle.solve(orc, (0.0, NSTEPS * DT), DT, 1)
+    err = {}
+    for fp64 in ("dw", "native"):
+        prob = gpe.GrossPitaevskiiProblem((np.asfortranarray(u0c.T),), (LB, LB), dispersion=disp,
+                                          nonlinearity=lambda u, p: g * np.abs(u[0]) ** 2)
+        it = gpe.init(prob, gpe.StrangSplitting(), (0.0, NSTEPS * DT), dt=DT, nsaves=1, fp64=fp64)
+        it.step(NSTEPS)
+        got = np.ascontiguousarray(np.array(it.get_fields()[0]).T)
+        it.close()
+        err[fp64] = oracle.rel_l2(got, ores[0, -1])
+    print(f"g={g}: rel L2 after {NSTEPS} steps: double-word {err['dw']:.3e}, native FP64 {err['native']:.3e}")
+    return err
+
+
+def test_smooth_kerr_1000_steps(gpe, oracle, lib):
+    err = run(gpe, oracle, 1.0)
+    assert err["dw"] <= 1e-11 and err["native"] <= 1e-12, err
+
+
+def test_collapsing_kerr_1000_steps(gpe, oracle, lib):
+    err = run(gpe, oracle, -2.0)
+    assert err["native"] <= 1e-9, err
+    assert err["dw"] <= 64 * err["native"], err
