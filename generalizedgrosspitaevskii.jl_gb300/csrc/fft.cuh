@@ -266,12 +266,18 @@ __device__ __forceinline__ void fft_stages(C (&x)[E], int t, const Lay& lay, con
 
 // Transform one line held as x[i] = point t + T*i.  DIR = -1 forward (unnormalised),
 // DIR = +1 inverse (unnormalised; the 1/P factor is folded into the k-space table).
-// Every thread of the block must call this the same number of times.
+// Every thread of the block must call this the same number of times.  renorm: close the
+// double-word values' deferred renormalisation; a caller whose next step consumes them in
+// double-word products and sums (which take unnormalised pairs at the same normwise
+// bound) leaves it out, and values bound for memory keep it.
 template <typename C, int N, int E, int DIR, class Lay>
-__device__ __forceinline__ void fft_line(C (&x)[E], int t, const Lay& lay, const C* __restrict__ tw) {
+__device__ __forceinline__ void fft_line(C (&x)[E], int t, const Lay& lay, const C* __restrict__ tw,
+                                         bool renorm = true) {
   fft_stages<C, N, E, DIR, 1>(x, t, lay, tw);
+  if (renorm) {
 #pragma unroll
-  for (int i = 0; i < E; ++i) x[i] = bfinish(x[i]);
+    for (int i = 0; i < E; ++i) x[i] = bfinish(x[i]);
+  }
 }
 
 // Joint transform of the M lines (components) a thread holds: each twiddle is loaded

@@ -590,7 +590,7 @@ __device__ __forceinline__ void conj_all(C (&x)[E]) {
 // both directions: component 1 is swapped into the slot of component 0 and back.
 template <typename C, int N, int E, int M, class Lay, bool JOINT = false>
 __device__ __forceinline__ void fft_components(C (&x)[M][E], bool inverse, int t, const Lay& lay,
-                                               const C* __restrict__ tw, int cstride = 0) {
+                                               const C* __restrict__ tw, int cstride = 0, bool renorm = true) {
   if constexpr (JOINT) {
     // all components in one pass (FP32: the twiddle loads and barriers are shared)
     if (inverse) {
@@ -606,7 +606,7 @@ __device__ __forceinline__ void fft_components(C (&x)[M][E], bool inverse, int t
 #pragma unroll 1
     for (int m = 0; m < M; ++m) {
       if (inverse) conj_all(x[0]);
-      fft_line<C, N, E, -1>(x[0], t, lay, tw);
+      fft_line<C, N, E, -1>(x[0], t, lay, tw, renorm);
       if (inverse) conj_all(x[0]);
       if constexpr (M == 2) {
 #pragma unroll
@@ -737,7 +737,10 @@ row_kernel(const PassArgs a, const int64_t nlines, const int lb) {
   for (int ph = 0; ph < 4; ++ph) {
     if (ph == 0 || ph == 3) {
       if (ph == 0 ? a.do_ifft : a.do_fft)
-        fft_components<C, N, E, M, RowLayout<C>, Cfg::JOINT>(x, ph == 0, t, lay, tw, lb * N);
+        // the inverse transform's values go straight into the half steps' double-word
+        // products and sums: no closing renormalisation, unless the pass ends without the
+        // forward transform (then they may be stored as they are)
+        fft_components<C, N, E, M, RowLayout<C>, Cfg::JOINT>(x, ph == 0, t, lay, tw, lb * N, ph != 0 || !a.do_fft);
       continue;
     }
     const int64_t hr = ph == 2 ? a.hB : a.hA;
@@ -774,7 +777,9 @@ __device__ __forceinline__ void col_tile_work(typename CT<Real>::T (&x)[M][LineC
   for (int ph = 0; ph < 3; ++ph) {
     if (ph != 1) {
       if (ph == 0 ? a.col_fwd : a.col_inv)
-        fft_components<C, N, E, M, ColLayout<C, CC>, Cfg::JOINT>(x, ph == 2, t, lay, tw, CC * Cfg::NPAD);
+        // the forward transform's values go straight into the table's complex products
+        fft_components<C, N, E, M, ColLayout<C, CC>, Cfg::JOINT>(x, ph == 2, t, lay, tw, CC * Cfg::NPAD,
+                                                                 ph == 2 || !a.ktab);
       continue;
     }
     if (a.ktab) {
