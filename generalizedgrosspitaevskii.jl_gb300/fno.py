@@ -16,7 +16,7 @@ modes.  Layout changes between the GEMMs are permutation kernels; GELU, bias, lo
 Adam are elementwise kernels.  torch tensors only hold device memory.
 
 The training data come from the solver itself (``generate_pairs``) and the solver is the
-fallback and judge of the surrogate (``hybrid_rollout``).
+fallback of the surrogate and measures its error (``hybrid_rollout``).
 """
 from __future__ import annotations
 

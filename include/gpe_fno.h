@@ -1,7 +1,7 @@
 /*
  * gpe_fno.h -- kernels of the Fourier-neural-operator surrogate of the StrangSplitting
  * solver (no counterpart in the reference: a learned model trained on trajectories the
- * solver generates, with the solver as its fallback and judge).
+ * solver generates, with the solver as its fallback and the measure of its error).
  *
  * All entry points take caller-owned device pointers (FP32) and an optional CUDA stream
  * (NULL = legacy default stream); they enqueue work and return GPE_OK (0) or a negative

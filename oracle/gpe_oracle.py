@@ -1,6 +1,6 @@
 """FP64 CPU oracle for the StrangSplitting time stepper of GeneralizedGrossPitaevskii.jl.
 
-TEST INFRASTRUCTURE ONLY.  This module is the checker that the GPU path is compared
+TEST INFRASTRUCTURE ONLY.  This module is the oracle that the GPU path is compared
 against; only ``tests/``, ``__graft_entry__.smoke()`` and the ``cpu_baseline`` /
 ``--impl reference`` legs of ``bench.py`` may import it.  The product path never calls it.
 

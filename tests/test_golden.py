@@ -1,6 +1,6 @@
 """The golden fixtures of tests/golden/ (outputs of the FP64 oracle on small seeded
 cases, written by tests/golden/make_golden.py) still come out of the oracle: guards the
-checker against accidental change.  CPU only."""
+oracle against accidental change.  CPU only."""
 import importlib.util
 from pathlib import Path
 
