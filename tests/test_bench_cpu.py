@@ -61,3 +61,17 @@ def test_closed_form_2x2_exponential():
         want = scipy_linalg.expm(A[:, :, n])
         got = np.array([[E[i][j][n] for j in range(2)] for i in range(2)])
         assert np.abs(got - want).max() <= 1e-13 * max(1.0, np.abs(want).max()), n
+
+
+def test_reference_arm_under_torchrun_prints_one_line():
+    """Two ranks launched as the multi-GPU bench is: rank 0 alone runs the reference arm
+    and prints; the other rank exits 0 without work."""
+    cmd = [sys.executable, "-m", "torch.distributed.run", "--nnodes=1", "--nproc-per-node", "2",
+           "--master-addr", "127.0.0.1", "--master-port", "29517", str(ROOT / "bench.py"),
+           "--impl", "reference", "--gpus", "2", "--steps", "1", "--warmup", "3"]
+    r = subprocess.run(cmd, capture_output=True, text=True, timeout=600, cwd=ROOT)
+    assert r.returncode == 0, r.stderr[-2000:]
+    lines = [ln for ln in r.stdout.splitlines() if ln.startswith("{")]
+    assert len(lines) == 1, r.stdout
+    d = json.loads(lines[0])
+    assert d["impl"] == "reference" and d["n_gpus"] == 2 and d["value"] > 0
