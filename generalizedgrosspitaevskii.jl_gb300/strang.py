@@ -136,19 +136,7 @@ class StrangSplittingIterator:
             V, kind = sample_table(prob.potential, dg, prob.param, M)
             L.check(lib, h, lib.gpe_set_potential(h, L.ptr(np.ascontiguousarray(V)), kind))
         if prob.pump is not None:
-            times = pump_sample_times(self.t0, self.dt, self.total_steps)
-            profiles, amps = classify_pump(prob.pump, dg, prob.param, M, times)
-            for m in range(M):
-                if profiles[m] is None:
-                    continue
-                a = np.ascontiguousarray(amps[m])
-                n_amp = len(a)
-                if np.all(a == a[0]):
-                    a, n_amp = a[:1].copy(), 1
-                prof = profiles[m]
-                cplx = int(np.any(prof.imag != 0))
-                pbuf = np.ascontiguousarray(prof if cplx else prof.real)
-                L.check(lib, h, lib.gpe_set_pump(h, m, L.ptr(pbuf), cplx, L.ptr(a), n_amp))
+            self._upload_pumps(dg)
         if prob.position_noise_func is not None:
             eta, prof = classify_noise(prob.position_noise_func, dg, prob.param, M, prob.spatial_shape)
             mode = L.GPE_NOISE_REPLAY if self.noise_replay is not None else L.GPE_NOISE_PHILOX
@@ -156,6 +144,37 @@ class StrangSplittingIterator:
             e = np.ascontiguousarray(eta)
             pr = None if prof is None else np.ascontiguousarray(prof)
             L.check(lib, h, lib.gpe_set_noise(h, mode, seed, L.ptr(e), L.ptr(pr)))
+
+    def _upload_pumps(self, dg=None):
+        """Pump profiles and the amplitudes at the reference's sampling times of steps
+        0 .. total_steps - 1 (the device schedule is indexed by the absolute step)."""
+        prob, lib, h = self.prob, self.lib, self.h
+        dg = direct_grid(prob) if dg is None else dg
+        times = pump_sample_times(self.t0, self.dt, self.total_steps)
+        profiles, amps = classify_pump(prob.pump, dg, prob.param, prob.M, times)
+        for m in range(prob.M):
+            if profiles[m] is None:
+                continue
+            a = np.ascontiguousarray(amps[m])
+            n_amp = len(a)
+            if np.all(a == a[0]):
+                a, n_amp = a[:1].copy(), 1
+            prof = profiles[m]
+            cplx = int(np.any(prof.imag != 0))
+            pbuf = np.ascontiguousarray(prof if cplx else prof.real)
+            L.check(lib, h, lib.gpe_set_pump(h, m, L.ptr(pbuf), cplx, L.ptr(a), n_amp))
+
+    def _cover_pump_schedule(self, nsteps: int):
+        """The reference's iterator evaluates the pump at any time, so stepping past tspan
+        is allowed there: extend the sampled schedule (at least doubling it) when the next
+        nsteps steps would run past it."""
+        if self.prob.pump is None:
+            return
+        need = int(self.state().steps) + int(nsteps)
+        if need <= self.total_steps:
+            return
+        self.total_steps = max(need, 2 * self.total_steps)
+        self._upload_pumps()
 
     def close(self):
         if getattr(self, "h", None) is not None and self.h.value:
@@ -179,6 +198,7 @@ class StrangSplittingIterator:
 
     def _run(self, nsteps: int, save_every: int, out: Optional[np.ndarray], ts: Optional[np.ndarray]):
         lib, h = self.lib, self.h
+        self._cover_pump_schedule(nsteps)
         xi = self._replay_xi(nsteps)
         if xi is not None:
             L.check(lib, h, lib.gpe_run_replay(h, nsteps, save_every, L.ptr(xi), L.ptr(out), L.ptr(ts)))
@@ -245,6 +265,7 @@ class StrangSplittingIterator:
                 full[m, 0] = np.asarray(self.prob.u0[m]).ravel(order="F")
         ts = np.empty(ns, np.float64)
         nsteps = ns * self.steps_per_save
+        self._cover_pump_schedule(nsteps)
         xi = self._replay_xi(nsteps)
         out = full[0, off:] if ns > 0 else full
         L.check(self.lib, self.h, self.lib.gpe_run_ex(self.h, nsteps, self.steps_per_save, L.ptr(xi), L.ptr(out),

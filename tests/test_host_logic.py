@@ -82,6 +82,68 @@ def test_pump_classification(gpe):
         classify_pump(lambda r, p, t: np.exp(-((r[0] - t) ** 2)), axes, None, 1, times)
 
 
+class _FakeLib:
+    """Stands in for libgpe in host-logic tests: records the pump schedules and refuses
+    a run whose schedule is too short, as gpe_run does."""
+
+    def __init__(self):
+        self.steps, self.amps = 0, {}
+
+    def gpe_create(self, dref, href):
+        href._obj.value = 1
+        return 0
+
+    def gpe_set_field(self, h, m, p):
+        return 0
+
+    def gpe_set_dispersion(self, h, p, kind):
+        return 0
+
+    def gpe_set_pump(self, h, m, prof, cplx, a, n):
+        import ctypes
+        v = np.frombuffer((ctypes.c_double * (2 * n)).from_address(a), np.float64)
+        self.amps[m] = v[0::2] + 1j * v[1::2]
+        return 0
+
+    def gpe_get_state(self, h, st):
+        st._obj.steps = self.steps
+        return 0
+
+    def gpe_run(self, h, nsteps, save_every, out, ts):
+        if any(len(a) > 1 and len(a) < 2 * (self.steps + nsteps) + 1 for a in self.amps.values()):
+            return -1
+        self.steps += nsteps
+        return 0
+
+    def gpe_last_error(self, h):
+        return b"pump schedule too short"
+
+    def gpe_destroy(self, h):
+        return 0
+
+
+def test_iterator_extends_the_pump_schedule(gpe, monkeypatch):
+    """The reference's iterator samples the pump at any time, so step! may run past
+    tspan; the schedule on the device is extended, with the reference's sampling times."""
+    fake = _FakeLib()
+    monkeypatch.setattr(gpe._lib, "load", lambda path=None: fake)
+    N, Lb, dt = 16, 8.0, 0.1
+    amp = lambda t: min(t / 2.0, 1.0) * np.exp(0.2j * t)
+    prob = gpe.GrossPitaevskiiProblem((np.zeros((N, N), np.complex128),), (Lb, Lb),
+                                      dispersion=lambda k, p: (k[0] ** 2 + k[1] ** 2) / 2,
+                                      pump=lambda r, p, t: amp(t) * np.exp(-((r[0] - 4) ** 2 + (r[1] - 4) ** 2)))
+    it = gpe.init(prob, gpe.StrangSplitting(), (0.0, 1.0), dt=dt, nsaves=2)
+    assert len(fake.amps[0]) == 2 * 10 + 1
+    it.step(10)
+    assert len(fake.amps[0]) == 21
+    it.step(5)
+    assert len(fake.amps[0]) >= 2 * 15 + 1
+    times = gpe.pump_sample_times(0.0, it.dt, (len(fake.amps[0]) - 1) // 2)
+    a = fake.amps[0]
+    assert np.allclose(a / a[-1], np.array([amp(t) for t in times]) / amp(times[-1]), rtol=1e-12, atol=1e-15)
+    it.close()
+
+
 def test_noise_classification(gpe):
     from gpe_gb300.problem import classify_noise, direct_grid_axis
     axes = (direct_grid_axis(10.0, 16),)
