@@ -12,11 +12,11 @@ package is the host-side mirror of the reference's Julia surface:
 from ._lib import GPEError, load as load_library
 from .problem import (GrossPitaevskiiProblem, SeparablePump, direct_grid, reciprocal_grid)
 from .strang import (StrangSplitting, StrangSplittingIterator, init, pump_sample_times,
-                     resolve_fixed_timestepping, solve)
+                     resolve_fixed_timestepping, solve, solve_, step)
 
 __all__ = [
     "GrossPitaevskiiProblem", "SeparablePump", "StrangSplitting", "StrangSplittingIterator", "init",
-    "solve", "direct_grid", "reciprocal_grid", "resolve_fixed_timestepping", "pump_sample_times",
+    "solve", "solve_", "step", "direct_grid", "reciprocal_grid", "resolve_fixed_timestepping", "pump_sample_times",
     "GPEError", "load_library", "build",
 ]
 

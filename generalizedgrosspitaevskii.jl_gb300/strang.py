@@ -296,6 +296,17 @@ def init(prob: GrossPitaevskiiProblem, alg: StrangSplitting, tspan, *, dt, nsave
                                    variant=variant, tma=tma)
 
 
+def step(it: StrangSplittingIterator, nsteps: int = 1) -> StrangSplittingIterator:
+    """CommonSolve.step!(iterator) (src/strang_splitting.jl:86-90): advance nsteps steps."""
+    it.step(nsteps)
+    return it
+
+
+def solve_(it: StrangSplittingIterator):
+    """CommonSolve.solve!(iterator) (src/fixed_time_stepping.jl:26-54) -> (ts, result)."""
+    return it.solve()
+
+
 def solve(prob: GrossPitaevskiiProblem, alg: StrangSplitting, tspan, **kwargs):
     """solve(prob, StrangSplitting(), tspan; dt, nsaves, ...) (src/fixed_time_stepping.jl:79-81)."""
     it = init(prob, alg, tspan, **kwargs)

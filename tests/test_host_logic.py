@@ -134,7 +134,7 @@ def test_iterator_extends_the_pump_schedule(gpe, monkeypatch):
                                       pump=lambda r, p, t: amp(t) * np.exp(-((r[0] - 4) ** 2 + (r[1] - 4) ** 2)))
     it = gpe.init(prob, gpe.StrangSplitting(), (0.0, 1.0), dt=dt, nsaves=2)
     assert len(fake.amps[0]) == 2 * 10 + 1
-    it.step(10)
+    gpe.step(it, 10)
     assert len(fake.amps[0]) == 21
     it.step(5)
     assert len(fake.amps[0]) >= 2 * 15 + 1
