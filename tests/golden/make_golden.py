@@ -108,8 +108,21 @@ def bistability1d():
     return dict(ts=ts, saves=res)
 
 
+def kerr3d():
+    """3D Kerr on (nx, ny, nz) = (32, 16, 16), L = (8, 6, 5): u0 = exp(-|r - (4, 3, 2.5)|^2)
+    exp(i x), D = (kx^2 + ky^2 + 2 kz^2)/2, V = 0.1 (z - 2.5)^2, G = -1.5|u|^2, tspan
+    (0, 0.2), dt 0.01, nsaves 2 (the last save kept)."""
+    L, shape = (8.0, 6.0, 5.0), (32, 16, 16)
+    X, Y, Z = O.mesh(O.grids(L, shape)[0])
+    u0 = (np.exp(-((X - 4) ** 2 + (Y - 3) ** 2 + (Z - 2.5) ** 2)) * np.exp(1j * X)).astype(np.complex128)
+    prob = O.OracleProblem(u0=(u0,), lengths=L, dispersion=lambda k, p: (k[0] ** 2 + k[1] ** 2 + 2 * k[2] ** 2) / 2,
+                           potential=lambda r, p: 0.1 * (r[2] - 2.5) ** 2, nonlin_g=np.array([[-1.5]]))
+    ts, res = O.solve(prob, (0.0, 0.2), 0.01, 2)
+    return dict(ts=ts, last=res[0, -1])
+
+
 CASES = {"kerr_c0": kerr_c0, "polariton64": polariton64, "philox_noise32": philox_noise32,
-         "matrix_nl32": matrix_nl32, "bistability1d": bistability1d}
+         "matrix_nl32": matrix_nl32, "bistability1d": bistability1d, "kerr3d": kerr3d}
 
 
 def main():

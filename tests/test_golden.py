@@ -17,7 +17,7 @@ def _maker():
     return mod
 
 
-@pytest.mark.parametrize("name", ["kerr_c0", "polariton64", "philox_noise32", "matrix_nl32", "bistability1d"])
+@pytest.mark.parametrize("name", ["kerr_c0", "polariton64", "philox_noise32", "matrix_nl32", "bistability1d", "kerr3d"])
 def test_oracle_reproduces_golden(name):
     mk = _maker()
     want = np.load(GOLDEN / f"{name}.npz")

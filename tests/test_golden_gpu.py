@@ -105,3 +105,19 @@ def test_golden_bistability_1d(gpe, lib, fp64):
     ts, (res,) = gpe.solve(prob, gpe.StrangSplitting(), (0.0, 10.0), dt=0.05, nsaves=2, fp64=fp64)
     assert np.allclose(ts, G["ts"], rtol=0, atol=1e-13)
     assert rel(c_order(res), G["saves"][0]) <= 1e-10
+
+
+@pytest.mark.parametrize("fp64", FP64)
+def test_golden_kerr_3d(gpe, lib, fp64):
+    """3D Kerr with a potential on (32, 16, 16): the x row pass and the y/z column passes."""
+    G = np.load(GOLDEN / "kerr3d.npz")
+    L, shape = (8.0, 6.0, 5.0), (32, 16, 16)
+    X, Y, Z = np.meshgrid(*(grid(l, n) for l, n in zip(L, shape)), indexing="ij")
+    u0 = (np.exp(-((X - 4) ** 2 + (Y - 3) ** 2 + (Z - 2.5) ** 2)) * np.exp(1j * X)).astype(np.complex128)
+    prob = gpe.GrossPitaevskiiProblem((u0,), L, dispersion=lambda k, p: (k[0] ** 2 + k[1] ** 2 + 2 * k[2] ** 2) / 2,
+                                      potential=lambda r, p: 0.1 * (r[2] - 2.5) ** 2,
+                                      nonlinearity=lambda u, p: -1.5 * np.abs(u[0]) ** 2)
+    ts, (res,) = gpe.solve(prob, gpe.StrangSplitting(), (0.0, 0.2), dt=0.01, nsaves=2, fp64=fp64)
+    assert res.shape == shape + (3,)
+    assert np.allclose(ts, G["ts"], rtol=0, atol=1e-15)
+    assert rel(c_order(res[..., -1]), G["last"]) <= 1e-10
