@@ -118,13 +118,29 @@ def as_array(val, shape) -> np.ndarray:
         return np.broadcast_to(a, shape)
     return a
 
+def eval_on_grid(f: Callable, coords, *args):
+    """A closure over the grid: called once with the coordinate arrays when it takes
+    them (numpy arithmetic), else once per point with a tuple of floats, as grid_map!
+    calls it (src/misc.jl:1-10) -- closures written for one point (math functions,
+    branches on a coordinate) then work unchanged.  Returns an array of shape
+    (entries..., *grid)."""
+    try:
+        return f(coords, *args)
+    except (TypeError, ValueError):
+        pass
+    gshape = coords[0].shape
+    flat = [np.ravel(c) for c in coords]
+    vals = np.stack([as_array(f(tuple(float(c[i]) for c in flat), *args), ()) for i in range(flat[0].size)], -1)
+    return vals.reshape(vals.shape[:-1] + gshape)
+
+
 def sample_table(f: Callable, axes, param, M: int):
     """Evaluate a dispersion/potential closure over the grid (src/misc.jl:1-20's
     grid_map!).  Returns (values, kind): values has shape (entries, P) complex128 in
     C-ABI point order (x fastest) and kind is one of the GPE_TABLE_* constants."""
     coords = mesh(axes)
     gshape = coords[0].shape
-    vals = as_array(f(coords, param), gshape)
+    vals = as_array(eval_on_grid(f, coords, param), gshape)
     nd = len(gshape)
     extra = vals.ndim - nd if vals.shape[-nd:] == gshape else vals.ndim
     if vals.ndim == 0 or extra == 0 and vals.shape != gshape:
@@ -241,7 +257,7 @@ class SeparablePump:
 
 
 def _pump_values(fn, coords, param, t, M, gshape):
-    F = as_array(fn(coords, param, t), gshape)
+    F = as_array(eval_on_grid(fn, coords, param, t), gshape)
     if F.ndim == 0 or F.shape == gshape:
         F = np.broadcast_to(F, gshape)[None]
         if M != 1:
@@ -278,12 +294,12 @@ def classify_pump(pump, axes, param, M: int, times: np.ndarray):
         pstar = p[star]
         pt = tuple(np.asarray([c[star]]) for c in coords)
         for i, t in enumerate(times):
-            v = as_array(pump(pt, param, float(t)), (1,)).reshape(-1)
+            v = as_array(eval_on_grid(pump, pt, param, float(t)), (1,)).reshape(-1)
             val = v[m] if v.size >= M and M > 1 else v[0]
             amps[m, i] = val / pstar
         # verify separability on the probes
         for F, t in probes:
-            a = as_array(pump(pt, param, t), (1,)).reshape(-1)
+            a = as_array(eval_on_grid(pump, pt, param, t), (1,)).reshape(-1)
             a = (a[m] if a.size >= M and M > 1 else a[0]) / pstar
             if np.abs(F[m] - a * p).max() > 1e-10 * max(1.0, np.abs(F[m]).max()):
                 raise NotImplementedError("pump is not separable as a(t) * p(r); the GPU backend needs that form")

@@ -282,3 +282,29 @@ def test_autotune_leaves_out_a_resident_kernel_that_does_not_fit(gpe, tmp_path, 
     # a cache entry from a tuner that did try it is not trusted for a grid that cannot fit
     A.tune(make, "kfits", chunks=(50,), trial_steps=200, variants=(0,))
     assert A.tune(make, "kfits", chunks=(50,), variants=(0,), resident_ok=False)[0] is False
+
+
+def test_per_point_closures_match_array_closures(gpe):
+    """Closures written for one point (math functions, branches on a coordinate), as
+    grid_map! calls them (src/misc.jl:1-10), sample to the same tables and pumps as their
+    array forms."""
+    from gpe_gb300.problem import classify_pump, direct_grid_axis, reciprocal_grid_axis, sample_table
+    L, N = 16.0, 32
+    ax = (direct_grid_axis(L, N), direct_grid_axis(L, N))
+    kax = (reciprocal_grid_axis(L, N), reciprocal_grid_axis(L, N))
+    a, ka = sample_table(lambda k, p: 0.5 * (k[0] ** 2 + k[1] ** 2), kax, None, 1)
+    b, kb = sample_table(lambda k, p: 0.5 * math.fsum(x * x for x in k), kax, None, 1)
+    assert ka == kb and np.array_equal(a, b)
+    a, _ = sample_table(lambda r, p: np.where(r[0] < 4, 1.0, 0.0), ax, None, 1)
+    b, _ = sample_table(lambda r, p: 1.0 if r[0] < 4 else 0.0, ax, None, 1)
+    assert np.array_equal(a, b)
+    a, ka = sample_table(lambda k, p: [[k[0] ** 2, 1.0 + 0 * k[0]], [1.0 + 0 * k[0], math.sin(1.0) * k[1]]], kax, None, 2)
+    b, kb = sample_table(lambda k, p: [[k[0] ** 2, 1.0], [1.0, math.sin(1.0) * float(k[1])]], kax, None, 2)
+    assert ka == kb == gpe._lib.GPE_TABLE_MATRIX and np.array_equal(a, b)
+    times = gpe.pump_sample_times(0.0, 0.1, 20)
+    pa, aa = classify_pump(lambda r, p, t: [min(t, 1.0) * np.exp(-((r[0] - 8) ** 2 + (r[1] - 8) ** 2) / 9), 0],
+                           ax, None, 2, times)
+    pb, ab = classify_pump(lambda r, p, t: [min(t, 1.0) * math.exp(-((r[0] - 8) ** 2 + (r[1] - 8) ** 2) / 9), 0.0],
+                           ax, None, 2, times)
+    assert pb[1] is None
+    assert np.allclose(aa[0][:, None] * pa[0][None], ab[0][:, None] * pb[0][None], rtol=1e-14, atol=1e-16)
