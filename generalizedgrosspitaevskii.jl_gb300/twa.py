@@ -92,7 +92,7 @@ def make_group(N: int, ntraj: int, prm: DampedDrivenParams, nsteps: int, seed: i
                resident: bool = True, noise_seed: Optional[int] = None, variant: int = 0,
                tma: Optional[bool] = None) -> StrangSplittingIterator:
     prob = wigner_problem(N, ntraj, prm, seed, dtype)
-    return StrangSplittingIterator(prob, (0.0, nsteps * prm.dt), dt=prm.dt, nsaves=1, rng=noise_seed or seed + 1,
+    return StrangSplittingIterator(prob, (0.0, nsteps * prm.dt), dt=prm.dt, nsaves=1, rng=seed + 1 if noise_seed is None else noise_seed,
                                    resident=resident, variant=variant, tma=tma)
 
 
