@@ -169,8 +169,10 @@ def allreduce_moments(fields: np.ndarray, group=None, batch_axis: int = -1):
         active = False
     if active:
         buf = torch.from_numpy(np.concatenate([[float(cnt)], s1.ravel(), s2.ravel()]))
+        if dist.get_backend(group) == "nccl":  # NCCL reduces device tensors only
+            buf = buf.to(torch.device("cuda", torch.cuda.current_device()))
         dist.all_reduce(buf, op=dist.ReduceOp.SUM, group=group)
-        v = buf.numpy()
+        v = buf.cpu().numpy()
         cnt = v[0]
         s1 = v[1:1 + s1.size].reshape(s1.shape)
         s2 = v[1 + s1.size:].reshape(s1.shape)
