@@ -308,3 +308,8 @@ def test_per_point_closures_match_array_closures(gpe):
                            ax, None, 2, times)
     assert pb[1] is None
     assert np.allclose(aa[0][:, None] * pa[0][None], ab[0][:, None] * pb[0][None], rtol=1e-14, atol=1e-16)
+    for shape in ((16,), (16, 8, 4)):
+        axes = tuple(direct_grid_axis(3.0 + a, n) for a, n in enumerate(shape))
+        a, _ = sample_table(lambda r, p: np.exp(-sum((x - 1.0) ** 2 for x in r)) * (r[-1] + 1), axes, None, 1)
+        b, _ = sample_table(lambda r, p: math.exp(-math.fsum((x - 1.0) ** 2 for x in r)) * (r[-1] + 1), axes, None, 1)
+        assert np.allclose(a, b, rtol=1e-15, atol=0), shape
