@@ -243,66 +243,39 @@ def algorithmic_bytes(dtype, B: int):
 
 
 def binding_limit(dtype, fp64: str) -> str:
-    """What bounds the passes of this precision, from the committed ncu captures."""
+    """What bounds the passes of this precision (from ncu captures of the same passes)."""
     if dtype == np.complex128 and fp64 == "native":
-        return ("FP64 pipe: 82-83 % active in both passes (1.2 TFLOP/s FP64 on GB300); "
-                "profiles/polariton512_dw_row_col_passes.md")
+        return ("FP64 pipe: 82-83 % active in both passes (GB300 issues FP64 at 1/64 of the FP32 rate, about "
+                "1.2 TFLOP/s); DRAM stays below 10 % of peak")
     if dtype == np.complex128:
-        return ("FP32-pipe instruction issue: double-word arithmetic, 1929 + 1341 instructions per point "
-                "(row + column), 70 % / 69 % of issue slots busy, DRAM 9-14 % of peak; "
-                "profiles/polariton512_dw_row_col_passes.md")
-    return ("instruction issue (row: ALU pipe 43 %, 68 % of issue slots) and global-load latency (column); "
-            "profiles/polariton512_f32_row_col_passes.md")
+        return ("FP32-pipe instruction issue: double-word arithmetic, about 1900 + 1300 instructions per point "
+                "(row + column), 70 % of issue slots busy, DRAM 9-14 % of peak")
+    return "instruction issue (row: ALU pipe 43 %, 68 % of issue slots) and global-load latency (column)"
 
 
-def dram_traffic(dtype: str, fp64: str, kernel: str):
-    """DRAM bytes per grid point of one launch of `kernel` ("row" / "col"), read from the
-    ncu summary in profiles/dram_traffic.md (rows "| precision | pass | bytes |"), or None."""
-    p = ROOT / "profiles" / "dram_traffic.md"
-    if not p.exists():
-        return None
-    prec = "f32" if dtype == "c64" else ("f64" if fp64 == "native" else "f64-dw")
-    for ln in p.read_text().splitlines():
-        cells = [c.strip() for c in ln.strip().strip("|").split("|")]
-        if len(cells) >= 3 and cells[0] == prec and cells[1] == kernel:
-            try:
-                return float(cells[2])
-            except ValueError:
-                return None
-    return None
+def arith_name(dtype, fp64: str) -> str:
+    if dtype == np.complex64:
+        return "f32"
+    return "f64" if fp64 == "native" else "f64-dw (double-word f32 pairs, 2^-48 unit roundoff)"
 
 
-def run_gpu(args, rank, world, local_rank):
-    import __graft_entry__ as G
-    pkg = G.load_package()
-    import ctypes
-    L = sys.modules["gpe_gb300._lib"]
-    lib = pkg.load_library()
-    dist = None
-    if world > 1:
-        import torch
-        import torch.distributed as tdist
-        torch.cuda.set_device(local_rank)
-        tdist.init_process_group("nccl")
-        dist = tdist
-    dtype = np.complex128 if args.dtype == "c128" else np.complex64
-    B = args.batch or batch_for(dtype)
+def measure_fused(pkg, lib, L, args, dtype, fp64: str, B: int, local_rank: int, world: int, dist, with_e2e: bool):
+    """Device-resident throughput of the fused passes on the polariton workload (and, with
+    with_e2e, the same through gpe_set_field / gpe_run with pinned host buffers)."""
     disp, nonl, pump = polariton_closures()
     u0 = np.zeros((N_GRID, N_GRID, B), dtype, order="F")
     prob = pkg.GrossPitaevskiiProblem((u0, u0.copy()), (L_BOX, L_BOX), dispersion=disp, nonlinearity=nonl, pump=pump)
     total = args.warmup + 3 * args.steps + 8
     it = pkg.StrangSplittingIterator(prob, (0.0, 200.0), dt=DT, nsaves=100, total_steps=max(total, 4000),
-                                     device=local_rank, fp64=args.fp64)
+                                     device=local_rank, fp64=fp64)
     h = it.h
     P = N_GRID * N_GRID
-    # warm-up
     it.step(args.warmup)
 
     def barrier():
         if dist:
             dist.barrier()
 
-    # ---- device-resident throughput (value), per-kernel events on
     # clocks sampled over both runs: the per-launch-event run (kernel times for the
     # roofline) and the clean run that `value` times
     with ClockSampler(local_rank) as clk:
@@ -323,75 +296,114 @@ def run_gpu(args, rank, world, local_rank):
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
         ms_clean = float(t.item())
     value = P * B * args.steps * world / (ms_clean * 1e-3)
-
-    # ---- end to end through the C ABI with host buffers
-    # the state in and the result out both live in pinned host memory
-    try:
-        import torch
-        rt = torch.float64 if dtype == np.complex128 else torch.float32
-        pinned = [torch.zeros(B * P * 2, dtype=rt).pin_memory() for _ in range(2)]
-        hbufs = [pb.numpy().view(dtype) for pb in pinned]
-        out_pinned = torch.empty(2 * B * P * 2, dtype=rt).pin_memory()
-        out = out_pinned.numpy().view(dtype).reshape(2, 1, B * P)
-    except Exception:
-        hbufs = [np.zeros(B * P, dtype) for _ in range(2)]
-        out = np.empty((2, 1, B * P), dtype)
-    for m in range(2):
-        hbufs[m][:] = 0
-    barrier()
-    t0 = time.perf_counter()
-    for m in range(2):
-        L.check(lib, h, lib.gpe_set_field(h, m, L.ptr(hbufs[m])))
-    L.check(lib, h, lib.gpe_run(h, args.steps, args.steps, L.ptr(out), None))
-    e2e_s = time.perf_counter() - t0
-    barrier()
-    if dist:
-        import torch
-        t = torch.tensor([e2e_s], device=f"cuda:{local_rank}")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        e2e_s = float(t.item())
-    e2e_value = P * B * args.steps * world / e2e_s
-    state_bytes = 2 * B * P * np.dtype(dtype).itemsize
+    out = {"value": value, "ms_clean": ms_clean, "launches": int(launches), "kms": kms, "kn": kn,
+           "clocks": clk.summary()}
+    if with_e2e:
+        # the state in and the result out both live in pinned host memory
+        try:
+            import torch
+            rt = torch.float64 if dtype == np.complex128 else torch.float32
+            pinned = [torch.zeros(B * P * 2, dtype=rt).pin_memory() for _ in range(2)]
+            hbufs = [pb.numpy().view(dtype) for pb in pinned]
+            out_pinned = torch.empty(2 * B * P * 2, dtype=rt).pin_memory()
+            res = out_pinned.numpy().view(dtype).reshape(2, 1, B * P)
+        except Exception:
+            hbufs = [np.zeros(B * P, dtype) for _ in range(2)]
+            res = np.empty((2, 1, B * P), dtype)
+        for m in range(2):
+            hbufs[m][:] = 0
+        barrier()
+        t0 = time.perf_counter()
+        for m in range(2):
+            L.check(lib, h, lib.gpe_set_field(h, m, L.ptr(hbufs[m])))
+        L.check(lib, h, lib.gpe_run(h, args.steps, args.steps, L.ptr(res), None))
+        e2e_s = time.perf_counter() - t0
+        barrier()
+        if dist:
+            import torch
+            t = torch.tensor([e2e_s], device=f"cuda:{local_rank}")
+            dist.all_reduce(t, op=dist.ReduceOp.MAX)
+            e2e_s = float(t.item())
+        out["e2e_value"] = P * B * args.steps * world / e2e_s
+        out["state_bytes"] = 2 * B * P * np.dtype(dtype).itemsize
     it.close()
-    plain = None
-    if args.plain_steps > 0:
-        plain = run_plain_gpu(dtype, B, args.plain_steps, 3, local_rank, value / world)
-        if dtype == np.complex128 and args.fp64 == "dw" and rank == 0:
-            plain["rel_l2_fused_vs_plain_f64"] = plain_vs_fused_rel_l2(pkg, local_rank)
-            plain["rel_l2_case"] = "one pumped 512^2 field from u = 0, 200 steps, fused double-word vs plain FP64"
+    return out
 
-    if rank != 0:
-        return
+
+def roofline_of(m: dict, dtype, fp64: str, B: int):
+    """Dominant kernel's algorithmic bytes per launch over its mean event-timed duration,
+    against the measured HBM copy bandwidth."""
+    P = N_GRID * N_GRID
+    kms, kn = m["kms"], m["kn"]
     ab = algorithmic_bytes(dtype, B)
     peak, peak_kind = measured_peaks()
     per_launch = {"row": (kms[0] / max(kn[0], 1), ab["row"]), "col": (kms[1] / max(kn[1], 1), ab["col"])}
-    dom = max(per_launch, key=lambda k: kms[0] if k == "row" else kms[1])
+    dom = "row" if kms[0] >= kms[1] else "col"
     d_ms, d_b = per_launch[dom]
     achieved = d_b * P * B / (d_ms * 1e-3) / 1e9
-    traffic = dram_traffic(args.dtype, args.fp64, dom)
-    if traffic is not None:
-        traffic = traffic * P * B
+    return {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+            "traffic": None, "kernel": f"{dom} pass", "peak_source": f"{peak_kind} hbm_gbs",
+            "traffic_note": "DRAM bytes per launch come from separate ncu captures of the same passes, not from "
+                            "this run",
+            "algorithmic_bytes_per_point": d_b, "launch_ms": d_ms,
+            "kernels": {k: {"launches": int(kn[i]), "total_ms": float(kms[i]),
+                            "mean_ms": float(kms[i] / max(kn[i], 1)),
+                            "achieved_gbs": float(ab[k] * P * B / (kms[i] / max(kn[i], 1) * 1e-3) / 1e9)}
+                        for i, k in enumerate(["row", "col"])},
+            "binding_limit": binding_limit(dtype, fp64)}
+
+
+def run_gpu(args, rank, world, local_rank):
+    import __graft_entry__ as G
+    pkg = G.load_package()
+    L = sys.modules["gpe_gb300._lib"]
+    lib = pkg.load_library()
+    dist = None
+    if world > 1:
+        import torch
+        import torch.distributed as tdist
+        torch.cuda.set_device(local_rank)
+        tdist.init_process_group("nccl")
+        dist = tdist
+    dtype = np.complex128 if args.dtype == "c128" else np.complex64
+    B = args.batch or batch_for(dtype)
+    P = N_GRID * N_GRID
+    m = measure_fused(pkg, lib, L, args, dtype, args.fp64, B, local_rank, world, dist, with_e2e=True)
+    value = m["value"]
+    dw = None
+    if dtype == np.complex128 and args.fp64 == "native" and not args.no_dw:
+        # the opt-in double-word mode on the same workload, reported beside the FP64 headline
+        mdw = measure_fused(pkg, lib, L, args, dtype, "dw", B, local_rank, world, dist, with_e2e=False)
+        dw = {"dtype": arith_name(dtype, "dw"), "value": mdw["value"], "unit": "grid-point-steps/s",
+              "ms_per_step": mdw["ms_clean"] / args.steps, "gpu_launches": mdw["launches"],
+              "speedup_vs_f64": mdw["value"] / value, "roofline": roofline_of(mdw, dtype, "dw", B),
+              "clocks": mdw["clocks"]}
+    plain = None
+    if args.plain_steps > 0:
+        plain = run_plain_gpu(dtype, B, args.plain_steps, 3, local_rank, value / world)
+        if dtype == np.complex128 and rank == 0:
+            plain["rel_l2_fused_vs_plain_f64"] = plain_vs_fused_rel_l2(pkg, local_rank, fp64=args.fp64)
+            plain["rel_l2_case"] = (f"one pumped 512^2 field from u = 0, 200 steps, fused "
+                                    f"{'FP64' if args.fp64 == 'native' else 'double-word'} vs plain FP64")
+
+    if rank != 0:
+        return
     line = {
         "metric": "grid-point-steps/s", "value": value, "unit": "grid-point-steps/s", "n_gpus": world,
-        "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_clean / args.steps, "higher_is_better": True,
-        "scaling": "weak", "vs_baseline": None,
-        "dtype": ("f64" if args.fp64 == "native" else "f64-dw (double-word f32 pairs, 2^-48 unit roundoff)")
-        if dtype == np.complex128 else "f32",
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": m["ms_clean"] / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": arith_name(dtype, args.fp64),
         "data": "synthetic (zero initial field, pumped; the reference's polariton parameters)",
         "config": config_dict(dtype, B, world),
-        "e2e": {"value": e2e_value, "unit": "grid-point-steps/s", "h2d_bytes_per_step": state_bytes / args.steps,
-                "d2h_bytes_per_step": state_bytes / args.steps},
-        "gpu_launches": int(launches),
-        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-                     "traffic": traffic, "kernel": f"{dom} pass", "peak_source": f"{peak_kind} hbm_gbs",
-                     "algorithmic_bytes_per_point": d_b, "launch_ms": d_ms,
-                     "kernels": {k: {"launches": int(kn[i]), "total_ms": float(kms[i]),
-                                     "mean_ms": float(kms[i] / max(kn[i], 1)),
-                                     "achieved_gbs": float(ab[k] * P * B / (kms[i] / max(kn[i], 1) * 1e-3) / 1e9)}
-                                 for i, k in enumerate(["row", "col"])},
-                     "binding_limit": binding_limit(dtype, args.fp64)},
-        "clocks": clk.summary(),
+        "e2e": {"value": m["e2e_value"], "unit": "grid-point-steps/s",
+                "h2d_bytes_per_step": m["state_bytes"] / args.steps,
+                "d2h_bytes_per_step": m["state_bytes"] / args.steps},
+        "gpu_launches": m["launches"],
+        "roofline": roofline_of(m, dtype, args.fp64, B),
+        "clocks": m["clocks"],
     }
+    if dw is not None:
+        line["double_word"] = dw
     if plain is not None:
         line["plain_gpu"] = plain
     if args.anchor_steps > 0:
@@ -413,19 +425,19 @@ def run_polariton_solve(pkg, lib, device):
     of the stepping alone; FP64 (double-word) and FP32."""
     disp, nonl, pump = polariton_closures()
     out = []
-    for dtype in (np.complex128, np.complex64):
+    for dtype, fp64 in ((np.complex128, "native"), (np.complex128, "dw"), (np.complex64, "native")):
         z = np.zeros((N_GRID, N_GRID), dtype, order="F")
         prob = pkg.GrossPitaevskiiProblem((z, z.copy()), (L_BOX, L_BOX), dispersion=disp, nonlinearity=nonl,
                                           pump=pump)
         t0 = time.perf_counter()
-        it = pkg.StrangSplittingIterator(prob, (0.0, 200.0), dt=DT, nsaves=100, device=device)
+        it = pkg.StrangSplittingIterator(prob, (0.0, 200.0), dt=DT, nsaves=100, device=device, fp64=fp64)
         t1 = time.perf_counter()
         ts, res = it.solve()
         t2 = time.perf_counter()
         it.close()
         steps = 4000
         save_bytes = 100 * 2 * N_GRID * N_GRID * np.dtype(dtype).itemsize
-        out.append({"dtype": "f64-dw" if dtype == np.complex128 else "f32", "steps": steps, "saves": 100,
+        out.append({"dtype": arith_name(dtype, fp64).split(" ")[0], "steps": steps, "saves": 100,
                     "setup_s": t1 - t0, "solve_s": t2 - t1, "total_s": t2 - t0,
                     "point_steps_per_s": N_GRID * N_GRID * steps / (t2 - t1),
                     "saved_bytes": save_bytes, "result_shape": list(res[0].shape),
@@ -602,14 +614,14 @@ def plain_single_field_ms(dtype, device: int, steps: int = 200) -> float:
     return e0.elapsed_time(e1) / steps
 
 
-def plain_vs_fused_rel_l2(pkg, device: int, steps: int = 200):
-    """rel L2 between the plain cuFFT form in FP64 and the fused double-word passes after
-    `steps` steps of one pumped polariton field from u = 0."""
+def plain_vs_fused_rel_l2(pkg, device: int, steps: int = 200, fp64: str = "native"):
+    """rel L2 between the plain cuFFT form in FP64 and the fused passes (native FP64 or
+    double-word) after `steps` steps of one pumped polariton field from u = 0."""
     import torch
     disp, nonl, pump = polariton_closures()
     z = np.zeros((N_GRID, N_GRID), np.complex128, order="F")
     prob = pkg.GrossPitaevskiiProblem((z, z.copy()), (L_BOX, L_BOX), dispersion=disp, nonlinearity=nonl, pump=pump)
-    it = pkg.StrangSplittingIterator(prob, (0.0, steps * DT), dt=DT, nsaves=1, device=device)
+    it = pkg.StrangSplittingIterator(prob, (0.0, steps * DT), dt=DT, nsaves=1, device=device, fp64=fp64)
     it.step(steps)
     got = np.stack([np.ascontiguousarray(f.T) for f in it.get_fields()])
     it.close()
@@ -768,102 +780,6 @@ def run_fno(args):
                       "window_cost_by_batch": per_window}), flush=True)
 
 
-def run_twa_breakdown(args):
-    """Per-group timing of the TWA ensemble: each group alone in a graph of 50 steps,
-    resident plane kernel and the two-pass path in both line tilings, 500 timed steps
-    (one JSON line)."""
-    import __graft_entry__ as G
-    G.load_package()
-    T = __import__("gpe_gb300.twa", fromlist=["Ensemble"])
-    prm = T.DampedDrivenParams()
-    out = []
-    for N, B in TWA_GROUPS:
-        for res, var in ((True, 0), (False, 0), (False, 1)):
-            it = T.make_group(N, B, prm, 1000, seed=N, resident=res, variant=var)
-            ens = T.Ensemble([it])
-            ens.run(50, 50)
-            ens.run(500, 50)
-            ms = ens.last_run_ms()
-            out.append({"grid": [N, N], "trajectories": B, "resident": res, "variant": var, "ms_per_step": ms / 500,
-                        "traj_steps_per_s": B * 500 / (ms * 1e-3), "point_steps_per_s": N * N * B * 500 / (ms * 1e-3)})
-            ens.close()
-            it.close()
-    print(json.dumps({"metric": "TWA per-group step time", "groups": out}), flush=True)
-
-
-def run_pass_breakdown(args):
-    """Where the row pass spends its time: the same passes on problems that drop one
-    term at a time (noise, pump, nonlinearity), event-timed per launch over 50 steps.
-    Trajectory group: 256^2 x 341 one-component FP32 fields (D = |k|^2/2 - 0.1i, G =
-    0.01|u|^2, constant pump 1, noise 0.3); polariton: 512^2 two-component fields (the
-    benchmark's 2x2 dispersion and G, Gaussian photon pump), 128 copies in FP32 and 64
-    in double-word FP64.  One JSON line."""
-    import __graft_entry__ as G
-    gpe = G.load_package()
-    L = sys.modules["gpe_gb300._lib"]
-
-    def timed(prob, dt):
-        it = gpe.StrangSplittingIterator(prob, (0.0, 1000 * dt), dt=dt, nsaves=1, device=0, resident=False, rng=5)
-        it.step(5)
-        if args.pass_case >= 0:  # one case, a few steps: a capture for ncu
-            it.close()
-            return {}
-        lib = it.lib
-        L.check(lib, it.h, lib.gpe_set_timing(it.h, 1))
-        L.check(lib, it.h, lib.gpe_run(it.h, 50, 0, None, None))
-        kms = np.zeros(3)
-        kn = np.zeros(3, np.int64)
-        L.check(lib, it.h, lib.gpe_kernel_times(it.h, L.ptr(kms), L.ptr(kn)))
-        it.close()
-        return {"row_ms": float(kms[0] / kn[0]), "col_ms": float(kms[1] / kn[1])}
-
-    rng = np.random.default_rng(0)
-    out = []
-    N, B = 256, 341
-    u0 = np.asfortranarray((1 + 0.3 * (rng.standard_normal((N, N, B)) + 1j * rng.standard_normal((N, N, B))))
-                           .astype(np.complex64))
-    nl = lambda u, p: 0.01 * np.abs(u[0]) ** 2
-    cases = [("all terms", dict(nonlinearity=nl, pump=lambda r, p, t: 1.0 + 0 * r[0],
-                                position_noise_func=lambda u, r, p: 0.3)),
-             ("no noise", dict(nonlinearity=nl, pump=lambda r, p, t: 1.0 + 0 * r[0])),
-             ("no noise, no pump", dict(nonlinearity=nl)),
-             ("transforms only", dict())]
-    for ci, (name, kw) in enumerate(cases):
-        if args.pass_case >= 0 and ci != args.pass_case:
-            continue
-        prob = gpe.GrossPitaevskiiProblem((u0,), (64.0, 64.0), dispersion=lambda k, p: (k[0] ** 2 + k[1] ** 2) / 2 - 0.1j,
-                                          **kw)
-        out.append({"workload": "256^2 x 341, one component, FP32", "case": name, **timed(prob, 0.02)})
-    if args.pass_case >= 0:
-        print(json.dumps({"metric": "pass time by term", "runs": out}), flush=True)
-        return
-    disp, nonl, pump = polariton_closures()
-    for dtype, B2 in ((np.complex64, 128), (np.complex128, 64)):
-        z = [np.asfortranarray((0.1 * (rng.standard_normal((N_GRID, N_GRID, B2)) + 1j * rng.standard_normal(
-            (N_GRID, N_GRID, B2)))).astype(dtype)) for _ in range(2)]
-        pump_now = lambda r, p, t: pump(r, p, 100.0)  # a constant amplitude, half the ramp's end value
-        for name, kw in (("all terms", dict(nonlinearity=nonl, pump=pump_now)), ("no pump", dict(nonlinearity=nonl)),
-                         ("transforms only", dict())):
-            prob = gpe.GrossPitaevskiiProblem(tuple(z), (L_BOX, L_BOX), dispersion=disp, **kw)
-            out.append({"workload": f"polariton 512^2 x {B2}, " + ("FP32" if dtype == np.complex64 else "double-word"),
-                        "case": name, **timed(prob, DT)})
-    print(json.dumps({"metric": "pass time by term", "runs": out}), flush=True)
-
-
-def run_twa_group_steps(args):
-    """A handful of plain steps of one TWA group (the capture case for ncu)."""
-    import __graft_entry__ as G
-    G.load_package()
-    T = __import__("gpe_gb300.twa", fromlist=["Ensemble"])
-    prm = T.DampedDrivenParams()
-    N = args.twa_group
-    B = dict(TWA_GROUPS)[N]
-    it = T.make_group(N, B, prm, 100, seed=N, resident=False)
-    it.step(args.steps)
-    print(json.dumps({"grid": [N, N], "trajectories": B, "steps": int(it.state().steps)}), flush=True)
-    it.close()
-
-
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -872,19 +788,13 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--dtype", default="c128", choices=["c128", "c64"])
     ap.add_argument("--batch", type=int, default=0)
-    ap.add_argument("--fp64", default="dw", choices=["dw", "native"],
-                    help="ComplexF64 arithmetic: double-word on the FP32 pipes (default) or native FP64")
+    ap.add_argument("--fp64", default="native", choices=["native", "dw"],
+                    help="ComplexF64 arithmetic: native FP64 (default) or double-word on the FP32 pipes")
+    ap.add_argument("--no-dw", action="store_true", help="skip the double-word measurement beside the FP64 headline")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--twa-steps", type=int, default=2000,
                     help="steps of the batched truncated-Wigner ensemble measurement (0 skips it)")
     ap.add_argument("--no-tune", action="store_true", help="skip the ensemble autotuner")
-    ap.add_argument("--twa-breakdown", action="store_true", help="print per-group TWA step times instead")
-    ap.add_argument("--pass-breakdown", action="store_true",
-                    help="print the row / column pass times of problems that drop one term at a time")
-    ap.add_argument("--pass-case", type=int, default=-1,
-                    help="with --pass-breakdown: run only trajectory case K (0-3) for a few steps, untimed")
-    ap.add_argument("--twa-group", type=int, default=0,
-                    help="run --steps plain steps of the TWA group on this grid (an ncu capture case)")
     ap.add_argument("--no-solve-run", dest="solve_run", action="store_false",
                     help="skip the full-length polariton solve() measurement")
     ap.add_argument("--plain-steps", type=int, default=20,
@@ -911,18 +821,6 @@ def main():
     if args.fno:
         if rank == 0:
             run_fno(args)
-        return
-    if args.twa_breakdown:
-        if rank == 0:
-            run_twa_breakdown(args)
-        return
-    if args.twa_group:
-        if rank == 0:
-            run_twa_group_steps(args)
-        return
-    if args.pass_breakdown:
-        if rank == 0:
-            run_pass_breakdown(args)
         return
     if args.impl == "reference":
         run_reference(args, rank, world)

@@ -1,21 +1,22 @@
 """Builds libgpe.so (the C-ABI library of include/gpe.h) for sm_103a with nvcc.
 
-Each .cu file of csrc/ is compiled to an object in parallel, then linked into
-``libgpe.so`` next to this file.  A rebuild happens only when a source or header is
-newer than the library.
+Each .cu file of csrc/ is compiled to an object in parallel in a temporary directory,
+then linked into ``libgpe.so`` next to this file (only the library stays in the tree).
+A rebuild happens only when a source or header is newer than the library.
 """
 from __future__ import annotations
 
 import os
+import shutil
 import subprocess
 import sys
+import tempfile
 from concurrent.futures import ThreadPoolExecutor
 from pathlib import Path
 
 PKG = Path(__file__).resolve().parent
 CSRC = PKG / "csrc"
 INCLUDE = PKG.parent / "include"
-BUILD = PKG / "_build"
 LIB = PKG / "libgpe.so"
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
@@ -48,12 +49,19 @@ def build(force: bool = False, verbose: bool = False, jobs: int | None = None) -
     """Compile and link libgpe.so; returns its path.  Raises RuntimeError on failure."""
     if not force and up_to_date():
         return LIB
-    BUILD.mkdir(exist_ok=True)
+    build_dir = Path(tempfile.mkdtemp(prefix="gpe_build_"))
+    try:
+        return _build_in(build_dir, verbose, jobs)
+    finally:
+        shutil.rmtree(build_dir, ignore_errors=True)
+
+
+def _build_in(build_dir: Path, verbose: bool, jobs) -> Path:
     nvcc = _nvcc()
     srcs = _sources()
 
     def compile_one(src: Path):
-        obj = BUILD / (src.stem + ".o")
+        obj = build_dir / (src.stem + ".o")
         cmd = [nvcc, *ARCH, *NVCC_FLAGS, "-c", str(src), "-o", str(obj)]
         if verbose:
             print(" ".join(cmd), flush=True)

@@ -50,17 +50,6 @@ __device__ __forceinline__ dw dw_add(dw x, dw y) {
 }
 __device__ __forceinline__ dw dw_neg(dw x) { return {-x.h, -x.l}; }
 __device__ __forceinline__ dw dw_sub(dw x, dw y) { return dw_add(x, dw_neg(y)); }
-// x + y without the closing renormalisation: (s, e) with s = fl(x.h + y.h) and e the
-// exact error of that sum plus the low parts.  The pair is not normalised (|e| may exceed
-// ulp(s)/2, and under cancellation s may be the smaller part), but its value carries the
-// same 2^-47 (|x| + |y|) normwise error bound, which is all an FFT butterfly needs; the
-// next TwoSum or product consumes it unchanged.  Used inside the line transforms, which
-// renormalise once at their end.
-__device__ __forceinline__ dw dw_add_lazy(dw x, dw y) {
-  const dw s = two_sum(x.h, y.h);
-  return {s.h, __fadd_rn(s.l, __fadd_rn(x.l, y.l))};
-}
-__device__ __forceinline__ dw dw_renorm(dw x) { return two_sum(x.h, x.l); }
 // x + y with relative error <= 3u^2 even under cancellation (Alg. 6)
 __device__ __forceinline__ dw dw_add_acc(dw x, dw y) {
   const dw s = two_sum(x.h, y.h);
@@ -98,20 +87,12 @@ __device__ __forceinline__ dwc mk(dw r, dw i) { dwc z; z.xh = r.h; z.xl = r.l; z
 
 __device__ __forceinline__ dwc cadd(dwc a, dwc b) { return mk(dw_add(re(a), re(b)), dw_add(im(a), im(b))); }
 __device__ __forceinline__ dwc csub(dwc a, dwc b) { return mk(dw_sub(re(a), re(b)), dw_sub(im(a), im(b))); }
-__device__ __forceinline__ dwc cadd_lazy(dwc a, dwc b) {
-  return mk(dw_add_lazy(re(a), re(b)), dw_add_lazy(im(a), im(b)));
-}
-__device__ __forceinline__ dwc csub_lazy(dwc a, dwc b) {
-  return mk(dw_add_lazy(re(a), dw_neg(re(b))), dw_add_lazy(im(a), dw_neg(im(b))));
-}
-__device__ __forceinline__ dwc crenorm(dwc a) { return mk(dw_renorm(re(a)), dw_renorm(im(a))); }
 
 // p*q - r*s (or + when SIGN = +1) for double-word p, q, r, s, rounded once: the two
-// high products and their exact errors, the four first-order cross terms, one TwoSum
-// and one FastTwoSum.  Terms of order lo*lo (2^-48 relative) are dropped.  The closing
-// FastTwoSum may see |hs.h| < |e| when the high products cancel; its error is then a
-// rounding of e, itself O(2^-24 (|pq| + |rs|)), so the result keeps the normwise bound
-// O(2^-47 (|pq| + |rs|)).
+// high products and their exact errors, the four first-order cross terms and two
+// TwoSums.  Terms of order lo*lo (2^-48 relative) are dropped.  The closing sum is a full
+// TwoSum: when the high products cancel, |hs.h| may be smaller than the error term e,
+// which a FastTwoSum would not renormalise exactly.
 template <int SIGN>
 __device__ __forceinline__ dw dot2(dw p, dw q, dw r, dw s) {
   const float a = __fmul_rn(p.h, q.h);
@@ -126,7 +107,7 @@ __device__ __forceinline__ dw dot2(dw p, dw q, dw r, dw s) {
   cross = __fmaf_rn(p.h, q.l, cross);
   cross = __fmaf_rn(p.l, q.h, cross);
   const float e = __fadd_rn(__fadd_rn(hs.l, SIGN > 0 ? __fadd_rn(ea, eb) : __fsub_rn(ea, eb)), cross);
-  return fast_two_sum(hs.h, e);
+  return two_sum(hs.h, e);
 }
 __device__ __forceinline__ dwc cmul(dwc a, dwc b) {
   return mk(dot2<-1>(re(a), re(b), im(a), im(b)), dot2<+1>(re(a), im(b), im(a), re(b)));

@@ -20,8 +20,8 @@
 // output index equals the input slot, so no exchange follows it.
 //
 // Twiddles come from a per-length FP64-built table w_N^k = exp(-2 pi i k / N);
-// the inverse uses its conjugate.  The in-register radix-R DFTs use exact
-// constants cos(2 pi k / 16).
+// the inverse uses its conjugate.  The in-register radix-R DFTs use the constants
+// cos(2 pi k / 16) (FP32 passes: as hi/lo pairs, see twc).
 #pragma once
 #include <cuda_runtime.h>
 #include <stdint.h>
@@ -124,6 +124,18 @@ __device__ __forceinline__ C twc(C d) {
       C r; r.x = -d.x; r.y = -d.y; return r;
     } else if constexpr (k == 12) {  // w = -DIR * i
       C r; r.x = DIR * d.y; r.y = -DIR * d.x; return r;
+    } else if constexpr (std::is_same<C, float2>::value) {
+      // FP32: the constant as an FP32 hi/lo pair with FMA corrections, so the product is
+      // the FP32 rounding of d times the exact constant.  Plain FP32 constants are each
+      // rounded once and |c + i s| misses 1 by a fixed amount (-3.4e-8 for cos = sin =
+      // 1/sqrt 2), which every transform of every step repeats: a systematic drift of the
+      // norm that grows linearly in time.
+      constexpr float ch = dwh(cos16(k)), cl = dwl(cos16(k));
+      constexpr float sh = dwh(DIR * sin16(k)), sl = dwl(DIR * sin16(k));
+      float2 r;
+      r.x = __fmaf_rn(d.x, ch, __fmaf_rn(-d.y, sh, __fmaf_rn(d.x, cl, -(d.y * sl))));
+      r.y = __fmaf_rn(d.x, sh, __fmaf_rn(d.y, ch, __fmaf_rn(d.x, sl, d.y * cl)));
+      return r;
     } else {
       using R = decltype(d.x);
       const R c = (R)cos16(k), s = (R)(DIR * sin16(k));
@@ -132,14 +144,14 @@ __device__ __forceinline__ C twc(C d) {
   }
 }
 
-// Butterfly sums: plain for FP32 / FP64; for double-word values the closing
-// renormalisation is deferred to the end of the line transform (fft_line).
+// Butterfly sums.  Double-word sums renormalise every result (dw_add closes with a
+// FastTwoSum), so every value a butterfly passes on is a normalised pair: deferring that
+// renormalisation to the end of the line transform saved 13 % of the double-word step
+// but doubled its distance to FP64 on a collapsing Kerr packet (2048^2, 1000 steps:
+// 1.5e-10 instead of 5.6e-11), which the 1e-10 parity bar does not allow.
 template <typename C> __device__ __forceinline__ C badd(C a, C b) { return cadd(a, b); }
 template <typename C> __device__ __forceinline__ C bsub(C a, C b) { return csub(a, b); }
 template <typename C> __device__ __forceinline__ C bfinish(C a) { return a; }
-template <> __device__ __forceinline__ dwc badd<dwc>(dwc a, dwc b) { return cadd_lazy(a, b); }
-template <> __device__ __forceinline__ dwc bsub<dwc>(dwc a, dwc b) { return csub_lazy(a, b); }
-template <> __device__ __forceinline__ dwc bfinish<dwc>(dwc a) { return crenorm(a); }
 
 // Radix-2 decimation-in-frequency layer of half-size H over an array of R points.
 template <int R, int DIR, int H, int B, int I, typename C>
@@ -266,10 +278,9 @@ __device__ __forceinline__ void fft_stages(C (&x)[E], int t, const Lay& lay, con
 
 // Transform one line held as x[i] = point t + T*i.  DIR = -1 forward (unnormalised),
 // DIR = +1 inverse (unnormalised; the 1/P factor is folded into the k-space table).
-// Every thread of the block must call this the same number of times.  renorm: close the
-// double-word values' deferred renormalisation; a caller whose next step consumes them in
-// double-word products and sums (which take unnormalised pairs at the same normwise
-// bound) leaves it out, and values bound for memory keep it.
+// Every thread of the block must call this the same number of times.  renorm: apply
+// bfinish to the outputs (a no-op for every precision now that double-word butterflies
+// renormalise as they go).
 template <typename C, int N, int E, int DIR, class Lay>
 __device__ __forceinline__ void fft_line(C (&x)[E], int t, const Lay& lay, const C* __restrict__ tw,
                                          bool renorm = true) {

@@ -85,7 +85,7 @@ struct gpe_handle {
   int dev = 0;
   int nsm = 152;  // multiprocessors of dev
   int M = 1, dtype = GPE_C128, ndim = 2;
-  int prec = gpe::PREC_DW;   // pass precision: FP64 fields default to double-word passes
+  int prec = gpe::PREC_F64;  // pass precision: FP64 fields run native FP64 unless GPE_FLAG_FP64_DW
   size_t rsz = 8, csz = 16;  // device bytes per real / complex number
   int64_t n[3] = {1, 1, 1};
   int logn[3] = {0, 0, 0};
@@ -242,6 +242,20 @@ static int upload_complex(gpe_handle* h, void** dst, const cd* src, size_t n) {
   }
   return GPE_OK;
 }
+// Upload n complex FP64 table entries (exp(-i dt D), exp(-i dt/2 V)) at FP64 accuracy in
+// every pass precision: double2 for FP64 passes, {re.hi, re.lo, im.hi, im.lo} floats for
+// the double-word and FP32 passes (16 bytes an entry either way).
+static int upload_table(gpe_handle* h, void** dst, const cd* src, size_t n) {
+  if (!*dst) CK(h, cudaMalloc(dst, n * 16));
+  if (h->prec == gpe::PREC_F64) {
+    CK(h, cudaMemcpy(*dst, src, n * 16, cudaMemcpyHostToDevice));
+  } else {
+    std::vector<float> tmp(4 * n);
+    for (size_t i = 0; i < n; ++i) { split_dw(src[i].real(), &tmp[4 * i]); split_dw(src[i].imag(), &tmp[4 * i + 2]); }
+    CK(h, cudaMemcpy(*dst, tmp.data(), n * 16, cudaMemcpyHostToDevice));
+  }
+  return GPE_OK;
+}
 // Upload n real FP64 values (double, float, or a {hi, lo} float pair).
 static int upload_real(gpe_handle* h, void** dst, const double* src, size_t n) {
   if (!*dst) CK(h, cudaMalloc(dst, n * h->rsz));
@@ -347,6 +361,10 @@ int gpe_create(const gpe_desc* desc, gpe_handle** out) {
   if (desc->ncomp < 1 || desc->ncomp > 2) return fail(nullptr, GPE_ERR_UNSUPPORTED, "ncomp must be 1 or 2");
   if (desc->dtype != GPE_C128 && desc->dtype != GPE_C64) return fail(nullptr, GPE_ERR_INVALID, "bad dtype");
   if (desc->batch < 1) return fail(nullptr, GPE_ERR_INVALID, "batch must be >= 1");
+  if ((desc->flags & GPE_FLAG_FP64_DW) && (desc->flags & GPE_FLAG_FP64_NATIVE))
+    return fail(nullptr, GPE_ERR_INVALID, "GPE_FLAG_FP64_DW and GPE_FLAG_FP64_NATIVE exclude each other");
+  if ((desc->flags & GPE_FLAG_FP64_DW) && desc->dtype != GPE_C128)
+    return fail(nullptr, GPE_ERR_INVALID, "GPE_FLAG_FP64_DW applies to GPE_C128 fields only");
   if (!(desc->dt > 0) || !std::isfinite(desc->dt)) return fail(nullptr, GPE_ERR_INVALID, "dt must be positive and finite");
   if (!std::isfinite(desc->t0)) return fail(nullptr, GPE_ERR_INVALID, "t0 must be finite");
   for (int a = 0; a < desc->ndim; ++a) {
@@ -370,7 +388,7 @@ int gpe_create(const gpe_desc* desc, gpe_handle** out) {
   h->M = desc->ncomp;
   h->dtype = desc->dtype;
   h->ndim = desc->ndim;
-  h->prec = desc->dtype == GPE_C64 ? gpe::PREC_F32 : ((desc->flags & GPE_FLAG_FP64_NATIVE) ? gpe::PREC_F64 : gpe::PREC_DW);
+  h->prec = desc->dtype == GPE_C64 ? gpe::PREC_F32 : ((desc->flags & GPE_FLAG_FP64_DW) ? gpe::PREC_DW : gpe::PREC_F64);
   h->rsz = desc->dtype == GPE_C128 ? 8 : 4;
   h->csz = 2 * h->rsz;
   h->B = desc->batch;
@@ -578,7 +596,7 @@ static int store_ktable(gpe_handle* h, const std::vector<cd>& tab, int kind) {
   cudaFree(h->ktab);
   h->ktab = nullptr;
   h->kkind = GPE_TABLE_NONE;
-  int rc = upload_complex(h, &h->ktab, tab.data(), tab.size());
+  int rc = upload_table(h, &h->ktab, tab.data(), tab.size());
   if (rc) return rc;
   h->kkind = kind;
   return GPE_OK;
@@ -629,7 +647,7 @@ static int store_vtable(gpe_handle* h, const std::vector<cd>& tab, int kind) {
   cudaFree(h->vtab);
   h->vtab = nullptr;
   h->vkind = GPE_TABLE_NONE;
-  int rc = upload_complex(h, &h->vtab, tab.data(), tab.size());
+  int rc = upload_table(h, &h->vtab, tab.data(), tab.size());
   if (rc) return rc;
   h->vkind = kind;
   return GPE_OK;
@@ -1731,8 +1749,13 @@ int gpe_wait(gpe_handle* h) {
   return take_status(h);
 }
 
+// the bound of every device wait in the library (gpe::kWaitLimitNs in tma.cuh)
+static constexpr int64_t kProbeWaitLimitNs = 1000000000;
+
 int gpe_selftest_wait(int device, int arrive, int64_t limit_ns) {
-  if (limit_ns < 0) return GPE_ERR_INVALID;
+  // the probe's wait must end on its own: limits above the library's own bound (1 s)
+  // are refused, so no caller can make it spin for longer
+  if (limit_ns < 0 || limit_ns > kProbeWaitLimitNs) return GPE_ERR_INVALID;
   if (cudaSetDevice(device < 0 ? 0 : device) != cudaSuccess) return GPE_ERR_CUDA;
   int32_t *hs = nullptr, *ds = nullptr;
   if (cudaHostAlloc((void**)&hs, sizeof(int32_t), cudaHostAllocMapped) != cudaSuccess) return GPE_ERR_NOMEM;

@@ -243,6 +243,25 @@ __device__ __forceinline__ double2 cunit_(double2*) { return make_double2(1.0, 0
 __device__ __forceinline__ dwc cunit_(dwc*) { return mk(dw{1.0f, 0.0f}, dw{0.0f, 0.0f}); }
 template <typename C> __device__ __forceinline__ C cunit() { return cunit_((C*)nullptr); }
 
+// Phase tables (k-space exp(-i dt D)/P, real-space exp(-i dt/2 V)) keep FP64 accuracy in
+// every precision: FP64 passes read double2, double-word and FP32 passes read hi/lo float
+// pairs (t = hi + lo, 16 bytes, the double-word layout).  FP32 passes apply such a table
+// entry to an FP32 value with FMA corrections, so the product is the FP32 rounding of the
+// product with the FP64 entry (within a few units of the last place, unbiased) -- as the
+// reference's ComplexF32 path, where the ComplexF64 table promotes the product to FP64
+// before it is stored in FP32 (src/misc.jl:16, src/kernels.jl:44-53).  A table rounded
+// to FP32 instead would carry a fixed error per entry that every step repeats.
+template <typename Real> struct TabT { using T = dwc; };
+template <> struct TabT<double> { using T = double2; };
+__device__ __forceinline__ double2 tmul(const double2& t, const double2& v) { return cmul(t, v); }
+__device__ __forceinline__ dwc tmul(const dwc& t, const dwc& v) { return cmul(t, v); }
+__device__ __forceinline__ float2 tmul(const dwc& t, const float2& v) {
+  float2 r;
+  r.x = __fmaf_rn(v.x, t.xh, __fmaf_rn(-v.y, t.yh, __fmaf_rn(v.x, t.xl, -(v.y * t.yl))));
+  r.y = __fmaf_rn(v.x, t.yh, __fmaf_rn(v.y, t.xh, __fmaf_rn(v.x, t.yl, v.y * t.xl)));
+  return r;
+}
+
 // whether half_step applies component j's two pump terms as one (no E multiplies it)
 __device__ __forceinline__ bool pump_merged(const PassArgs& a, int j) {
   return !a.nl_on[j] && a.vkind == TAB_NONE;
@@ -366,14 +385,15 @@ __device__ __forceinline__ void matrix_phase(const typename CT<Real>::T (&u)[2],
     G[ab] = {__ldg(c) + __ldg(g) * d0 + __ldg(g + 2) * d1, __ldg(c + 1) + __ldg(g + 1) * d0 + __ldg(g + 3) * d1};
   }
   expm2_dev(G, 0.5 * a.dt, E);
+  using TT = typename TabT<Real>::T;
   if (a.vkind == TAB_SCALAR) {
-    const cd2 v = to_cd2(ldgc((const C*)a.vtab + p));
+    const cd2 v = to_cd2(ldgc((const TT*)a.vtab + p));
 #pragma unroll
     for (int q = 0; q < 4; ++q) E[q] = cdmul(E[q], v);
   } else if (a.vkind == TAB_MATRIX) {
     cd2 V[4];
 #pragma unroll
-    for (int q = 0; q < 4; ++q) V[q] = to_cd2(ldgc((const C*)a.vtab + (int64_t)q * a.P + p));
+    for (int q = 0; q < 4; ++q) V[q] = to_cd2(ldgc((const TT*)a.vtab + (int64_t)q * a.P + p));
     const cd2 r0 = cdadd(cdmul(E[0], V[0]), cdmul(E[1], V[2]));
     const cd2 r1 = cdadd(cdmul(E[0], V[1]), cdmul(E[1], V[3]));
     const cd2 r2 = cdadd(cdmul(E[2], V[0]), cdmul(E[3], V[2]));
@@ -460,19 +480,23 @@ __device__ __forceinline__ void half_step(typename CT<Real>::T (&u)[M], const Pa
       }
     }
   }
-  if (a.vkind == TAB_SCALAR) {
-    const C v = ldgc((const C*)a.vtab + p);
+  // real-space table.  FP64 and double-word passes fold it into E (E = cis(-delta G) V,
+  // the reference's order); FP32 passes apply it as its own FMA-corrected product after
+  // cis(-delta G), so it keeps its FP64 accuracy (an FP32 E V would round it)
+  using TT = typename TabT<Real>::T;
+  constexpr bool SEPV = std::is_same<Real, float>::value;
+  TT vt[SEPV ? M : 1];
+  const bool hasV = SEPV && (a.vkind == TAB_SCALAR || a.vkind == TAB_DIAG);
+  if (a.vkind == TAB_SCALAR || a.vkind == TAB_DIAG) {
 #pragma unroll
     for (int j = 0; j < M; ++j) {
-      E[j] = hasE[j] ? cmul(E[j], v) : v;
-      hasE[j] = true;
-    }
-  } else if (a.vkind == TAB_DIAG) {
-#pragma unroll
-    for (int j = 0; j < M; ++j) {
-      const C v = ldgc((const C*)a.vtab + (int64_t)j * a.P + p);
-      E[j] = hasE[j] ? cmul(E[j], v) : v;
-      hasE[j] = true;
+      const TT v = ldgc((const TT*)a.vtab + (a.vkind == TAB_DIAG ? (int64_t)j * a.P : 0) + p);
+      if constexpr (SEPV) {
+        vt[j] = v;
+      } else {
+        E[j] = hasE[j] ? cmul(E[j], v) : v;
+        hasE[j] = true;
+      }
     }
   }
   C prof[M];
@@ -491,17 +515,21 @@ __device__ __forceinline__ void half_step(typename CT<Real>::T (&u)[M], const Pa
   }
   if (a.vkind == TAB_MATRIX && M == 2) {
     // matrix potential with no nonlinearity: mat-vec with the per-point 2x2 table
-    const C* vt = (const C*)a.vtab;
-    const C t00 = ldgc(vt + p), t01 = ldgc(vt + a.P + p);
-    const C t10 = ldgc(vt + 2 * a.P + p), t11 = ldgc(vt + 3 * a.P + p);
-    const C y0 = cadd(cmul(t00, u[0]), cmul(t01, u[M - 1]));
-    const C y1 = cadd(cmul(t10, u[0]), cmul(t11, u[M - 1]));
+    const TT* mt = (const TT*)a.vtab;
+    const TT t00 = ldgc(mt + p), t01 = ldgc(mt + a.P + p);
+    const TT t10 = ldgc(mt + 2 * a.P + p), t11 = ldgc(mt + 3 * a.P + p);
+    const C y0 = cadd(tmul(t00, u[0]), tmul(t01, u[M - 1]));
+    const C y1 = cadd(tmul(t10, u[0]), tmul(t11, u[M - 1]));
     u[0] = y0;
     u[M - 1] = y1;
   } else {
 #pragma unroll
-    for (int j = 0; j < M; ++j)
+    for (int j = 0; j < M; ++j) {
       if (hasE[j]) u[j] = cmul(E[j], u[j]);
+      if constexpr (SEPV) {
+        if (hasV) u[j] = tmul(vt[j], u[j]);
+      }
+    }
   }
 #pragma unroll
   for (int j = 0; j < M; ++j)
@@ -537,24 +565,25 @@ __device__ __forceinline__ void half_step(typename CT<Real>::T (&u)[M], const Pa
 template <typename Real, int M>
 __device__ __forceinline__ void kmul(typename CT<Real>::T (&v)[M], const PassArgs& a, int64_t kp) {
   using C = typename CT<Real>::T;
-  const C* kt = (const C*)a.ktab;
+  using TT = typename TabT<Real>::T;
+  const TT* kt = (const TT*)a.ktab;
   if (a.kkind == TAB_SCALAR) {
-    const C k = ldgc(kt + kp);
+    const TT k = ldgc(kt + kp);
 #pragma unroll
-    for (int m = 0; m < M; ++m) v[m] = cmul(k, v[m]);
+    for (int m = 0; m < M; ++m) v[m] = tmul(k, v[m]);
   } else if (a.kkind == TAB_DIAG) {
 #pragma unroll
-    for (int m = 0; m < M; ++m) v[m] = cmul(ldgc(kt + (int64_t)m * a.P + kp), v[m]);
+    for (int m = 0; m < M; ++m) v[m] = tmul(ldgc(kt + (int64_t)m * a.P + kp), v[m]);
   } else if (a.kkind == TAB_MATRIX) {
     if constexpr (M == 2) {
-      const C t00 = ldgc(kt + kp), t01 = ldgc(kt + a.P + kp);
-      const C t10 = ldgc(kt + 2 * a.P + kp), t11 = ldgc(kt + 3 * a.P + kp);
-      const C y0 = cadd(cmul(t00, v[0]), cmul(t01, v[1]));
-      const C y1 = cadd(cmul(t10, v[0]), cmul(t11, v[1]));
+      const TT t00 = ldgc(kt + kp), t01 = ldgc(kt + a.P + kp);
+      const TT t10 = ldgc(kt + 2 * a.P + kp), t11 = ldgc(kt + 3 * a.P + kp);
+      const C y0 = cadd(tmul(t00, v[0]), tmul(t01, v[1]));
+      const C y1 = cadd(tmul(t10, v[0]), tmul(t11, v[1]));
       v[0] = y0;
       v[1] = y1;
     } else {
-      v[0] = cmul(ldgc(kt + kp), v[0]);
+      v[0] = tmul(ldgc(kt + kp), v[0]);
     }
   }
 }

@@ -118,16 +118,57 @@ def as_array(val, shape) -> np.ndarray:
         return np.broadcast_to(a, shape)
     return a
 
+def _value_at(vals: np.ndarray, gshape, idx):
+    """The entries of a whole-grid closure result at the grid multi-index idx."""
+    nd = len(gshape)
+    if vals.ndim >= nd and vals.shape[vals.ndim - nd:] == gshape:
+        return vals[(Ellipsis,) + tuple(idx)]
+    return np.broadcast_to(vals, vals.shape[:max(vals.ndim - nd, 0)] + gshape)[(Ellipsis,) + tuple(idx)]
+
+
+def _agrees_per_point(f: Callable, coords, vals, args) -> bool:
+    """Whether the whole-grid result of f equals f called on single points (a corner, the
+    centre and one seeded random point).  A closure written for one point can run on the
+    coordinate arrays without an error and still compute something else there: a
+    reduction such as np.linalg.norm(r) then spans the whole grid instead of one point."""
+    gshape = coords[0].shape
+    if int(np.prod(gshape)) <= 1:
+        return True
+    rng = np.random.default_rng(20240607)
+    picks = [tuple(0 for _ in gshape), tuple(n // 2 for n in gshape), tuple(int(rng.integers(n)) for n in gshape)]
+    try:
+        arr = as_array(vals, gshape)
+    except (TypeError, ValueError):
+        return False
+    for idx in picks:
+        pt = tuple(float(c[idx]) for c in coords)
+        try:
+            one = as_array(f(pt, *args), ())
+        except Exception:
+            return True  # the closure only works on arrays: nothing to compare against
+        try:
+            got = _value_at(arr, gshape, idx)
+            ok = np.shape(got) == np.shape(one) and np.allclose(got, one, rtol=1e-10, atol=1e-300)
+        except (TypeError, ValueError):
+            ok = False
+        if not ok:
+            return False
+    return True
+
+
 def eval_on_grid(f: Callable, coords, *args):
     """A closure over the grid: called once with the coordinate arrays when it takes
-    them (numpy arithmetic), else once per point with a tuple of floats, as grid_map!
-    calls it (src/misc.jl:1-10) -- closures written for one point (math functions,
-    branches on a coordinate) then work unchanged.  Returns an array of shape
+    them (numpy arithmetic) and gives there what it gives point by point, else once per
+    point with a tuple of floats, as grid_map! calls it (src/misc.jl:1-10) -- closures
+    written for one point (math functions, branches on a coordinate, reductions over the
+    point's coordinates such as norm(r)) then work unchanged.  Returns an array of shape
     (entries..., *grid)."""
     try:
-        return f(coords, *args)
+        vals = f(coords, *args)
     except (TypeError, ValueError):
-        pass
+        vals = None
+    if vals is not None and _agrees_per_point(f, coords, vals, args):
+        return vals
     gshape = coords[0].shape
     flat = [np.ravel(c) for c in coords]
     vals = np.stack([as_array(f(tuple(float(c[i]) for c in flat), *args), ()) for i in range(flat[0].size)], -1)

@@ -67,7 +67,7 @@ class StrangSplittingIterator:
 
     def __init__(self, prob: GrossPitaevskiiProblem, tspan, *, dt, nsaves, save_start=True, rng=None,
                  noise_replay: Optional[Callable] = None, total_steps: Optional[int] = None,
-                 device: int = -1, fp64: str = "dw", resident: bool = True, variant: Optional[int] = None,
+                 device: int = -1, fp64: str = "native", resident: bool = True, variant: Optional[int] = None,
                  tma: Optional[bool] = None):
         self.lib = L.load()
         self.variant = variant
@@ -97,8 +97,10 @@ class StrangSplittingIterator:
         d.t0 = self.t0
         d.device = device
         if fp64 not in ("dw", "native"):
-            raise ValueError("fp64 must be 'dw' (double-word on the FP32 pipes) or 'native'")
-        d.flags = ((L.GPE_FLAG_FP64_NATIVE if fp64 == "native" else 0) | (0 if resident else L.GPE_FLAG_NO_RESIDENT)
+            raise ValueError("fp64 must be 'native' (FP64 instructions, the default) or 'dw' (double-word on the "
+                             "FP32 pipes)")
+        self.fp64 = fp64 if self.dtype == np.complex128 else None
+        d.flags = ((L.GPE_FLAG_FP64_DW if self.fp64 == "dw" else 0) | (0 if resident else L.GPE_FLAG_NO_RESIDENT)
                    | (0 if tma is None else L.GPE_FLAG_TMA if tma else L.GPE_FLAG_NO_TMA))
         h = ctypes.c_void_p()
         rc = self.lib.gpe_create(ctypes.byref(d), ctypes.byref(h))
@@ -277,14 +279,15 @@ class StrangSplittingIterator:
 
 
 def init(prob: GrossPitaevskiiProblem, alg: StrangSplitting, tspan, *, dt, nsaves, show_progress=False,
-         progress=None, save_start=True, workgroup_size=(), rng=None, noise_replay=None, fp64="dw", device=-1,
+         progress=None, save_start=True, workgroup_size=(), rng=None, noise_replay=None, fp64="native", device=-1,
          resident=True, variant=None, tma=None):
     """init(prob, StrangSplitting(), tspan; dt, nsaves, ...) (src/strang_splitting.jl:32-67).
     show_progress / progress / workgroup_size are accepted for signature parity and
     have no effect: the backend picks its own launch shapes.  Extra keywords: ``rng``
     (Philox seed or numpy Generator), ``noise_replay`` (callable h -> xi for replayed
-    noise), ``fp64`` ("dw": ComplexF64 fields advanced in double-word arithmetic on the
-    FP32 pipes, the default; "native": FP64 instructions), ``device`` (CUDA ordinal),
+    noise), ``fp64`` (ComplexF64 fields: "native", FP64 instructions as the reference's
+    Float64 arithmetic, the default; "dw", the opt-in fast mode in double-word arithmetic
+    on the FP32 pipes, unit roundoff 2^-48; ignored for ComplexF32), ``device`` (CUDA ordinal),
     ``resident`` (False forces the two-pass HBM path for small square 2D grids),
     ``variant`` (line tiling of the two-pass passes, see gpe_set_variant; None lets the
     library choose by field size), ``tma`` (TMA staging of 2D column tiles: True wherever

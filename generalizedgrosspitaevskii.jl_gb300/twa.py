@@ -147,20 +147,41 @@ def momentum_statistics(it: StrangSplittingIterator, commutator: float, comp: in
     return nk, G2, G2 / np.outer(nk, nk)
 
 
-def local_moment_sums(fields: np.ndarray, batch_axis: int = -1):
-    """Per-site sums over the local trajectories: (count, sum |u|^2, sum |u|^4) in FP64."""
+def local_moments(fields: np.ndarray, batch_axis: int = -1):
+    """Per-site moments of n = |u|^2 over the local trajectories, in FP64: (count, mean,
+    M2) with M2 = sum (n - mean)^2, each formed in two passes (mean first), so the spread
+    keeps its digits when it is small next to the mean density."""
     n = np.abs(np.asarray(fields).astype(np.complex128)) ** 2
     n = np.moveaxis(n, batch_axis, 0)
-    return n.shape[0], n.sum(axis=0), (n * n).sum(axis=0)
+    mean = n.mean(axis=0)
+    return n.shape[0], mean, ((n - mean) ** 2).sum(axis=0)
+
+
+def merge_moments(parts):
+    """Chan, Golub and LeVeque's pairwise update ("Updating formulae and a pairwise
+    algorithm for computing sample variances", 1979) over (count, mean, M2) triples, in
+    the order given: n = na + nb, d = mean_b - mean_a, mean = mean_a + d nb / n,
+    M2 = M2_a + M2_b + d^2 na nb / n."""
+    na, ma, qa = parts[0]
+    for nb, mb, qb in parts[1:]:
+        if nb == 0:
+            continue
+        n = na + nb
+        d = mb - ma
+        ma = ma + d * (nb / n)
+        qa = qa + qb + d * d * (na * nb / n)
+        na = n
+    return na, ma, qa
 
 
 def allreduce_moments(fields: np.ndarray, group=None, batch_axis: int = -1):
-    """Ensemble mean and variance of |u|^2 per site when the trajectories are sharded over
-    ranks (one process per GPU, each advancing its own trajectories with no exchange
-    during the run).  The one collective is this all-reduce of (count, sum n, sum n^2)
-    in FP64 over torch.distributed (NCCL or gloo).  Without an initialised process group
-    it reduces the local trajectories only."""
-    cnt, s1, s2 = local_moment_sums(fields, batch_axis)
+    """Ensemble mean and variance (population, ddof 0) of |u|^2 per site when the
+    trajectories are sharded over ranks (one process per GPU, each advancing its own
+    trajectories with no exchange during the run).  The one collective is an all-gather
+    of every rank's (count, mean, M2) in FP64 over torch.distributed (NCCL or gloo); each
+    rank merges them in rank order with Chan's pairwise formula, so every rank gets the
+    same bits.  Without an initialised process group it uses the local trajectories only."""
+    cnt, mean, m2 = local_moments(fields, batch_axis)
     try:
         import torch
         import torch.distributed as dist
@@ -168,13 +189,14 @@ def allreduce_moments(fields: np.ndarray, group=None, batch_axis: int = -1):
     except ImportError:
         active = False
     if active:
-        buf = torch.from_numpy(np.concatenate([[float(cnt)], s1.ravel(), s2.ravel()]))
-        if dist.get_backend(group) == "nccl":  # NCCL reduces device tensors only
+        buf = torch.from_numpy(np.concatenate([[float(cnt)], mean.ravel(), m2.ravel()]))
+        if dist.get_backend(group) == "nccl":  # NCCL moves device tensors only
             buf = buf.to(torch.device("cuda", torch.cuda.current_device()))
-        dist.all_reduce(buf, op=dist.ReduceOp.SUM, group=group)
-        v = buf.cpu().numpy()
-        cnt = v[0]
-        s1 = v[1:1 + s1.size].reshape(s1.shape)
-        s2 = v[1 + s1.size:].reshape(s1.shape)
-    mean = s1 / cnt
-    return mean, s2 / cnt - mean * mean
+        parts = [torch.empty_like(buf) for _ in range(dist.get_world_size(group))]
+        dist.all_gather(parts, buf, group=group)
+        triples = []
+        for v in parts:
+            v = v.cpu().numpy()
+            triples.append((v[0], v[1:1 + mean.size].reshape(mean.shape), v[1 + mean.size:].reshape(mean.shape)))
+        cnt, mean, m2 = merge_moments(triples)
+    return mean, m2 / cnt

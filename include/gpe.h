@@ -47,14 +47,19 @@ extern "C" {
 #define GPE_ERR_NOMEM (-6)       /* device allocation failed */
 
 /* field precision */
-#define GPE_C128 0 /* ComplexF64 fields, FP64-accurate arithmetic (see GPE_FLAG_FP64_NATIVE) */
-#define GPE_C64 1  /* ComplexF32 fields, FP32 arithmetic, FP64 tables/time built on host */
+#define GPE_C128 0 /* ComplexF64 fields, native FP64 arithmetic (the reference's Float64) */
+#define GPE_C64 1  /* ComplexF32 fields, FP32 arithmetic; FP64 tables, times and reductions */
 
 /* gpe_desc.flags */
-/* GPE_C128 runs by default on the FP32 pipes in double-word arithmetic (pairs of floats,
- * 48-bit significands, unit roundoff 2^-48): GB300 issues FP32 FMAs 62x faster than FP64
- * ones.  With this flag the passes use native FP64 instead. */
+/* GPE_C128 runs in native FP64 by default, the arithmetic of the reference's ComplexF64
+ * path.  This flag states that default explicitly. */
 #define GPE_FLAG_FP64_NATIVE 1
+/* Opt-in fast mode for GPE_C128: the passes run on the FP32 pipes in double-word
+ * arithmetic (pairs of floats, 48-bit significands, unit roundoff 2^-48, narrower than
+ * FP64's 2^-53; GB300 issues FP32 FMAs 62x faster than FP64 ones).  The state, the saves
+ * and every result still cross this ABI as FP64.  Cannot be combined with
+ * GPE_FLAG_FP64_NATIVE. */
+#define GPE_FLAG_FP64_DW 16
 /* Square 2D fields small enough for one CTA's shared memory (FP32 up to 128x128 with one
  * component, 16-byte types up to 64x64) run every step of a gpe_run call in one resident
  * launch, one CTA per trajectory.  This flag forces the two-pass HBM path instead. */
@@ -229,7 +234,8 @@ int gpe_wait(gpe_handle* h);
 /* Probe of the bounded device wait the TMA column pass relies on: one CTA waits on an
  * mbarrier with limit_ns as its limit.  arrive = 0: nothing completes the barrier, the
  * wait runs out and the call returns GPE_ERR_TIMEOUT with the context still usable;
- * arrive = 1: the barrier completes and the call returns GPE_OK. */
+ * arrive = 1: the barrier completes and the call returns GPE_OK.  limit_ns must lie in
+ * [0, 1e9] (the library's own wait bound, 1 s); anything else is GPE_ERR_INVALID. */
 int gpe_selftest_wait(int device, int arrive, int64_t limit_ns);
 /* Several handles (e.g. trajectory groups on grids of different sizes) advanced together
  * by ONE captured CUDA graph: each handle's chunk of steps_per_graph steps runs on its own
@@ -273,7 +279,9 @@ int64_t gpe_last_run_launches(const gpe_handle* h);
  * 65535) is rejected with GPE_ERR_INVALID.  Nothing is allocated: no cudaMalloc, no
  * cudaFree, no allocating library routine.  The first call on a device looks up the
  * array's device address (cudaGetSymbolAddress, with that device current), so make it
- * before any stream capture.  The call is synchronous on the legacy default stream.
+ * before any stream capture.  That address is kept for the life of the process: do not
+ * call this entry point after cudaDeviceReset (or anything else that destroys and
+ * recreates the device's primary context), whose new context places the array elsewhere.  The call is synchronous on the legacy default stream.
  * Every call shares the one array and overwrites the slots it uses, so calls that
  * overlap on the GPU (from several host threads or streams) race.  Errors are
  * described by gpe_noalloc_last_error() (per host thread). */

@@ -8,6 +8,7 @@
  */
 #include <math.h>
 #include <stdio.h>
+#include <string.h>
 #include <stdlib.h>
 
 #include "gpe.h"
@@ -44,7 +45,7 @@ int main(int argc, char** argv) {
   d.dt = dt;
   d.t0 = 0.0;
   d.device = -1;
-  d.flags = (argc > 2) ? GPE_FLAG_FP64_NATIVE : 0;
+  d.flags = (argc > 2 && strcmp(argv[2], "dw") == 0) ? GPE_FLAG_FP64_DW : 0; /* native FP64 by default */
   gpe_handle* h = NULL;
   CHECK(NULL, gpe_create(&d, &h));
 

@@ -116,6 +116,15 @@ def test_create_rejects_bad_descriptors(lib, gpe, kw, code):
     assert lib.gpe_last_error(None)
 
 
+def test_wait_probe_refuses_limits_beyond_one_second(lib, gpe):
+    """gpe_selftest_wait checks its limit before it touches the device, so a caller cannot
+    make the probe spin for longer than the library's own wait bound."""
+    L = gpe._lib
+    assert lib.gpe_selftest_wait(0, 0, 10 ** 9 + 1) == L.GPE_ERR_INVALID
+    assert lib.gpe_selftest_wait(0, 0, -1) == L.GPE_ERR_INVALID
+    assert lib.gpe_selftest_wait(0, 1, 2 ** 63 - 1) == L.GPE_ERR_INVALID
+
+
 def test_null_arguments(lib, gpe):
     assert lib.gpe_create(None, None) == -1
     assert lib.gpe_destroy(None) == 0

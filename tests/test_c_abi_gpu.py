@@ -21,7 +21,7 @@ def test_plain_case_from_c(gpe, lib, tmp_path, mode):
     subprocess.run(["gcc", "-O2", "-I", str(ROOT / "include"), str(ROOT / "tests" / "c_abi" / "kerr_c0.c"),
                     f"-L{libdir}", "-lgpe", f"-Wl,-rpath,{libdir}", "-lm", "-o", str(exe)], check=True)
     out = tmp_path / "out.bin"
-    args = [str(exe), str(out)] + (["native"] if mode == "native" else [])
+    args = [str(exe), str(out)] + (["dw"] if mode == "dw" else [])
     r = subprocess.run(args, capture_output=True, text=True, timeout=300)
     assert r.returncode == 0, r.stderr
     raw = np.fromfile(out, np.float64)

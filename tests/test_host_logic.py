@@ -115,6 +115,16 @@ class _FakeLib:
         self.steps += nsteps
         return 0
 
+    def gpe_run_ex(self, h, nsteps, save_every, xi, out, stride, ts):
+        import ctypes
+        if any(len(a) > 1 and len(a) < 2 * (self.steps + nsteps) + 1 for a in self.amps.values()):
+            return -1
+        ns = nsteps // save_every
+        t = np.frombuffer((ctypes.c_double * ns).from_address(ts), np.float64)
+        t[:] = 0.1 * (self.steps + save_every * np.arange(1, ns + 1))  # the handle's time: t0 + steps * dt
+        self.steps += nsteps
+        return 0
+
     def gpe_last_error(self, h):
         return b"pump schedule too short"
 
@@ -308,8 +318,40 @@ def test_per_point_closures_match_array_closures(gpe):
                            ax, None, 2, times)
     assert pb[1] is None
     assert np.allclose(aa[0][:, None] * pa[0][None], ab[0][:, None] * pb[0][None], rtol=1e-14, atol=1e-16)
+    # closures that reduce over the point's coordinates (norm(r), the natural form of code
+    # ported from Julia) run on the coordinate arrays without an error but reduce over the
+    # whole grid there: they must still sample point by point
+    a, ka = sample_table(lambda r, p: 0.5 * (r[0] ** 2 + r[1] ** 2), ax, None, 1)
+    b, kb = sample_table(lambda r, p: 0.5 * np.linalg.norm(r) ** 2, ax, None, 1)
+    assert ka == kb and np.allclose(a, b, rtol=1e-13, atol=0) and np.ptp(b.real) > 0
+    pa, aa = classify_pump(lambda r, p, t: min(t, 1.0) * np.exp(-((r[0] - 8) ** 2 + (r[1] - 8) ** 2) / 9),
+                           ax, None, 1, times)
+    pb, ab = classify_pump(lambda r, p, t: min(t, 1.0) * np.exp(-np.linalg.norm(np.asarray(r) - 8.0) ** 2 / 9),
+                           ax, None, 1, times)
+    assert pb[0] is not None
+    assert np.allclose(aa[0][:, None] * pa[0][None], ab[0][:, None] * pb[0][None], rtol=1e-13, atol=1e-16)
     for shape in ((16,), (16, 8, 4)):
         axes = tuple(direct_grid_axis(3.0 + a, n) for a, n in enumerate(shape))
         a, _ = sample_table(lambda r, p: np.exp(-sum((x - 1.0) ** 2 for x in r)) * (r[-1] + 1), axes, None, 1)
         b, _ = sample_table(lambda r, p: math.exp(-math.fsum((x - 1.0) ** 2 for x in r)) * (r[-1] + 1), axes, None, 1)
         assert np.allclose(a, b, rtol=1e-15, atol=0), shape
+
+
+def test_solve_after_step_continues_from_the_handle(gpe, monkeypatch):
+    """solve_ after step continues the handle's clock: its saves and times follow the k
+    steps already taken, and the pump schedule is extended to cover them.  (The
+    reference's solve! restarts t at tspan[1] while keeping the advanced field; the
+    difference is documented with the iterator form of the C ABI.)"""
+    fake = _FakeLib()
+    monkeypatch.setattr(gpe._lib, "load", lambda path=None: fake)
+    N, Lb, dt = 16, 8.0, 0.1
+    prob = gpe.GrossPitaevskiiProblem((np.zeros((N, N), np.complex128),), (Lb, Lb),
+                                      dispersion=lambda k, p: (k[0] ** 2 + k[1] ** 2) / 2,
+                                      pump=lambda r, p, t: min(t, 1.0) * np.exp(-((r[0] - 4) ** 2 + (r[1] - 4) ** 2)))
+    it = gpe.init(prob, gpe.StrangSplitting(), (0.0, 1.0), dt=dt, nsaves=2)
+    gpe.step(it, 3)
+    ts, _ = gpe.solve_(it)
+    assert fake.steps == 13
+    assert np.allclose(ts, [0.0, 0.8, 1.3])  # u0's slot keeps t0; the saves follow the 3 steps taken
+    assert len(fake.amps[0]) >= 2 * 13 + 1
+    it.close()

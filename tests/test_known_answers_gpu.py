@@ -1,0 +1,169 @@
+"""The reference's own known-answer tests, run through the GPU path (gpe.solve on
+libgpe) at the reference's parameters and tolerances, in native FP64 (the ComplexF64
+default), in the double-word mode and with ComplexF32 fields:
+
+* test/bistability_cycle.jl:1-71 -- the full 1D cycle to t = 3300 against the analytic
+  bistability curve (mean error over saves 140..400 <= 3e-3), and the 27 closure-shape
+  variants of :67-71 (scalar / SVector / SMatrix{1,1} dispersion, nonlinearity and pump)
+  equal to the base run at Julia's isapprox (rel L2 <= sqrt(eps));
+* test/exciton_polariton_test.jl:1-53 -- the two-component polariton at 128^2 to t = 100
+  and its two steady-state relations at the pump centre within 3e-2;
+* test/windowed_ft.jl:22-99 -- the truncated-Wigner vacuum, 10^4 trajectories with the
+  in-kernel Philox generator, windowed-FT correlation against the analytic commutator at
+  rtol 7e-2 (the acceptance test of a noise generator).
+
+These are the only assertions the reference holds for this path (it stores no golden
+vectors), so they pin the GPU path to the reference directly, independent of the oracle.
+"""
+import math
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+MODES = [(np.complex128, "native"), (np.complex128, "dw"), (np.complex64, "native")]
+IDS = ["f64", "f64-dw", "f32"]
+ISAPPROX = math.sqrt(np.finfo(np.float64).eps)  # Julia's default rtol for Float64 arrays
+
+
+def rel_l2(a, b):
+    den = max(np.linalg.norm(a), np.linalg.norm(b))
+    return 0.0 if den == 0 else float(np.linalg.norm(a - b) / den)
+
+
+# ------------------------------------------------------------------ bistability cycle
+BI = dict(w0=1483.0, g=0.01, d=0.3, kz=27.0, gam=0.1, L=256.0, N=256, Imax=0.6, width=50.0, tmax=3300.0)
+BI["wp"] = BI["w0"] + BI["d"]
+
+
+def bi_I(t, tmax=BI["tmax"], Imax=BI["Imax"]):
+    val = -Imax * t * (t - tmax) * 4 / tmax ** 2
+    return 0.0 if val < 0 else val
+
+
+def bi_dispersion(k, p):
+    return -1j * p["gam"] / 2 + p["w0"] * (1 + sum(np.abs(x) ** 2 for x in k) / (2 * p["kz"] ** 2)) - p["wp"]
+
+
+def bi_nonlinearity(u, p):
+    return p["g"] * np.abs(u[0]) ** 2
+
+
+def bi_pump(r, p, t):
+    return np.exp(-sum((x - p["L"] / 2) ** 2 for x in r) / p["width"] ** 2) * math.sqrt(bi_I(t))
+
+
+def bi_solve(gpe, dtype, fp64, dispersion=bi_dispersion, nonlinearity=bi_nonlinearity, pump=bi_pump):
+    u0 = (np.zeros(BI["N"], dtype),)
+    prob = gpe.GrossPitaevskiiProblem(u0, (BI["L"],), dispersion=dispersion, nonlinearity=nonlinearity, pump=pump,
+                                      param=BI)
+    return gpe.solve(prob, gpe.StrangSplitting(), (0.0, BI["tmax"]), dt=0.05, nsaves=512, fp64=fp64)
+
+
+@pytest.mark.parametrize("dtype,fp64", MODES, ids=IDS)
+def test_bistability_cycle(gpe, lib, dtype, fp64):
+    """test/bistability_cycle.jl:56-65: n_max (gamma^2/4 + (g n_max - delta)^2) follows the
+    pump intensity I(t) over the cycle; the reference asserts sum(error[140:400]) / 513
+    <= 3e-3 (Julia indices 140..400 are Python 139..399)."""
+    ts, (sol,) = bi_solve(gpe, dtype, fp64)
+    assert sol.shape == (BI["N"], 513) and len(ts) == 513
+    err = np.empty(len(ts))
+    for n in range(len(ts)):
+        nmax = float(np.max(np.abs(sol[:, n].astype(np.complex128)) ** 2))
+        pred = nmax * (BI["gam"] ** 2 / 4 + (BI["g"] * nmax - BI["d"]) ** 2)
+        err[n] = abs(pred - bi_I(ts[n]))
+    assert err[139:400].sum() / len(ts) <= 3e-3, err[139:400].sum() / len(ts)
+
+
+def test_bistability_closure_shape_variants(gpe, lib):
+    """test/bistability_cycle.jl:67-71: every combination of scalar, SVector and
+    SMatrix{1,1} forms of the dispersion, nonlinearity and pump gives the base solution
+    (sol2[1] ≈ sol[1]); native FP64, the full cycle."""
+    ts0, (base,) = bi_solve(gpe, np.complex128, "native")
+    disp = [bi_dispersion, lambda k, p: [bi_dispersion(k, p)], lambda k, p: [[bi_dispersion(k, p)]]]
+    nonl = [bi_nonlinearity, lambda u, p: [bi_nonlinearity(u, p)], lambda u, p: [[bi_nonlinearity(u, p)]]]
+    pump = [bi_pump, lambda r, p, t: [bi_pump(r, p, t)], lambda r, p, t: [[bi_pump(r, p, t)]]]
+    for d in disp:
+        for g in nonl:
+            for f in pump:
+                ts, (sol,) = bi_solve(gpe, np.complex128, "native", d, g, f)
+                assert np.array_equal(ts, ts0)
+                assert rel_l2(sol, base) <= ISAPPROX
+
+
+# ------------------------------------------------------------------ exciton polariton
+def test_exciton_polariton_steady_state_relations(gpe, lib):
+    """test/exciton_polariton_test.jl:15-53 in the three precisions (one solve each)."""
+    hb = 0.654
+    P = dict(hb=hb, Om=5.07 / 2 / hb, gx=0.0015 / hb, gc=0.07 / 0.6571 / hb, wx=1484.44 / hb, wc=1482.76 / hb,
+             m=hb ** 2 / (2 * 2e-1), A=2.0, w=100.0, g=1e-2 / hb, L=256.0)
+    P["wp"] = P["wc"]
+    P["dx"], P["dc"] = P["wp"] - P["wx"], P["wp"] - P["wc"]
+    N = 128
+
+    def dispersion(k, p):
+        Dcc = p["hb"] * sum(np.abs(x) ** 2 for x in k) / (2 * p["m"]) - p["dc"] - 1j * p["gc"]
+        return [[Dcc, p["Om"]], [p["Om"], -p["dx"] - 1j * p["gx"]]]
+
+    def nonlinearity(u, p):
+        return [0 * u[0], p["g"] * np.abs(u[1]) ** 2]
+
+    def pump(r, p, t):
+        return [p["A"] * np.exp(-sum((x - p["L"] / 2) ** 2 for x in r) / p["w"] ** 2), 0]
+
+    for (dtype, fp64), name in zip(MODES, IDS):
+        u0 = (np.zeros((N, N), dtype), np.zeros((N, N), dtype))
+        prob = gpe.GrossPitaevskiiProblem(u0, (P["L"], P["L"]), dispersion=dispersion, nonlinearity=nonlinearity,
+                                          pump=pump, param=P)
+        ts, sol = gpe.solve(prob, gpe.StrangSplitting(), (0.0, 100.0), dt=0.1, nsaves=256, fp64=fp64)
+        nx = abs(complex(sol[1][N // 2, N // 2, -1])) ** 2
+        nc = abs(complex(sol[0][N // 2, N // 2, -1])) ** 2
+        Om, dx, dc, gx, gc, g, A = P["Om"], P["dx"], P["dc"], P["gx"], P["gc"], P["g"], P["A"]
+        r1 = abs(abs(Om - (dx + 1j * gx / 2 - g * nx) * (dc + 1j * gc / 2) / Om) ** 2 * nx / abs(A) ** 2 - 1)
+        r2 = abs(abs(dx + 1j * gx / 2 - g * nx) ** 2 * nx / Om ** 2 / nc - 1)
+        assert r1 < 3e-2 and r2 < 3e-2, (name, r1, r2)
+
+
+# ------------------------------------------------------------------ windowed FT (TWA)
+def windowed_correlation(sol, rs, w1, w2):
+    """correlation() of test/windowed_ft.jl:27-44: sol is (N, trajectories)."""
+    s1 = sol * w1(rs)[:, None]
+    s2 = sol * w2(rs)[:, None]
+    f1 = np.fft.ifftshift(np.fft.fft(np.fft.fftshift(s1, 0), axis=0), 0)
+    f2 = np.fft.ifftshift(np.fft.fft(np.fft.fftshift(s2, 0), axis=0), 0)
+    # g1[i, j] = dot(ft2[j, :], ft1[i, :]) / length(sol), dot conjugating its first argument
+    return (f1 @ f2.conj().T) / sol.size
+
+
+@pytest.mark.parametrize("dtype,fp64", MODES, ids=IDS)
+def test_windowed_ft_commutator_philox(gpe, lib, dtype, fp64):
+    """test/windowed_ft.jl:45-99 with the noise drawn in-kernel by Philox4x32-10: 10^4
+    vacuum trajectories of the damped 1D field, one save at t = 200 (dt = 4), windowed-FT
+    correlations for x0 in -1:1 and w in 3:5 against the analytic commutator, rtol 7e-2."""
+    L, N, B = 20.0, 64, 10 ** 4
+    dL = L / N
+    hb = 0.6582
+    p = dict(gam=0.1 / hb, m=hb ** 2 / 2.5, d0=0.49 / hb, hb=hb, dL=dL)
+    u0 = (np.zeros((N, B), dtype),)
+    prob = gpe.GrossPitaevskiiProblem(
+        u0, (L,), param=p,
+        dispersion=lambda k, q: -1j * q["gam"] / 2 + q["hb"] * sum(np.abs(x) ** 2 for x in k) / (2 * q["m"]) - q["d0"],
+        position_noise_func=lambda u, r, q: math.sqrt(q["gam"] / 2 / q["dL"]))
+    ts, (res,) = gpe.solve(prob, gpe.StrangSplitting(), (0.0, 200.0), dt=4.0, nsaves=1, save_start=False, rng=1234,
+                           fp64=fp64)
+    assert res.shape == (N, B, 1) and len(ts) == 1 and ts[0] == 200.0
+    sol = res[:, :, 0].astype(np.complex128)
+    rs = -L / 2 + np.arange(N) * (L / N)
+    ks = -math.pi / L + np.arange(N) * (2 * math.pi / L)
+    worst = 0.0
+    for x0 in (-1, 0, 1):
+        for w in (3, 4, 5):
+            win1 = lambda x, x0=x0, w=w: np.exp(-((x - x0) ** 2) / w ** 2)
+            win2 = lambda x, x0=x0, w=w: np.exp(-((x + x0) ** 2) / w ** 2)
+            corr = windowed_correlation(sol, rs, win1, win2)
+            ph = np.exp(1j * (ks[:, None, None] - ks[None, :, None]) * rs[None, None, :])
+            an = (ph * (win1(rs) * np.conj(win2(rs)))[None, None, :]).sum(-1) / (rs[-1] - rs[0]) / 2
+            e = np.linalg.norm(corr - an) / max(np.linalg.norm(corr), np.linalg.norm(an))
+            worst = max(worst, e)
+    assert worst <= 7e-2, worst

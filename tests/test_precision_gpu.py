@@ -1,9 +1,9 @@
 """Long-run accuracy of the FP64 modes on 2D Kerr over 1000 steps against the FP64
-oracle.  The defocusing packet (g = +1) stays smooth: both modes stay far inside the
-1e-10 parity bar.  The self-focusing packet (g = -2, norm just above the collapse
-threshold) amplifies every difference in rounding, the oracle's own FFT order included:
-there the double-word mode is held to its unit roundoff against native FP64 (2^-48
-against 2^-53, a factor 32), i.e. within 64x of native FP64's distance to the oracle."""
+oracle, at 256^2 (the full 2048^2 configuration is tests/test_c3_precision_gpu.py).  The
+defocusing packet (g = +1) stays smooth and both modes stay far inside the 1e-10 parity
+bar.  The self-focusing packet (g = -2, norm just above the collapse threshold) amplifies
+every difference in rounding, the oracle's own FFT order included; both modes must still
+end within the 1e-10 bar."""
 import numpy as np
 import pytest
 
@@ -39,5 +39,4 @@ def test_smooth_kerr_1000_steps(gpe, oracle, lib):
 
 def test_collapsing_kerr_1000_steps(gpe, oracle, lib):
     err = run(gpe, oracle, -2.0)
-    assert err["native"] <= 1e-9, err
-    assert err["dw"] <= 64 * err["native"], err
+    assert err["native"] <= 1e-10 and err["dw"] <= 1e-10, err

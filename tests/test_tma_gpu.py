@@ -76,6 +76,9 @@ def test_bounded_wait_times_out_and_context_survives(gpe, lib):
     L = gpe._lib
     assert lib.gpe_selftest_wait(0, 1, 10 ** 9) == L.GPE_OK
     assert lib.gpe_selftest_wait(0, 0, 2 * 10 ** 6) == L.GPE_ERR_TIMEOUT
+    # a limit above the library's own 1 s bound is refused before anything is launched
+    assert lib.gpe_selftest_wait(0, 0, 10 ** 9 + 1) == L.GPE_ERR_INVALID
+    assert lib.gpe_selftest_wait(0, 0, 2 ** 62) == L.GPE_ERR_INVALID
     # the context still runs a solve afterwards
     a = run(gpe, (64, 64), 2, 1, np.complex128, "dw", tma=True, steps=2)
     assert all(np.isfinite(x).all() for x in a)
