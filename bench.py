@@ -683,7 +683,51 @@ def run_twa(pkg, steps: int, tune: bool):
             "dtype": "f32 (tables built in FP64)", "steps_per_graph": chunk, "autotune": choices or None,
             "plain_per_trajectory": {"value": plain_value, "unit": "traj-steps/s",
                                      "sample": "3 trajectories x 100 steps per grid, one handle each, two-pass path"},
-            "speedup_vs_plain_per_trajectory": value / plain_value}
+            "speedup_vs_plain_per_trajectory": value / plain_value,
+            "statistics_vs_fp64_cpu_ensemble": twa_c2_statistics(pkg, steps)}
+
+
+def twa_c2_statistics(pkg, steps: int = 2000, N: int = 64, ntraj: int = 342):
+    """The ensemble statistics of the batched truncated-Wigner configuration, checked
+    against an FP64 CPU ensemble: the 64^2 group (342 trajectories, FP32 fields, Philox
+    noise) after `steps` steps on the GPU, and the same trajectories advanced in FP64 by
+    the C oracle on the host cores with the same initial states and the same Philox draws
+    (FP32 draws evaluated in FP64).  Reported: the per-site mean and variance of |u|^2 over
+    the trajectories, their rel L2 difference between the two ensembles, and the largest
+    per-trajectory rel L2 difference."""
+    import math as _m
+    T = sys.modules.get("gpe_gb300.twa") or __import__("gpe_gb300.twa", fromlist=["Ensemble"])
+    from oracle import gpe_oracle as O
+    from oracle import gpe_oracle_c as OC
+    prm = T.DampedDrivenParams()
+    seed = N
+    it = T.make_group(N, ntraj, prm, steps, seed=seed)
+    it.step(steps)
+    g = it.get_fields()[0].astype(np.complex128)  # (x, y, b)
+    it.close()
+    u0 = T.wigner_initial(N, 0, ntraj, prm, seed, np.complex64)
+    dV = (prm.L / N) ** 2
+    prob = O.OracleProblem(u0=(np.ascontiguousarray(np.transpose(u0, (2, 1, 0))).astype(np.complex128),),
+                           lengths=(prm.L, prm.L),
+                           dispersion=lambda k, p: (k[0] ** 2 + k[1] ** 2) / 2 - 0.5j * prm.gamma,
+                           nonlin_g=np.array([[prm.g]]), pump_profile=np.ones((1, N, N), np.complex128),
+                           pump_amp=lambda t: np.array([prm.F]), eta=np.array([_m.sqrt(prm.gamma / (2 * dV))]))
+    t0 = time.perf_counter()
+    cit = OC.CIterator(prob, (0.0, steps * prm.dt), prm.dt, 1, philox_seed=seed + 1, draw32=True)
+    cit.step(steps)
+    cpu_s = time.perf_counter() - t0
+    c = np.transpose(cit.u[0], (2, 1, 0))  # (x, y, b)
+    ng, nc = np.abs(g) ** 2, np.abs(c) ** 2
+    mg, mc, vg, vc = ng.mean(-1), nc.mean(-1), ng.var(-1), nc.var(-1)
+    rel = lambda a, b: float(np.linalg.norm(a - b) / np.linalg.norm(b))
+    per_traj = max(rel(g[..., b], c[..., b]) for b in range(ntraj))
+    return {"group": f"{N}x{N}, {ntraj} trajectories, {steps} steps", "gpu": "FP32 fields, Philox FP32 draws",
+            "cpu": f"FP64 C oracle on {os.cpu_count()} host threads, the same initial states and Philox draws "
+                   f"({cpu_s:.1f} s)",
+            "mean_density_gpu": float(mg.mean()), "mean_density_cpu": float(mc.mean()),
+            "density_variance_gpu": float(vg.mean()), "density_variance_cpu": float(vc.mean()),
+            "rel_l2_mean_density_field": rel(mg, mc), "rel_l2_variance_field": rel(vg, vc),
+            "max_rel_l2_per_trajectory": per_traj}
 
 
 def run_precision_sweep(args):

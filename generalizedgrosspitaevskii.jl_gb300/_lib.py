@@ -108,6 +108,7 @@ SIGNATURES = {
     "gpe_run_async": (c_int, [H, c_int64]),
     "gpe_wait": (c_int, [H]),
     "gpe_selftest_wait": (c_int, [c_int, c_int, c_int64]),
+    "gpe_set_noise_offset": (c_int, [c_void_p, c_int64]),
     "gpe_ensemble_create": (c_int, [c_void_p, c_int, POINTER(c_void_p)]),
     "gpe_ensemble_run": (c_int, [c_void_p, c_int64, c_int64]),
     "gpe_ensemble_destroy": (c_int, [c_void_p]),

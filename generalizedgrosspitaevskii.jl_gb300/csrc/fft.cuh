@@ -21,7 +21,8 @@
 //
 // Twiddles come from a per-length FP64-built table w_N^k = exp(-2 pi i k / N);
 // the inverse uses its conjugate.  The in-register radix-R DFTs use the constants
-// cos(2 pi k / 16) (FP32 passes: as hi/lo pairs, see twc).
+// cos(2 pi k / 16).  FP32 passes hold both as FP32 hi/lo pairs and apply them with FMA
+// corrections (cmul_hl), so no rounded constant biases every transform the same way.
 #pragma once
 #include <cuda_runtime.h>
 #include <stdint.h>
@@ -66,6 +67,33 @@ template <typename C> __device__ __forceinline__ C cmulc(C a, C b) {
   return r;
 }
 template <typename C, typename R> __device__ __forceinline__ C cscale(C a, R s) { C r; r.x = a.x * s; r.y = a.y * s; return r; }
+
+// FP32 value times an FP64-accurate constant held as hi/lo float pairs (w = (xh + xl) +
+// i (yh + yl)), with FMA corrections: the FP32 rounding of the product with the exact
+// constant (within a few units of the last place, unbiased), where a plain FP32 constant
+// would carry a fixed rounding error into every product with it.
+__device__ __forceinline__ float2 cmul_hl(float2 v, dwc w) {
+  float2 r;
+  r.x = __fmaf_rn(v.x, w.xh, __fmaf_rn(-v.y, w.yh, __fmaf_rn(v.x, w.xl, -(v.y * w.yl))));
+  r.y = __fmaf_rn(v.x, w.yh, __fmaf_rn(v.y, w.xh, __fmaf_rn(v.x, w.yl, v.y * w.xl)));
+  return r;
+}
+// v * conj(w)
+__device__ __forceinline__ float2 cmulc_hl(float2 v, dwc w) {
+  float2 r;
+  r.x = __fmaf_rn(v.x, w.xh, __fmaf_rn(v.y, w.yh, __fmaf_rn(v.x, w.xl, v.y * w.yl)));
+  r.y = __fmaf_rn(v.y, w.xh, __fmaf_rn(-v.x, w.yh, __fmaf_rn(v.y, w.xl, -(v.x * w.yl))));
+  return r;
+}
+
+// Twiddle tables: the complex type of the pass for FP64 and double-word passes, hi/lo
+// float pairs (16 bytes an entry) for FP32 passes.
+template <typename C> struct TwT { using T = C; };
+template <> struct TwT<float2> { using T = dwc; };
+template <typename C> __device__ __forceinline__ C twmul(C v, C w) { return cmul(v, w); }
+template <typename C> __device__ __forceinline__ C twmulc(C v, C w) { return cmulc(v, w); }
+__device__ __forceinline__ float2 twmul(float2 v, dwc w) { return cmul_hl(v, w); }
+__device__ __forceinline__ float2 twmulc(float2 v, dwc w) { return cmulc_hl(v, w); }
 template <typename C> __device__ __forceinline__ C cmake(double x, double y) { C r; r.x = x; r.y = y; return r; }
 
 // cos(2 pi k / 16), k in [0, 16): exact constants of the regular 16-gon.
@@ -231,7 +259,7 @@ struct ColLayout {
 
 // One Stockham stage.  x: this thread's E points; t: thread index in the line.
 template <typename C, int N, int E, int R, int NS, int DIR, bool LAST, class Lay>
-__device__ __forceinline__ void fft_stage(C (&x)[E], int t, const Lay& lay, const C* __restrict__ tw) {
+__device__ __forceinline__ void fft_stage(C (&x)[E], int t, const Lay& lay, const typename TwT<C>::T* __restrict__ tw) {
   constexpr int T = N / E, Q = E / R;
 #pragma unroll
   for (int q = 0; q < Q; ++q) {
@@ -244,8 +272,8 @@ __device__ __forceinline__ void fft_stage(C (&x)[E], int t, const Lay& lay, cons
       constexpr int TS = N / (NS * R);
 #pragma unroll
       for (int r = 1; r < R; ++r) {
-        const C w = ldgc(tw + k * r * TS);
-        v[r] = (DIR < 0) ? cmul(v[r], w) : cmulc(v[r], w);
+        const auto w = ldgc(tw + k * r * TS);
+        v[r] = (DIR < 0) ? twmul(v[r], w) : twmulc(v[r], w);
       }
     }
     dft_regs<R, DIR>(v);
@@ -261,7 +289,7 @@ __device__ __forceinline__ void fft_stage(C (&x)[E], int t, const Lay& lay, cons
 }
 
 template <typename C, int N, int E, int DIR, int NS, class Lay>
-__device__ __forceinline__ void fft_stages(C (&x)[E], int t, const Lay& lay, const C* __restrict__ tw) {
+__device__ __forceinline__ void fft_stages(C (&x)[E], int t, const Lay& lay, const typename TwT<C>::T* __restrict__ tw) {
   constexpr int REM = N / NS;
   constexpr int R = REM >= E ? E : REM;
   constexpr bool LAST = (NS * R == N);
@@ -282,7 +310,7 @@ __device__ __forceinline__ void fft_stages(C (&x)[E], int t, const Lay& lay, con
 // bfinish to the outputs (a no-op for every precision now that double-word butterflies
 // renormalise as they go).
 template <typename C, int N, int E, int DIR, class Lay>
-__device__ __forceinline__ void fft_line(C (&x)[E], int t, const Lay& lay, const C* __restrict__ tw,
+__device__ __forceinline__ void fft_line(C (&x)[E], int t, const Lay& lay, const typename TwT<C>::T* __restrict__ tw,
                                          bool renorm = true) {
   fft_stages<C, N, E, DIR, 1>(x, t, lay, tw);
   if (renorm) {
@@ -296,7 +324,7 @@ __device__ __forceinline__ void fft_line(C (&x)[E], int t, const Lay& lay, const
 // Component m exchanges through lay.base + m * cstride.
 template <typename C, int N, int E, int R, int NS, int DIR, bool LAST, int M, class Lay>
 __device__ __forceinline__ void fft_stage_joint(C (&x)[M][E], int t, const Lay& lay, int cstride,
-                                                const C* __restrict__ tw) {
+                                                const typename TwT<C>::T* __restrict__ tw) {
   constexpr int T = N / E, Q = E / R;
 #pragma unroll
   for (int q = 0; q < Q; ++q) {
@@ -311,9 +339,9 @@ __device__ __forceinline__ void fft_stage_joint(C (&x)[M][E], int t, const Lay& 
       constexpr int TS = N / (NS * R);
 #pragma unroll
       for (int r = 1; r < R; ++r) {
-        const C w = ldgc(tw + k * r * TS);
+        const auto w = ldgc(tw + k * r * TS);
 #pragma unroll
-        for (int m = 0; m < M; ++m) v[m][r] = (DIR < 0) ? cmul(v[m][r], w) : cmulc(v[m][r], w);
+        for (int m = 0; m < M; ++m) v[m][r] = (DIR < 0) ? twmul(v[m][r], w) : twmulc(v[m][r], w);
       }
     }
 #pragma unroll
@@ -337,7 +365,7 @@ __device__ __forceinline__ void fft_stage_joint(C (&x)[M][E], int t, const Lay& 
 
 template <typename C, int N, int E, int DIR, int NS, int M, class Lay>
 __device__ __forceinline__ void fft_stages_joint(C (&x)[M][E], int t, const Lay& lay, int cstride,
-                                                 const C* __restrict__ tw) {
+                                                 const typename TwT<C>::T* __restrict__ tw) {
   constexpr int REM = N / NS;
   constexpr int R = REM >= E ? E : REM;
   constexpr bool LAST = (NS * R == N);
@@ -358,7 +386,7 @@ __device__ __forceinline__ void fft_stages_joint(C (&x)[M][E], int t, const Lay&
 
 template <typename C, int N, int E, int DIR, int M, class Lay>
 __device__ __forceinline__ void fft_line_joint(C (&x)[M][E], int t, const Lay& lay, int cstride,
-                                               const C* __restrict__ tw) {
+                                               const typename TwT<C>::T* __restrict__ tw) {
   fft_stages_joint<C, N, E, DIR, 1, M>(x, t, lay, cstride, tw);
 #pragma unroll
   for (int m = 0; m < M; ++m)

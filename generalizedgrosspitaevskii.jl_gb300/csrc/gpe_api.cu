@@ -113,6 +113,7 @@ struct gpe_handle {
   void* etaprof[2] = {nullptr, nullptr};
   int noise = GPE_NOISE_OFF;
   uint64_t seed = 0;
+  int64_t traj0 = 0;  // global index of the first trajectory (gpe_set_noise_offset)
   double eta[2][2] = {{0, 0}, {0, 0}};
   double g[2][2][2] = {};
   double c[2][2] = {};
@@ -426,7 +427,7 @@ int gpe_create(const gpe_desc* desc, gpe_handle** out) {
     return bail(GPE_ERR_NOMEM);
   }
   *h->hstat = 0;
-  // twiddles w_N^k = exp(-2 pi i k / N) per axis, built in FP64
+  // twiddles w_N^k = exp(-2 pi i k / N) per axis, built in FP64 and kept at FP64 accuracy
   for (int a = 0; a < h->ndim; ++a) {
     const int64_t N = h->n[a];
     std::vector<cd> w((size_t)N);
@@ -434,7 +435,7 @@ int gpe_create(const gpe_desc* desc, gpe_handle** out) {
       const double th = -2.0 * M_PI * (double)k / (double)N;
       w[(size_t)k] = cd(std::cos(th), std::sin(th));
     }
-    int rc = upload_complex(h, &h->tw[a], w.data(), (size_t)N);
+    int rc = upload_table(h, &h->tw[a], w.data(), (size_t)N);  // FP32 passes: hi/lo pairs
     if (rc) { g_create_error = h->err; return bail(rc); }
   }
   cudaDeviceSynchronize();
@@ -897,6 +898,7 @@ static PassArgs base_args(gpe_handle* h) {
   a.noise = h->noise;
   a.seed_lo = (uint32_t)h->seed;
   a.seed_hi = (uint32_t)(h->seed >> 32);
+  a.traj0 = h->traj0;
   // -i sqrt(dt/2) eta  (src/kernels.jl:42 with delta = dt/2)
   const double sq = std::sqrt(0.5 * h->d.dt);
   for (int m = 0; m < h->M; ++m) {
@@ -1585,6 +1587,16 @@ int gpe_run_replay(gpe_handle* h, int64_t nsteps, int64_t save_every, const void
   if (!h) return GPE_ERR_INVALID;
   if (!xi_host && nsteps > 0) return fail(h, GPE_ERR_INVALID, "null xi");
   return run_common(h, nsteps, save_every, out_host, false, ts_out, xi_host);
+}
+
+int gpe_set_noise_offset(gpe_handle* h, int64_t traj0) {
+  if (!h) return GPE_ERR_INVALID;
+  // the counter holds the global trajectory index in one 32-bit word
+  if (traj0 < 0 || traj0 + h->B > (int64_t(1) << 32))
+    return fail(h, GPE_ERR_INVALID, "trajectory offset %lld: offset + batch must lie in [0, 2^32]", (long long)traj0);
+  if (traj0 != h->traj0) ++h->gen;  // a kernel argument: captured graphs are recaptured
+  h->traj0 = traj0;
+  return GPE_OK;
 }
 
 int gpe_get_state(gpe_handle* h, gpe_state* st) {

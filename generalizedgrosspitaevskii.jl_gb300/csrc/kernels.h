@@ -53,6 +53,7 @@ struct PassArgs {
   // noise: -i sqrt(dt/2) eta_m (host-formed) [* eta profile] * xi
   int32_t noise;
   uint32_t seed_lo, seed_hi;
+  int64_t traj0;  // global index of this handle's first trajectory (Philox counter word 1)
   double nfac[2][2];
   float nfacf[2][2], nfacl[2][2];
   const void* etaprof[2];

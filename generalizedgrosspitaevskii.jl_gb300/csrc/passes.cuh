@@ -109,16 +109,22 @@ struct LineCfg {
 // ------------------------------------------------------------------ scalar helpers
 template <typename Real> __device__ __forceinline__ void sc(Real x, Real* s, Real* c);
 // FP64 sin/cos of the nonlinear phase.  FP64 runs at 1/64 of the FP32 rate on GB300, so
-// small angles (the usual case: |dt/2 * G| << 1) use the Taylor series of sin and cos
-// to x^13 / x^12 (truncation error below x^14/14! < 3e-24 for |x| <= 1/8), about a
-// third of the cost of the general routine, which handles the rest.
+// small angles (the usual case: |dt/2 * G| << 1) use Taylor series of sin and cos with as
+// many terms as FP64 needs on their interval: for |x| < 2^-6 through x^7 / x^6 (the first
+// dropped terms, x^9/9! and x^8/8!, are below 1e-19 of the result), for |x| < 1/8 through
+// x^9 / x^10 (below 3e-17 relative and 3e-20), about a third and a half of the cost of
+// the general routine, which handles the rest.  The interval is picked from the high word
+// of x on the integer pipe, leaving the FP64 pipe to the arithmetic.
 template <> __device__ __forceinline__ void sc<double>(double x, double* s, double* c) {
-  if (fabs(x) <= 0.125) {
+  const int hx = __double2hiint(x) & 0x7fffffff;  // |x| < 2^-6 iff hx < 0x3f900000, < 1/8 iff < 0x3fc00000
+  if (hx < 0x3f900000) {
     const double x2 = x * x;
-    *c = 1.0 + x2 * (-1.0 / 2 + x2 * (1.0 / 24 + x2 * (-1.0 / 720 + x2 * (1.0 / 40320 + x2 * (-1.0 / 3628800 +
-         x2 * (1.0 / 479001600))))));
-    *s = x * (1.0 + x2 * (-1.0 / 6 + x2 * (1.0 / 120 + x2 * (-1.0 / 5040 + x2 * (1.0 / 362880 + x2 * (-1.0 / 39916800 +
-         x2 * (1.0 / 6227020800.0)))))));
+    *c = 1.0 + x2 * (-1.0 / 2 + x2 * (1.0 / 24 + x2 * (-1.0 / 720)));
+    *s = x * (1.0 + x2 * (-1.0 / 6 + x2 * (1.0 / 120 + x2 * (-1.0 / 5040))));
+  } else if (hx < 0x3fc00000) {
+    const double x2 = x * x;
+    *c = 1.0 + x2 * (-1.0 / 2 + x2 * (1.0 / 24 + x2 * (-1.0 / 720 + x2 * (1.0 / 40320 + x2 * (-1.0 / 3628800)))));
+    *s = x * (1.0 + x2 * (-1.0 / 6 + x2 * (1.0 / 120 + x2 * (-1.0 / 5040 + x2 * (1.0 / 362880)))));
   } else {
     sincos(x, s, c);
   }
@@ -132,6 +138,21 @@ template <> __device__ __forceinline__ void sc<float>(float x, float* s, float* 
     *s = x * (1.0f + x2 * (-1.0f / 6 + x2 * (1.0f / 120 + x2 * (-1.0f / 5040))));
   } else {
     sincosf(x, s, c);
+  }
+}
+// FP32 sin x and cos x - 1.  The nonlinear phase factor is applied to FP32 fields as
+// u + (E - 1) u with E - 1 = (cos - 1) - i sin formed without the leading 1: rounded near
+// 1, cos carries an error of up to 3e-8 that depends smoothly on x, so it does not average
+// out over a smooth field, and |E|^2 - 1 of that size would bias the norm every half step.
+__device__ __forceinline__ void sc_m1(float x, float* s, float* cm1) {
+  if (fabsf(x) <= 0.125f) {
+    const float x2 = x * x;
+    *cm1 = x2 * (-0.5f + x2 * (1.0f / 24 + x2 * (-1.0f / 720 + x2 * (1.0f / 40320))));
+    *s = x * (1.0f + x2 * (-1.0f / 6 + x2 * (1.0f / 120 + x2 * (-1.0f / 5040))));
+  } else {
+    float c;
+    sincosf(x, s, &c);
+    *cm1 = c - 1.0f;
   }
 }
 __device__ __forceinline__ double rexp(double x) { return exp(x); }
@@ -255,12 +276,7 @@ template <typename Real> struct TabT { using T = dwc; };
 template <> struct TabT<double> { using T = double2; };
 __device__ __forceinline__ double2 tmul(const double2& t, const double2& v) { return cmul(t, v); }
 __device__ __forceinline__ dwc tmul(const dwc& t, const dwc& v) { return cmul(t, v); }
-__device__ __forceinline__ float2 tmul(const dwc& t, const float2& v) {
-  float2 r;
-  r.x = __fmaf_rn(v.x, t.xh, __fmaf_rn(-v.y, t.yh, __fmaf_rn(v.x, t.xl, -(v.y * t.yl))));
-  r.y = __fmaf_rn(v.x, t.yh, __fmaf_rn(v.y, t.xh, __fmaf_rn(v.x, t.yl, v.y * t.xl)));
-  return r;
-}
+__device__ __forceinline__ float2 tmul(const dwc& t, const float2& v) { return cmul_hl(v, t); }
 
 // whether half_step applies component j's two pump terms as one (no E multiplies it)
 __device__ __forceinline__ bool pump_merged(const PassArgs& a, int j) {
@@ -303,10 +319,10 @@ __device__ __forceinline__ void draw_xi(const PassArgs& a, int64_t p, int64_t b,
     if constexpr (M == 1) {
       const int64_t hx = a.n0 >> 1;
       const bool up = (p & (a.n0 - 1)) >= hx;
-      const uint4 r = Philox4x32::gen(noise_counter(up ? p - hx : p, b, h), a.seed_lo, a.seed_hi);
+      const uint4 r = Philox4x32::gen(noise_counter(up ? p - hx : p, b + a.traj0, h), a.seed_lo, a.seed_hi);
       xi[0] = Xi<Real>::get(up ? r.z : r.x, up ? r.w : r.y);
     } else {
-      const uint4 r = Philox4x32::gen(noise_counter(p, b, h), a.seed_lo, a.seed_hi);
+      const uint4 r = Philox4x32::gen(noise_counter(p, b + a.traj0, h), a.seed_lo, a.seed_hi);
       xi[0] = Xi<Real>::get(r.x, r.y);
       xi[M - 1] = Xi<Real>::get(r.z, r.w);
     }
@@ -472,11 +488,25 @@ __device__ __forceinline__ void half_step(typename CT<Real>::T (&u)[M], const Pa
           gr += K::g(a, j, l, 0) * dens[l];
           gi += K::g(a, j, l, 1) * dens[l];
         }
-        Real s, c;
-        sc<Real>(dth * gr, &s, &c);
-        const Real mag = a.nl_imag[j] ? rexp(dth * gi) : (Real)1;
-        E[j].x = mag * c;
-        E[j].y = -mag * s;
+        if constexpr (std::is_same<Real, float>::value) {
+          // E - 1 (see sc_m1): mag cos - 1 = (mag - 1) + mag (cos - 1)
+          float s, cm1;
+          sc_m1(dth * gr, &s, &cm1);
+          if (a.nl_imag[j]) {
+            const float em1 = expm1f(dth * gi), mag = 1.0f + em1;
+            E[j].x = __fmaf_rn(mag, cm1, em1);
+            E[j].y = -mag * s;
+          } else {
+            E[j].x = cm1;
+            E[j].y = -s;
+          }
+        } else {
+          Real s, c;
+          sc<Real>(dth * gr, &s, &c);
+          const Real mag = a.nl_imag[j] ? rexp(dth * gi) : (Real)1;
+          E[j].x = mag * c;
+          E[j].y = -mag * s;
+        }
       }
     }
   }
@@ -525,9 +555,15 @@ __device__ __forceinline__ void half_step(typename CT<Real>::T (&u)[M], const Pa
   } else {
 #pragma unroll
     for (int j = 0; j < M; ++j) {
-      if (hasE[j]) u[j] = cmul(E[j], u[j]);
       if constexpr (SEPV) {
+        if (hasE[j]) {  // u + (E - 1) u
+          const C v = u[j];
+          u[j].x = __fmaf_rn(E[j].x, v.x, __fmaf_rn(-E[j].y, v.y, v.x));
+          u[j].y = __fmaf_rn(E[j].x, v.y, __fmaf_rn(E[j].y, v.x, v.y));
+        }
         if (hasV) u[j] = tmul(vt[j], u[j]);
+      } else {
+        if (hasE[j]) u[j] = cmul(E[j], u[j]);
       }
     }
   }
@@ -619,7 +655,7 @@ __device__ __forceinline__ void conj_all(C (&x)[E]) {
 // both directions: component 1 is swapped into the slot of component 0 and back.
 template <typename C, int N, int E, int M, class Lay, bool JOINT = false>
 __device__ __forceinline__ void fft_components(C (&x)[M][E], bool inverse, int t, const Lay& lay,
-                                               const C* __restrict__ tw, int cstride = 0, bool renorm = true) {
+                                               const typename TwT<C>::T* __restrict__ tw, int cstride = 0, bool renorm = true) {
   if constexpr (JOINT) {
     // all components in one pass (FP32: the twiddle loads and barriers are shared)
     if (inverse) {
@@ -696,7 +732,7 @@ __device__ __forceinline__ void half_points(typename CT<Real>::T (&x)[M][E], con
       C xa[1], xb[1];
       const bool pre = a.noise == NOISE_PHILOX;
       if (pre) {
-        const uint4 r = Philox4x32::gen(noise_counter(pa, b, h), a.seed_lo, a.seed_hi);
+        const uint4 r = Philox4x32::gen(noise_counter(pa, b + a.traj0, h), a.seed_lo, a.seed_hi);
         xa[0] = Xi<Real>::get(r.x, r.y);
         xb[0] = Xi<Real>::get(r.z, r.w);
       }
@@ -747,7 +783,7 @@ row_kernel(const PassArgs a, const int64_t nlines, const int lb) {
   const bool active = line < nlines;
   if (!active) line = nlines - 1;  // idle lines of the last block compute a copy, store nothing
   const RowLayout<C> lay{sm + l * N};
-  const C* tw = (const C*)a.tw;
+  const auto* tw = (const typename TwT<C>::T*)a.tw;
   const int64_t lpb = a.P / N;
   const int64_t b = line / lpb;
   const int64_t p0 = (line - b * lpb) * N + t;
@@ -801,7 +837,7 @@ __device__ __forceinline__ void col_tile_work(typename CT<Real>::T (&x)[M][LineC
   using Cfg = LineCfg<Real, M, LOGN, V>;
   using C = typename CT<Real>::T;
   constexpr int N = Cfg::N, E = Cfg::E, CC = Cfg::CC;
-  const C* tw = (const C*)a.tw;
+  const auto* tw = (const typename TwT<C>::T*)a.tw;
 #pragma unroll 1
   for (int ph = 0; ph < 3; ++ph) {
     if (ph != 1) {
@@ -961,7 +997,7 @@ line1d_kernel(const PassArgs a, const int64_t nlines) {
   const bool active = line < nlines;
   if (!active) line = nlines - 1;
   const RowLayout<C> lay{sm + l * N};
-  const C* tw = (const C*)a.tw;
+  const auto* tw = (const typename TwT<C>::T*)a.tw;
   const int64_t b = line;
   const int64_t g0 = b * a.P + t;
   C x[M][E];
@@ -1051,8 +1087,8 @@ plane_kernel(const PassArgs a) {
   C* f = reinterpret_cast<C*>(smraw);  // f[m * P + p]
   const int64_t b = blockIdx.x;
   const int tid = threadIdx.x;
-  const C* twx = (const C*)a.tw;
-  const C* twy = (const C*)a.tw2;
+  const auto* twx = (const typename TwT<C>::T*)a.tw;
+  const auto* twy = (const typename TwT<C>::T*)a.tw2;
   for (int m = 0; m < M; ++m)
     for (int p = tid; p < P; p += NT) f[m * P + p] = ((const C*)a.u[m])[b * P + p];
   __syncthreads();

@@ -41,7 +41,9 @@ struct Philox4x32 {
   }
 };
 
-// counter for (point p, trajectory b, half step h)
+// counter for (point p, global trajectory index b, half step h): a handle holding
+// trajectories b0 .. b0 + B - 1 of an ensemble (gpe_set_noise_offset) draws exactly their
+// part of the whole ensemble's noise
 __device__ __forceinline__ uint4 noise_counter(int64_t p, int64_t b, int64_t h) {
   return make_uint4((uint32_t)p, (uint32_t)b, (uint32_t)h, (uint32_t)((uint64_t)h >> 32));
 }

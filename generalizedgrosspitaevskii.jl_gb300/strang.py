@@ -211,6 +211,11 @@ class StrangSplittingIterator:
         """Advance nsteps full Strang steps (step!, src/strang_splitting.jl:86-90)."""
         self._run(int(nsteps), 0, None, None)
 
+    def set_noise_offset(self, traj0: int):
+        """Draw the Philox noise of trajectories traj0 .. traj0 + batch - 1 of a larger
+        ensemble with the same seed (gpe_set_noise_offset)."""
+        L.check(self.lib, self.h, self.lib.gpe_set_noise_offset(self.h, int(traj0)))
+
     def state(self) -> L.GpeState:
         st = L.GpeState()
         L.check(self.lib, self.h, self.lib.gpe_get_state(self.h, ctypes.byref(st)))

@@ -36,13 +36,25 @@ class DampedDrivenParams:
     dt: float = 0.02
 
 
-def wigner_problem(N: int, ntraj: int, prm: DampedDrivenParams, seed: int, dtype=np.complex64):
-    """One group: ntraj trajectories on an N x N grid starting from the coherent state
-    1 plus Wigner vacuum noise xi / sqrt(2 dV) (examples/truncated_wigner.jl:89)."""
+def wigner_initial(N: int, traj0: int, ntraj: int, prm: DampedDrivenParams, seed: int, dtype=np.complex64):
+    """Trajectories traj0 .. traj0 + ntraj - 1 of an ensemble on an N x N grid, each starting
+    from the coherent state 1 plus Wigner vacuum noise xi / sqrt(2 dV)
+    (examples/truncated_wigner.jl:89).  Trajectory b draws its xi from its own generator
+    (seed, b), so any slice of the ensemble is the same whichever process builds it."""
     dV = (prm.L / N) ** 2
-    rng = np.random.default_rng(seed)
-    xi = (rng.standard_normal((N, N, ntraj)) + 1j * rng.standard_normal((N, N, ntraj))) * math.sqrt(0.5)
-    u0 = (1.0 + xi / math.sqrt(2 * dV)).astype(dtype)
+    u0 = np.empty((N, N, ntraj), dtype, order="F")
+    for j in range(ntraj):
+        rng = np.random.default_rng([seed, traj0 + j])
+        xi = (rng.standard_normal((N, N)) + 1j * rng.standard_normal((N, N))) * math.sqrt(0.5)
+        u0[:, :, j] = 1.0 + xi / math.sqrt(2 * dV)
+    return u0
+
+
+def wigner_problem(N: int, ntraj: int, prm: DampedDrivenParams, seed: int, dtype=np.complex64, traj0: int = 0):
+    """One group: trajectories traj0 .. traj0 + ntraj - 1 of the damped-driven ensemble on
+    an N x N grid (wigner_initial)."""
+    dV = (prm.L / N) ** 2
+    u0 = wigner_initial(N, traj0, ntraj, prm, seed, dtype)
     eta = math.sqrt(prm.gamma / (2 * dV))
     return GrossPitaevskiiProblem(
         (np.asfortranarray(u0),), (prm.L, prm.L),
@@ -90,10 +102,43 @@ class Ensemble:
 
 def make_group(N: int, ntraj: int, prm: DampedDrivenParams, nsteps: int, seed: int, dtype=np.complex64,
                resident: bool = True, noise_seed: Optional[int] = None, variant: int = 0,
-               tma: Optional[bool] = None) -> StrangSplittingIterator:
-    prob = wigner_problem(N, ntraj, prm, seed, dtype)
-    return StrangSplittingIterator(prob, (0.0, nsteps * prm.dt), dt=prm.dt, nsaves=1, rng=seed + 1 if noise_seed is None else noise_seed,
-                                   resident=resident, variant=variant, tma=tma)
+               tma: Optional[bool] = None, traj0: int = 0, device: int = -1) -> StrangSplittingIterator:
+    """A handle advancing trajectories traj0 .. traj0 + ntraj - 1 of the ensemble (initial
+    state and Philox noise both indexed by the global trajectory number)."""
+    prob = wigner_problem(N, ntraj, prm, seed, dtype, traj0)
+    it = StrangSplittingIterator(prob, (0.0, nsteps * prm.dt), dt=prm.dt, nsaves=1,
+                                 rng=seed + 1 if noise_seed is None else noise_seed,
+                                 resident=resident, variant=variant, tma=tma, device=device)
+    if traj0:
+        it.set_noise_offset(traj0)
+    return it
+
+
+def shard_range(ntraj: int, rank: int, world: int):
+    """Contiguous slice of an ensemble of ntraj trajectories owned by rank: (first, count),
+    the first ntraj % world ranks taking one trajectory more."""
+    if not 0 <= rank < world:
+        raise ValueError("rank must lie in [0, world)")
+    base, extra = divmod(int(ntraj), int(world))
+    return rank * base + min(rank, extra), base + (1 if rank < extra else 0)
+
+
+def run_shard(N: int, ntraj: int, prm: DampedDrivenParams, nsteps: int, seed: int, rank: int, world: int,
+              dtype=np.complex64, noise_seed: Optional[int] = None, device: int = -1, group=None):
+    """One rank's part of an ensemble sharded over processes (one GPU each): it advances its
+    contiguous slice of trajectories (shard_range) with no exchange during the run, then
+    all-reduces the per-site density moments.  Because initial states and noise are indexed
+    by the global trajectory number, the union of the shards is the single-GPU ensemble.
+    Returns (mean, variance) of |u|^2 per site over all ntraj trajectories, and the slice."""
+    first, count = shard_range(ntraj, rank, world)
+    it = make_group(N, count, prm, nsteps, seed, dtype, noise_seed=noise_seed, traj0=first, device=device)
+    try:
+        it.step(nsteps)
+        fields = it.get_fields()[0]
+    finally:
+        it.close()
+    mean, var = allreduce_moments(fields, group=group)
+    return mean, var, (first, count)
 
 
 def density_moments(it: StrangSplittingIterator):

@@ -171,6 +171,13 @@ int gpe_set_pump(gpe_handle* h, int comp, const double* profile, int profile_com
  * component, point, trajectory); GPE_NOISE_REPLAY takes xi from gpe_run_replay. */
 int gpe_set_noise(gpe_handle* h, int mode, uint64_t seed, const double* eta,
                   const double* eta_profile);
+/* Global index of the handle's first trajectory in the Philox counter (default 0): a
+ * handle with batch B' and offset b0 draws the noise of trajectories b0 .. b0 + B' - 1 of
+ * an ensemble with the same seed, so an ensemble sharded over GPUs (one handle per rank,
+ * each with its own contiguous slice) reproduces the single-handle run bit for bit.
+ * b0 + batch must not exceed 2^32.  The reference keeps its ensemble on one device and
+ * has no counterpart (its batching is the trailing dims, src/kernels.jl:27). */
+int gpe_set_noise_offset(gpe_handle* h, int64_t traj0);
 
 /* ---- stepping ------------------------------------------------------------ */
 /* Advance nsteps full Strang steps (src/fixed_time_stepping.jl:38-50).  After every

@@ -505,14 +505,15 @@ def box_muller_f32(w0, w1):
 
 
 class PhiloxNoise:
-    """xi for half step h as drawn by the GPU noise path: counter (point, trajectory,
+    """xi for half step h as drawn by the GPU noise path: counter (point, traj0 + trajectory,
     h mod 2^32, h >> 32), key (seed mod 2^32, seed >> 32).  Two components: point p draws
     its own block, components 0 and 1 use word pairs (0,1) and (2,3).  One component: the
     points x and x + nx/2 of a row share the block of the lower one, which takes words
     (0,1) and the upper one (2,3).  Returns (M, *batch, *spatial) in C order."""
 
-    def __init__(self, seed: int, M: int, batch_shape, spatial_shape_c, fp32: bool = False):
+    def __init__(self, seed: int, M: int, batch_shape, spatial_shape_c, fp32: bool = False, traj0: int = 0):
         self.seed = int(seed)
+        self.traj0 = int(traj0)  # global index of the first trajectory (counter word 1)
         self.M = M
         self.batch_shape = tuple(batch_shape)
         self.spatial = tuple(spatial_shape_c)
@@ -522,7 +523,7 @@ class PhiloxNoise:
         P = int(np.prod(self.spatial))
         B = int(np.prod(self.batch_shape)) if self.batch_shape else 1
         p = np.tile(np.arange(P, dtype=np.uint64), B)
-        b = np.repeat(np.arange(B, dtype=np.uint64), P)
+        b = np.repeat(np.arange(B, dtype=np.uint64) + np.uint64(self.traj0), P)
         upper = None
         if self.M == 1:
             half = np.uint64(self.spatial[-1] // 2)

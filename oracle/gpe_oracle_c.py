@@ -36,7 +36,8 @@ class Desc(ctypes.Structure):
                 ("vtab", ctypes.c_void_p), ("vkind", ctypes.c_int32),
                 ("g", ctypes.c_void_p), ("c", ctypes.c_void_p),
                 ("pprof", ctypes.c_void_p * 2), ("pamp", ctypes.c_void_p * 2), ("namp", ctypes.c_int64),
-                ("dt", ctypes.c_double)]
+                ("dt", ctypes.c_double), ("noise", ctypes.c_int32), ("draw32", ctypes.c_int32),
+                ("seed", ctypes.c_uint64), ("traj0", ctypes.c_int64), ("eta", ctypes.c_void_p)]
 
 
 def build(force: bool = False) -> Path:
@@ -72,10 +73,14 @@ class CIterator:
     state (M, *batch, *spatial) complex128 in C order, as in the numpy oracle."""
 
     def __init__(self, prob: O.OracleProblem, tspan, dt: float, nsaves: int, save_start: bool = True,
-                 fp32: bool = False, threads: int = 0):
-        if prob.eta is not None or prob.nonlin_fn is not None or prob.nonlin_matrix is not None or \
-                prob.pump_fn is not None:
-            raise NotImplementedError("the C oracle covers the coefficient families without noise")
+                 fp32: bool = False, threads: int = 0, philox_seed=None, draw32: bool = False, traj0: int = 0):
+        """philox_seed: position noise (prob.eta, constant amplitudes) drawn in C by
+        Philox4x32-10 as the GPU path draws it (draw32: its FP32 draws, the top 24 bits of
+        each word, evaluated in FP64); traj0: global index of the first trajectory."""
+        if prob.nonlin_fn is not None or prob.nonlin_matrix is not None or prob.pump_fn is not None:
+            raise NotImplementedError("the C oracle covers the coefficient families")
+        if prob.eta is not None and (philox_seed is None or prob.eta_profile is not None):
+            raise NotImplementedError("the C oracle draws noise by Philox only, with constant amplitudes")
         it = O.OracleIterator(prob, tspan, dt, nsaves, save_start)
         if prob.ndim not in (1, 2) or prob.M not in (1, 2):
             raise NotImplementedError("the C oracle covers 1D and 2D grids with one or two components")
@@ -106,6 +111,9 @@ class CIterator:
             d.g = self._ptr(g)
             if prob.nonlin_c is not None:
                 d.c = self._ptr(np.asarray(prob.nonlin_c, np.complex128))
+        if prob.eta is not None:
+            d.noise, d.draw32, d.seed, d.traj0 = 1, int(draw32), int(philox_seed) & (2 ** 64 - 1), int(traj0)
+            d.eta = self._ptr(np.asarray(prob.eta, np.complex128))
         self.desc = d
         self._pump_steps = 0
         self._set_pump(nsaves * it.steps_per_save)

@@ -16,7 +16,8 @@
  * (scalar or diagonal), both built in FP64 by the caller (src/misc.jl:12-20); the
  * nonlinearity G_j = sum_l g_jl |u_l|^2 + c_j; separable pumps a_j(t) p_j(r) with a_j
  * sampled at the reference's times (t0, then t_k + dt/2 and t_k + dt for step k with end
- * time t_k).  No noise.  1D and 2D grids, one or two components, any batch.
+ * time t_k); position noise with constant amplitudes drawn by Philox4x32-10 exactly as
+ * the GPU path draws it.  1D and 2D grids, one or two components, any batch.
  *
  * Arithmetic.  fp32 = 0: everything in FP64 (the reference's ComplexF64 path).
  * fp32 = 1: the reference's ComplexF32 path as Julia evaluates it -- the fields are
@@ -57,6 +58,13 @@ typedef struct oref_desc {
   const double* pamp[2]; /* a_j at the sampling times: namp complex values */
   int64_t namp;
   double dt;
+  /* position noise -i sqrt(dt/2) eta_j xi (src/kernels.jl:42,49) with xi drawn by
+     Philox4x32-10 from (point, traj0 + trajectory, half step) as the GPU path draws it */
+  int32_t noise;         /* 0 off, 1 Philox */
+  int32_t draw32;        /* 1: the FP32 draw (top 24 bits of each word), evaluated in FP64 */
+  uint64_t seed;
+  int64_t traj0;
+  const double* eta;     /* M complex noise amplitudes */
 } oref_desc;
 
 typedef struct { double re, im; } cdbl;
@@ -188,11 +196,62 @@ static cflt* twiddles_f(const cdbl* wd, int64_t N) {
   return w;
 }
 
+/* ------------------------------------------------------------------ noise
+ * Philox4x32-10 (Salmon, Moraes, Dror, Shaw, "Parallel random numbers: as easy as 1, 2,
+ * 3", SC'11): ten rounds of two 32x32->64 multiplications with the published multipliers
+ * and Weyl key increments.  Counter (point, trajectory, h mod 2^32, h >> 32), key (seed
+ * mod 2^32, seed >> 32). */
+static void philox(uint32_t c[4], uint32_t k0, uint32_t k1) {
+  for (int r = 0; r < 10; ++r) {
+    if (r) {
+      k0 += 0x9E3779B9u;
+      k1 += 0xBB67AE85u;
+    }
+    const uint64_t p0 = (uint64_t)0xD2511F53u * c[0], p1 = (uint64_t)0xCD9E8D57u * c[2];
+    const uint32_t n0 = (uint32_t)(p1 >> 32) ^ c[1] ^ k0, n1 = (uint32_t)p1;
+    const uint32_t n2 = (uint32_t)(p0 >> 32) ^ c[3] ^ k1, n3 = (uint32_t)p0;
+    c[0] = n0; c[1] = n1; c[2] = n2; c[3] = n3;
+  }
+}
+/* Box-Muller: sqrt(-ln u1) (cos 2 pi u2, sin 2 pi u2), E|xi|^2 = 1.  FP64 draw:
+ * u1 = (w0 + 1/2) 2^-32, u2 = w1 2^-32; FP32 draw: the top 24 bits of each word. */
+static cdbl box_muller(uint32_t w0, uint32_t w1, int draw32) {
+  double u1, u2;
+  if (draw32) {
+    u1 = ((double)(w0 >> 8) + 0.5) * 0x1p-24;
+    u2 = (double)(w1 >> 8) * 0x1p-24;
+  } else {
+    u1 = ((double)w0 + 0.5) * 0x1p-32;
+    u2 = (double)w1 * 0x1p-32;
+  }
+  const double mag = sqrt(-log(u1));
+  double sn, cs;
+  sincos(2.0 * M_PI * u2, &sn, &cs);
+  if (draw32) return cd((double)(float)(mag * cs), (double)(float)(mag * sn)); /* an FP32 draw */
+  return cd(mag * cs, mag * sn);
+}
+/* xi of point p (x = p mod nx) of trajectory b at half step h, components 0..M-1: two
+ * components draw their own block (words 0,1 and 2,3); one component shares the block of
+ * the points x and x + nx/2 of a row (words 0,1 for the lower, 2,3 for the upper). */
+static void draw_xi(const oref_desc* d, int64_t p, int64_t b, int64_t h, cdbl xi[2]) {
+  const int64_t nx = d->n[0];
+  const int up = d->M == 1 && (p % nx) >= nx / 2;
+  uint32_t c[4] = {(uint32_t)(up ? p - nx / 2 : p), (uint32_t)(b + d->traj0), (uint32_t)h, (uint32_t)((uint64_t)h >> 32)};
+  philox(c, (uint32_t)d->seed, (uint32_t)(d->seed >> 32));
+  if (d->M == 1) {
+    xi[0] = up ? box_muller(c[2], c[3], d->draw32) : box_muller(c[0], c[1], d->draw32);
+  } else {
+    xi[0] = box_muller(c[0], c[1], d->draw32);
+    xi[1] = box_muller(c[2], c[3], d->draw32);
+  }
+}
+
 /* ------------------------------------------------------------------ half step
  * src/kernels.jl:37-54 with delta = dt/2 at one point:
  *   u <- cis(-delta G(u)) V (u + delta/2 F_now) + delta/2 F_next,
  * G evaluated on u before the pump is added (:40,44). */
-static void half_point(const oref_desc* d, cdbl* v, int64_t p, int64_t P, cdbl an[2], cdbl ax[2]) {
+static void half_point(const oref_desc* d, cdbl* v, int64_t p, int64_t b, int64_t h, int64_t P, cdbl an[2],
+                       cdbl ax[2]) {
   const int M = d->M;
   const double delta = 0.5 * d->dt;
   cdbl E[2];
@@ -233,6 +292,16 @@ static void half_point(const oref_desc* d, cdbl* v, int64_t p, int64_t P, cdbl a
     if (hasE[j]) w = cdmul(E[j], w);
     if (pr) w = cdadd(w, cdscale(cdmul(ax[j], prof), delta / 2));
     v[j] = w;
+  }
+  if (d->noise) {
+    /* -i sqrt(delta) eta xi, added after the linear part (src/kernels.jl:42,49) */
+    cdbl xi[2];
+    draw_xi(d, p, b, h, xi);
+    const double sq = sqrt(delta);
+    for (int j = 0; j < M; ++j) {
+      const cdbl nf = cd(sq * d->eta[2 * j + 1], -sq * d->eta[2 * j]);
+      v[j] = cdadd(v[j], cdmul(nf, xi[j]));
+    }
   }
 }
 
@@ -280,7 +349,7 @@ static void pointwise(const oref_desc* d, cdbl* u64, cflt* u32, int64_t P, int k
     for (int j = 0; j < M; ++j) v[j] = u64 ? u64[j * BP + i] : cd(u32[j * BP + i].re, u32[j * BP + i].im);
     if (kind == 0) {
       cdbl a0[2] = {an[0], an[1]}, a1[2] = {ax[0], ax[1]};
-      half_point(d, v, p, P, a0, a1);
+      half_point(d, v, p, i / P, h, P, a0, a1);
     } else {
       /* the table product, then the inverse transform's 1/P: a power of two, so scaling
          before the inverse transform rounds exactly as scaling after it */

@@ -73,3 +73,75 @@ def test_merged_moments_keep_a_small_spread_over_a_large_mean():
     assert np.allclose(m2 / cnt, n.var(-1), rtol=1e-9)
     one_pass = (n * n).mean(-1) - n.mean(-1) ** 2
     assert np.abs(one_pass / n.var(-1) - 1).max() > 1e-6  # the cancellation the merge avoids
+
+
+def test_shard_range_covers_the_ensemble_once():
+    import __graft_entry__
+    __graft_entry__.load_package()
+    from gpe_gb300 import twa
+    for ntraj in (1, 7, 1024, 1025):
+        for world in (1, 2, 3, 8):
+            nxt = 0
+            for r in range(world):
+                first, count = twa.shard_range(ntraj, r, world)
+                assert first == nxt and count >= 0
+                nxt = first + count
+            assert nxt == ntraj
+            counts = [twa.shard_range(ntraj, r, world)[1] for r in range(world)]
+            assert max(counts) - min(counts) <= 1
+    with pytest.raises(ValueError):
+        twa.shard_range(10, 2, 2)
+
+
+def test_wigner_initial_slices_equal_the_full_draw():
+    import __graft_entry__
+    __graft_entry__.load_package()
+    from gpe_gb300 import twa
+    prm = twa.DampedDrivenParams()
+    full = twa.wigner_initial(16, 0, 9, prm, seed=4)
+    part = twa.wigner_initial(16, 3, 4, prm, seed=4)
+    assert np.array_equal(full[:, :, 3:7], part)
+
+
+def test_philox_restatement_offset_draws_the_slice():
+    from oracle import gpe_oracle as O
+    full = O.PhiloxNoise(11, 1, (6,), (8, 16))
+    part = O.PhiloxNoise(11, 1, (2,), (8, 16), traj0=3)
+    for h in (0, 5):
+        assert np.array_equal(full(h)[:, 3:5], part(h))
+
+
+def _shard_worker(rank, world, port, out):
+    import torch.distributed as dist
+
+    import __graft_entry__
+    __graft_entry__.load_package()
+    from gpe_gb300 import twa
+    os.environ["MASTER_ADDR"] = "127.0.0.1"
+    os.environ["MASTER_PORT"] = str(port)
+    dist.init_process_group("gloo", rank=rank, world_size=world)
+    prm = twa.DampedDrivenParams()
+    first, count = twa.shard_range(13, rank, world)
+    fields = twa.wigner_initial(16, first, count, prm, seed=9)
+    mean, var = twa.allreduce_moments(fields)
+    out[rank] = (first, count, mean, var)
+    dist.barrier()
+    dist.destroy_process_group()
+
+
+def test_sharded_plan_and_merged_moments_two_ranks():
+    """The rank-aware plan (two gloo ranks): each rank builds its contiguous slice of a
+    13-trajectory ensemble and the merged density moments equal the whole ensemble's."""
+    import __graft_entry__
+    __graft_entry__.load_package()
+    from gpe_gb300 import twa
+    mgr = mp.Manager()
+    out = mgr.dict()
+    mp.spawn(_shard_worker, args=(2, _free_port(), out), nprocs=2, join=True)
+    full = twa.wigner_initial(16, 0, 13, twa.DampedDrivenParams(), seed=9)
+    n = np.abs(full.astype(np.complex128)) ** 2
+    assert [out[r][:2] for r in range(2)] == [(0, 7), (7, 6)]
+    for r in range(2):
+        assert np.allclose(out[r][2], n.mean(-1), rtol=1e-13)
+        assert np.allclose(out[r][3], n.var(-1), rtol=1e-11)
+    assert np.array_equal(out[0][3], out[1][3])  # every rank merges in rank order: the same bits

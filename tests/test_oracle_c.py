@@ -128,4 +128,28 @@ def test_rejects_what_it_does_not_restate():
     u0 = np.zeros((N, N), np.complex128)
     prob = O.OracleProblem(u0=(u0,), lengths=(1.0, 1.0), dispersion=lambda k, p: k[0] * 0, eta=np.array([0.1]))
     with pytest.raises(NotImplementedError):
-        OC.CIterator(prob, (0.0, 1.0), 0.1, 1)
+        OC.CIterator(prob, (0.0, 1.0), 0.1, 1)  # noise needs the Philox seed
+    prob.nonlin_fn = lambda u: u
+    with pytest.raises(NotImplementedError):
+        OC.CIterator(prob, (0.0, 1.0), 0.1, 1, philox_seed=1)
+
+
+@pytest.mark.parametrize("M,draw32", [(1, False), (1, True), (2, False)])
+def test_philox_noise_matches_numpy_restatement(M, draw32):
+    """The C oracle's Philox noise equals the numpy oracle fed with PhiloxNoise (the same
+    counter layout, key and Box-Muller transform) on a batched 2D problem with an offset."""
+    N, B, seed, traj0 = 16, 3, 977, 5
+    X, Y = O.mesh(O.grids((8.0, 8.0), (N, N))[0])
+    rng = np.random.default_rng(1)
+    u0 = tuple((rng.standard_normal((B, N, N)) + 1j * rng.standard_normal((B, N, N))) * 0.3 for _ in range(M))
+    g = np.array([[0.2]]) if M == 1 else np.array([[0.2, 0.1], [0.1, 0.3]])
+    prob = O.OracleProblem(u0=u0, lengths=(8.0, 8.0), dispersion=lambda k, p: (k[0] ** 2 + k[1] ** 2) / 2 - 0.1j,
+                           nonlin_g=g, eta=np.array([0.7 + 0.1j, 0.4][:M]))
+    noise = O.PhiloxNoise(seed, M, (B,), (N, N), fp32=draw32, traj0=traj0)
+    _, want = O.solve(prob, (0.0, 0.2), 0.02, 2, xi_source=lambda h: noise(h))
+    _, got = OC.CIterator(prob, (0.0, 0.2), 0.02, 2, philox_seed=seed, draw32=draw32, traj0=traj0).solve()
+    # FP32 draws are rounded to single precision; a last-place difference between the two
+    # libm sin/cos can move that rounding by one FP32 unit on a few draws
+    tol = 1e-7 if draw32 else 1e-12
+    for s in range(want.shape[1]):
+        assert O.rel_l2(got[:, s], want[:, s]) <= tol

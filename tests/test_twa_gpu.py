@@ -173,3 +173,50 @@ def test_variant_needs_fp32_one_component(gpe, lib):
     assert lib.gpe_set_variant(it.h, 0) == 0
     it.step(2)
     it.close()
+
+
+@pytest.mark.parametrize("dtype,resident", [(np.complex64, True), (np.complex64, False), (np.complex128, False)],
+                         ids=["f32-resident", "f32-two-pass", "f64-two-pass"])
+def test_noise_offset_reproduces_the_slice(gpe, lib, dtype, resident):
+    """A handle holding trajectories 3..5 of an ensemble (gpe_set_noise_offset, initial
+    states drawn by global trajectory index) equals trajectories 3..5 of the whole 7-
+    trajectory handle bit for bit: sharded ensembles reproduce the single-GPU run."""
+    T = twa(gpe)
+    prm = T.DampedDrivenParams()
+    N, nsteps = 64, 30
+    full = T.make_group(N, 7, prm, nsteps, seed=21, dtype=dtype, resident=resident)
+    part = T.make_group(N, 3, prm, nsteps, seed=21, dtype=dtype, resident=resident, traj0=3)
+    full.step(nsteps)
+    part.step(nsteps)
+    a, b = full.get_fields()[0], part.get_fields()[0]
+    assert np.array_equal(a[:, :, 3:6], b)
+    assert not np.array_equal(a[:, :, 0:3], b)
+    full.close()
+    part.close()
+
+
+@pytest.mark.parametrize("dtype", [np.complex64, np.complex128], ids=["f32", "f64"])
+def test_philox_draws_have_gaussian_moments(gpe, lib, dtype):
+    """Over 2^21 draws of the in-kernel generator (FP32 Box-Muller on the hardware log and
+    sin/cos approximations, FP64 on the accurate routines): a noise-only 1D field from
+    u = 0 after one step (dt = 2, eta = 1) is s = -i (xi_a + xi_b) for the two half steps'
+    draws, complex normal with <|s|^2> = 2, <s^2> = 0, <|s|^4> = 8 if <|xi|^2> = 1,
+    <xi^2> = 0 and <|xi|^4> = 2.  Bounds: 5 standard errors."""
+    N, B = 1024, 1024
+    prob = gpe.GrossPitaevskiiProblem((np.zeros((N, B), dtype),), (float(N),),
+                                      position_noise_func=lambda u, r, p: 1.0)
+    it = gpe.init(prob, gpe.StrangSplitting(), (0.0, 2.0), dt=2.0, nsaves=1, rng=20251204)
+    it.step(1)
+    s = it.get_fields()[0].astype(np.complex128).ravel()
+    it.close()
+    n = s.size
+    m2 = np.mean(np.abs(s) ** 2)
+    c2 = np.mean(s * s)
+    m4 = np.mean(np.abs(s) ** 4)
+    assert abs(m2 - 2.0) <= 5 * 2.0 / math.sqrt(n), m2            # var |s|^2 = 4
+    assert abs(c2) <= 5 * math.sqrt(8.0 / n), c2                   # <|s^2|^2> = 8
+    assert abs(m4 - 8.0) <= 5 * math.sqrt(384.0 - 64.0) / math.sqrt(n), m4  # <|s|^8> = 384
+    # no correlation between neighbouring points or trajectories
+    g = s.reshape(B, N)
+    assert abs(np.mean(g[:, 1:] * np.conj(g[:, :-1]))) <= 5 * 2.0 / math.sqrt(n)
+    assert abs(np.mean(g[1:] * np.conj(g[:-1]))) <= 5 * 2.0 / math.sqrt(n)
