@@ -15,12 +15,13 @@ e2e        : the same through the C ABI with host buffers: H2D of the state from
              memory, K steps, D2H of the final state, wall-clock timed
 roofline   : dominant kernel, algorithmic bytes per launch / its mean event-timed
              duration, against the measured HBM copy bandwidth
-cpu_baseline: the FP64 oracle (scipy FFT, all host threads) on a bounded sample
+cpu_baseline: the FP64 CPU restatements (C/OpenMP and numpy/scipy.fft, all host threads) on
+             bounded samples; the faster is the baseline
 plain_gpu  : the plain GPU split step on the same workload (cuFFT transforms + unfused
              torch elementwise kernels, the reference's step order): its rate, the rate
              of its transforms alone, and the fused passes' speed-up over both
 --impl reference: the reference's algorithm on the host cores (the Julia reference
-             cannot run here; its restatement in oracle/ is the reference arm)
+             cannot run here; its C/OpenMP restatement in oracle/ is the reference arm)
 """
 from __future__ import annotations
 
@@ -145,29 +146,52 @@ def cpu_model() -> str:
     return platform.machine()
 
 
-def cpu_baseline(steps_hint: int = 0):
-    """FP64 oracle on the host cores: one trajectory of the workload, scipy FFT with all
-    threads, steps chosen for ~10 s of work."""
+def _time_cpu_form(form: str, seconds: float):
+    """Steps per second of one FP64 CPU form of the reference's algorithm on one 512^2
+    two-component polariton trajectory, all host threads, about `seconds` of work:
+    "c" = the C/OpenMP restatement (oracle/gpe_ref.c), "numpy" = the numpy/scipy.fft one."""
     from oracle import gpe_oracle as O
     prob = oracle_problem(O)
     cores = os.cpu_count() or 1
+    if form == "c":
+        from oracle import gpe_oracle_c as OC
+        it = OC.CIterator(prob, (0.0, 200.0), DT, 100, threads=cores)
+        it.step(2)  # warm-up
+        n, t0 = 0, time.perf_counter()
+        while time.perf_counter() - t0 < seconds and n < 4000:
+            it.step(10)
+            n += 10
+        return n, time.perf_counter() - t0
     it = O.OracleIterator(prob, (0.0, 200.0), DT, 100, fft_workers=cores)
-    t = 0.0
-    it.step(t + DT, DT)  # warm-up
-    t0 = time.perf_counter()
-    n = 0
-    while True:
+    t = DT
+    it.step(t, DT)  # warm-up
+    n, t0 = 0, time.perf_counter()
+    while time.perf_counter() - t0 < seconds and n < 4000:
         t += DT
         it.step(t, DT)
         n += 1
-        el = time.perf_counter() - t0
-        if (steps_hint and n >= steps_hint) or (not steps_hint and (el > 10.0 or n >= 4000)):
-            break
-    el = time.perf_counter() - t0
+    return n, time.perf_counter() - t0
+
+
+def cpu_baseline(seconds: float = 10.0):
+    """The FP64 CPU restatements of the reference's algorithm on the host cores, each on a
+    bounded sample (~`seconds` of work): the faster is the baseline, the other is listed."""
+    cores = os.cpu_count() or 1
     P = N_GRID * N_GRID
-    return {"value": P * n / el, "unit": "grid-point-steps/s", "cores": cores, "cpu": cpu_model(), "kind": "port",
-            "sample": f"{n} Strang steps of one 512^2 two-component trajectory, FP64 numpy/scipy.fft "
-                      f"with workers={cores}, {el:.1f} s"}
+    forms = {}
+    for form in ("c", "numpy"):
+        n, el = _time_cpu_form(form, seconds)
+        forms[form] = {"value": P * n / el, "steps": n, "seconds": el}
+    best = max(forms, key=lambda f: forms[f]["value"])
+    other = "numpy" if best == "c" else "c"
+    name = {"c": "C/OpenMP restatement with its own radix-2 FFT (oracle/gpe_ref.c)",
+            "numpy": "numpy restatement with scipy.fft"}
+    return {"value": forms[best]["value"], "unit": "grid-point-steps/s", "cores": cores, "cpu": cpu_model(),
+            "kind": "port",
+            "sample": f"{forms[best]['steps']} Strang steps of one 512^2 two-component trajectory, FP64, "
+                      f"{name[best]}, {cores} threads, {forms[best]['seconds']:.1f} s",
+            "other_form": {"form": name[other], "value": forms[other]["value"],
+                           "sample": f"{forms[other]['steps']} steps, {forms[other]['seconds']:.1f} s"}}
 
 
 def oracle_problem(O):
@@ -190,21 +214,18 @@ def oracle_problem(O):
 
 
 def run_reference(args, rank, world):
-    """The reference arm: the reference's algorithm (oracle restatement) on the host."""
+    """The reference arm: the reference's algorithm on the host cores, in its faster CPU
+    restatement (the C/OpenMP one; the Julia reference has no julia binary here)."""
     if rank != 0:
         return
     from oracle import gpe_oracle as O
+    from oracle import gpe_oracle_c as OC
     prob = oracle_problem(O)
     cores = os.cpu_count() or 1
-    it = O.OracleIterator(prob, (0.0, 200.0), DT, 100, fft_workers=cores)
-    t = 0.0
-    for _ in range(args.warmup):
-        t += DT
-        it.step(t, DT)
+    it = OC.CIterator(prob, (0.0, 200.0), DT, 100, threads=cores)
+    it.step(args.warmup)
     t0 = time.perf_counter()
-    for _ in range(args.steps):
-        t += DT
-        it.step(t, DT)
+    it.step(args.steps)
     el = time.perf_counter() - t0
     P = N_GRID * N_GRID
     v = P * args.steps / el
@@ -214,8 +235,9 @@ def run_reference(args, rank, world):
             "config": config_dict(np.complex128, batch_for(np.complex128), world),
             "cpu_baseline": {"value": v, "unit": "grid-point-steps/s", "cores": cores, "cpu": cpu_model(), "kind": "port",
                              "sample": f"each step = one Strang step of one 512^2 two-component trajectory "
-                                       f"(FP64 numpy/scipy.fft, workers={cores}); the Julia reference has no "
-                                       f"julia binary on this box, so its algorithm runs as the oracle restatement"},
+                                       f"(FP64, the C/OpenMP restatement oracle/gpe_ref.c, {cores} threads); the "
+                                       f"Julia reference has no julia binary on this box, so its algorithm runs as "
+                                       f"this restatement"},
             "e2e": {"value": v, "unit": "grid-point-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
 

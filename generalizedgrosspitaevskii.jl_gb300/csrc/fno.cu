@@ -2,10 +2,9 @@
 //
 // Every linear map of the network (lift, the truncated DFTs along x and y, the per-mode
 // complex channel mixing, the pointwise channel mixing, the projection) and every
-// gradient of it is one call of a strided, batched GEMM on the tensor cores:
-// operands are rounded to BF16 while they are staged in shared memory, products
-// accumulate in FP32 (mma.sync m16n8k16), results are FP32.  GELU, bias and Adam are
-// elementwise kernels.
+// gradient of it is one call of a strided, batched GEMM on the tensor cores: operands
+// are rounded to BF16 while they are staged in shared memory, tcgen05.mma accumulates in
+// FP32 in tensor memory, results are FP32.  GELU, bias and Adam are elementwise kernels.
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
 #include <stdint.h>
@@ -14,95 +13,205 @@
 
 namespace {
 
-constexpr int BM = 128, BN = 64, BK = 32;  // CTA tile
-constexpr int NTH = 256;                   // 8 warps: 4 along M x 2 along N, warp tile 32 x 32
-constexpr int SA = BK + 8;                 // shared row pitch (bf16) of the A tile [BM][SA]
-constexpr int SB = BK + 8;                 // shared row pitch of the B tile stored as [BN][SB] (k fastest)
+// ---------------------------------------------------------------- GEMM on tcgen05
+// One CTA computes a TBM x TBN tile of C with the fifth-generation tensor cores: the
+// operand tiles are staged into shared memory as BF16 (rounded from FP32 while they are
+// loaded, any strides), one thread issues tcgen05.mma (kind::f16, BF16 x BF16 -> FP32)
+// with the accumulator in tensor memory (TMEM), and the epilogue reads it back with
+// tcgen05.ld.  K is walked in TBK-deep stages through two shared-memory buffers: the
+// threads fill one while the MMAs of the other run; tcgen05.commit arrives on a
+// per-buffer mbarrier when the MMAs reading it are done.
+//
+// Shared-memory operand layout (both A and B "K-major", no swizzle): 8 x 16-byte core
+// matrices (8 rows, 8 BF16 along K each), element (r, k) at byte
+//   (r / 8) * SBO + (k / 8) * LBO + (r % 8) * 16 + (k % 8) * 2,  LBO = 128, SBO = TBK * 16,
+// so one MMA of K = 16 reads two K-adjacent core matrices and the next one starts 256
+// bytes further.
+constexpr int TBM = 128, TBK = 64, TNTH = 256;
+constexpr uint32_t kLBO = 128, kSBO = TBK * 16;
+constexpr uint64_t kTcWaitNs = 1000000000ull;  // 1 s bound on every mbarrier wait
 
-// D = A(16x16, row) * B(16x8, col) + D with BF16 inputs and FP32 accumulators
-__device__ __forceinline__ void mma_bf16(float (&d)[4], const uint32_t (&a)[4], const uint32_t (&b)[2]) {
-  asm volatile(
-      "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
-      "{%0,%1,%2,%3};\n"
-      : "+f"(d[0]), "+f"(d[1]), "+f"(d[2]), "+f"(d[3])
-      : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b[0]), "r"(b[1]));
+__device__ int32_t g_tc_status;  // set to 1 when a wait of the GEMM ran out (gpe_fno_take_status)
+
+__device__ __forceinline__ uint32_t sptr(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+__device__ __forceinline__ uint64_t gtimer() {
+  uint64_t t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
 }
 
+__device__ __forceinline__ bool mbar_try(uint32_t bar, uint32_t parity) {
+  uint32_t done;
+  asm volatile(
+      "{\n\t.reg .pred p;\n\t"
+      "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+      "selp.u32 %0, 1, 0, p;\n\t}"
+      : "=r"(done)
+      : "r"(bar), "r"(parity)
+      : "memory");
+  return done != 0;
+}
+// bounded wait for the given phase parity of the barrier; false after kTcWaitNs
+__device__ __forceinline__ bool mbar_wait_bounded(uint32_t bar, uint32_t parity) {
+  if (mbar_try(bar, parity)) return true;
+  const uint64_t t0 = gtimer();
+  while (!mbar_try(bar, parity))
+    if (gtimer() - t0 > kTcWaitNs) return false;
+  return true;
+}
+
+// shared-memory matrix descriptor: start address, leading (K) and stride (M/N) byte
+// offsets (all encoded >> 4), the fixed 0b001 at bits 46-48, no swizzle (bits 61-63 = 0)
+__device__ __forceinline__ uint64_t smem_desc(uint32_t saddr) {
+  return (uint64_t)((saddr & 0x3FFFFu) >> 4) | ((uint64_t)((kLBO & 0x3FFFFu) >> 4) << 16) |
+         ((uint64_t)((kSBO & 0x3FFFFu) >> 4) << 32) | ((uint64_t)1 << 46);
+}
+// instruction descriptor of kind::f16: FP32 accumulator (bits 4-5 = 1), BF16 A and B
+// (bits 7-9 and 10-12 = 1), both K-major (bits 15, 16 = 0), N >> 3 at bits 17-22, M >> 4
+// at bits 24-28
+template <int BN>
+__device__ __forceinline__ uint32_t instr_desc() {
+  return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(BN >> 3) << 17) | ((uint32_t)(TBM >> 4) << 24);
+}
+
+__device__ __forceinline__ uint32_t core_off(int r, int k) {
+  return (uint32_t)((r >> 3) * kSBO + (k >> 3) * kLBO + (r & 7) * 16 + (k & 7) * 2);
+}
+
+template <int BN>
+struct TcSmem {
+  static constexpr uint32_t A_BYTES = TBM * TBK * 2, B_BYTES = BN * TBK * 2;
+  static constexpr uint32_t STAGE = A_BYTES + B_BYTES;
+  static constexpr uint32_t BAR = 2 * STAGE;   // two mbarriers
+  static constexpr uint32_t SLOT = BAR + 16;   // TMEM base address written by tcgen05.alloc
+  static constexpr uint32_t BYTES = SLOT + 16 + 1024;  // + alignment slack of the dynamic base
+};
+
 // C[z] = alpha * A[z] B[z] + beta * C[z], element (i, j) of X at X + i*x_r + j*x_c.
-__global__ void __launch_bounds__(NTH) gemm_kernel(gpe_gemm_desc g) {
-  __shared__ __align__(16) __nv_bfloat16 As[BM * SA];
-  __shared__ __align__(16) __nv_bfloat16 Bs[BN * SB];
+template <int BN>
+__global__ void __launch_bounds__(TNTH, 1) gemm_tc_kernel(gpe_gemm_desc g) {
+  using S = TcSmem<BN>;
+  extern __shared__ __align__(1024) unsigned char tc_raw[];
+  unsigned char* sm = tc_raw + ((1024u - (sptr(tc_raw) & 1023u)) & 1023u);
+  const uint32_t sbase = sptr(sm);
+  const uint32_t bar0 = sbase + S::BAR, bar1 = bar0 + 8;
+  uint32_t* tslot = reinterpret_cast<uint32_t*>(sm + S::SLOT);
   const int z = blockIdx.z;
   const float* A = g.A + (int64_t)z * g.a_z;
   const float* B = g.B + (int64_t)z * g.b_z;
   float* C = g.C + (int64_t)z * g.c_z;
-  const int64_t m0 = (int64_t)blockIdx.y * BM, n0 = (int64_t)blockIdx.x * BN;
+  const int64_t m0 = (int64_t)blockIdx.y * TBM, n0 = (int64_t)blockIdx.x * BN;
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-  const int wm = warp & 3, wn = warp >> 2;  // warp tile origin (wm*32, wn*32)
-  const int gq = lane >> 2, tq = lane & 3;
-  float acc[2][4][4];
-#pragma unroll
-  for (int i = 0; i < 2; ++i)
-#pragma unroll
-    for (int j = 0; j < 4; ++j)
-#pragma unroll
-      for (int r = 0; r < 4; ++r) acc[i][j][r] = 0.f;
-  for (int64_t k0 = 0; k0 < g.K; k0 += BK) {
-    // stage A[m0:m0+BM, k0:k0+BK] -> As[m][k], zero outside the matrix
-    for (int e = tid; e < BM * BK; e += NTH) {
-      // consecutive threads walk the operand's contiguous index
-      const int mi = g.a_r == 1 ? e % BM : e / BK, ki = g.a_r == 1 ? e / BM : e % BK;
+
+  if (warp == 0) {
+    // BN columns of tensor memory (128 lanes x BN FP32 accumulators)
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(sptr(tslot)), "r"(BN)
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+  }
+  if (tid == 0) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(bar0) : "memory");
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(bar1) : "memory");
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+  const uint32_t tmem = *tslot;
+
+  const int64_t ktiles = (g.K + TBK - 1) / TBK;
+  bool ok = true;
+  int64_t committed = -1;  // last stage whose MMAs were committed (the same in every thread)
+  for (int64_t t = 0; t < ktiles; ++t) {
+    const int buf = (int)(t & 1);
+    const uint32_t bar = buf ? bar1 : bar0;
+    if (t >= 2 && !mbar_wait_bounded(bar, (uint32_t)(((t - 2) >> 1) & 1))) ok = false;  // MMAs of stage t-2 done
+    if (__syncthreads_or(!ok)) break;
+    unsigned char* As = sm + buf * S::STAGE;
+    unsigned char* Bs = As + S::A_BYTES;
+    const int64_t k0 = t * TBK;
+    // stage A[m0:m0+TBM, k0:k0+TBK] (zero outside), consecutive threads walking the
+    // operand's contiguous index
+    for (int e = tid; e < TBM * TBK; e += TNTH) {
+      const int mi = g.a_r == 1 ? e % TBM : e / TBK, ki = g.a_r == 1 ? e / TBM : e % TBK;
       const int64_t m = m0 + mi, k = k0 + ki;
       const float v = (m < g.M && k < g.K) ? A[m * g.a_r + k * g.a_c] : 0.f;
-      As[mi * SA + ki] = __float2bfloat16_rn(v);
+      *reinterpret_cast<__nv_bfloat16*>(As + core_off(mi, ki)) = __float2bfloat16_rn(v);
     }
-    // stage B[k0:k0+BK, n0:n0+BN] -> Bs[n][k]
-    for (int e = tid; e < BN * BK; e += NTH) {
-      const int ni = g.b_c == 1 ? e % BN : e / BK, ki = g.b_c == 1 ? e / BN : e % BK;
+    // stage B[k0:k0+TBK, n0:n0+BN] as its transpose (n rows, K-major)
+    for (int e = tid; e < BN * TBK; e += TNTH) {
+      const int ni = g.b_c == 1 ? e % BN : e / TBK, ki = g.b_c == 1 ? e / BN : e % TBK;
       const int64_t n = n0 + ni, k = k0 + ki;
       const float v = (n < g.N && k < g.K) ? B[k * g.b_r + n * g.b_c] : 0.f;
-      Bs[ni * SB + ki] = __float2bfloat16_rn(v);
+      *reinterpret_cast<__nv_bfloat16*>(Bs + core_off(ni, ki)) = __float2bfloat16_rn(v);
     }
+    // the generic-proxy stores must be visible to the tensor core (async proxy)
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
     __syncthreads();
+    if (tid == 0) {
+      asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+      const uint32_t idesc = instr_desc<BN>();
 #pragma unroll
-    for (int kk = 0; kk < BK; kk += 16) {
-      uint32_t af[2][4], bf[4][2];
-#pragma unroll
-      for (int i = 0; i < 2; ++i) {
-        const int r0 = wm * 32 + i * 16 + gq;
-        const __nv_bfloat16* p = As + r0 * SA + kk + 2 * tq;
-        af[i][0] = *reinterpret_cast<const uint32_t*>(p);
-        af[i][1] = *reinterpret_cast<const uint32_t*>(p + 8 * SA);
-        af[i][2] = *reinterpret_cast<const uint32_t*>(p + 8);
-        af[i][3] = *reinterpret_cast<const uint32_t*>(p + 8 * SA + 8);
+      for (int kk = 0; kk < TBK / 16; ++kk) {
+        const uint64_t ad = smem_desc(sptr(As) + kk * 2 * kLBO);
+        const uint64_t bd = smem_desc(sptr(Bs) + kk * 2 * kLBO);
+        const uint32_t accum = (t > 0 || kk > 0) ? 1u : 0u;
+        asm volatile(
+            "{\n\t.reg .pred p;\n\t"
+            "setp.ne.b32 p, %4, 0;\n\t"
+            "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}"
+            ::"r"(tmem), "l"(ad), "l"(bd), "r"(idesc), "r"(accum)
+            : "memory");
       }
-#pragma unroll
-      for (int j = 0; j < 4; ++j) {
-        const int c0 = wn * 32 + j * 8 + gq;
-        const __nv_bfloat16* p = Bs + c0 * SB + kk + 2 * tq;
-        bf[j][0] = *reinterpret_cast<const uint32_t*>(p);
-        bf[j][1] = *reinterpret_cast<const uint32_t*>(p + 8);
-      }
-#pragma unroll
-      for (int i = 0; i < 2; ++i)
-#pragma unroll
-        for (int j = 0; j < 4; ++j) mma_bf16(acc[i][j], af[i], bf[j]);
+      // arrives on this buffer's barrier once every MMA issued so far has completed
+      asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(bar)
+                   : "memory");
     }
-    __syncthreads();
+    committed = t;
   }
+  // the last commit covers every MMA issued (also after a wait that ran out: the tensor
+  // memory is freed only once the MMAs writing it are done, or the bound has passed again)
+  if (committed >= 0 && !mbar_wait_bounded((committed & 1) ? bar1 : bar0, (uint32_t)((committed >> 1) & 1)))
+    ok = false;
+  if (!ok && tid == 0) atomicExch(&g_tc_status, 1);
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+  if (__syncthreads_and(ok)) {
+    // warp w reads TMEM lanes 32 (w % 4) .. + 31 (rows of the tile) and half w / 4 of the columns
+    const int q = warp & 3, half = warp >> 2;
+    constexpr int NC = BN / 2;
+    const int64_t m = m0 + 32 * q + lane;
 #pragma unroll
-  for (int i = 0; i < 2; ++i)
+    for (int c0 = 0; c0 < NC; c0 += 16) {
+      uint32_t r[16];
+      const uint32_t taddr = tmem + ((uint32_t)(32 * q) << 16) + (uint32_t)(half * NC + c0);
+      asm volatile(
+          "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, "
+          "%15}, [%16];"
+          : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+            "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+          : "r"(taddr)
+          : "memory");
+      asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+      if (m < g.M) {
 #pragma unroll
-    for (int j = 0; j < 4; ++j)
-#pragma unroll
-      for (int r = 0; r < 4; ++r) {
-        const int64_t m = m0 + wm * 32 + i * 16 + gq + (r >= 2 ? 8 : 0);
-        const int64_t n = n0 + wn * 32 + j * 8 + 2 * tq + (r & 1);
-        if (m < g.M && n < g.N) {
-          float* c = C + m * g.c_r + n * g.c_c;
-          *c = g.alpha * acc[i][j][r] + (g.beta != 0.f ? g.beta * *c : 0.f);
+        for (int j = 0; j < 16; ++j) {
+          const int64_t n = n0 + half * NC + c0 + j;
+          if (n < g.N) {
+            float* c = C + m * g.c_r + n * g.c_c;
+            const float acc = __uint_as_float(r[j]);
+            *c = g.alpha * acc + (g.beta != 0.f ? g.beta * *c : 0.f);
+          }
         }
       }
+    }
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  if (warp == 0) {
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(BN) : "memory");
+  }
 }
 
 // ---------------------------------------------------------------- elementwise kernels
@@ -216,6 +325,22 @@ unsigned grid_for(int64_t n) {
   return (unsigned)(b > 152 * 32 ? 152 * 32 : (b < 1 ? 1 : b));
 }
 
+template <int BN>
+int launch_gemm_tc(const gpe_gemm_desc* d, cudaStream_t s) {
+  static_assert(TcSmem<BN>::BYTES <= 227 * 1024, "shared memory");
+  const dim3 grid((unsigned)((d->N + BN - 1) / BN), (unsigned)((d->M + TBM - 1) / TBM), (unsigned)d->batch);
+  if (grid.y > 65535) return GPE_ERR_INVALID;
+  static bool attr = false;  // idempotent: every caller sets the same value
+  if (!attr) {
+    if (cudaFuncSetAttribute(gemm_tc_kernel<BN>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)TcSmem<BN>::BYTES) != cudaSuccess)
+      return GPE_ERR_CUDA;
+    attr = true;
+  }
+  gemm_tc_kernel<BN><<<grid, TNTH, TcSmem<BN>::BYTES, s>>>(*d);
+  return cudaGetLastError() == cudaSuccess ? GPE_OK : GPE_ERR_CUDA;
+}
+
 }  // namespace
 
 extern "C" {
@@ -223,10 +348,15 @@ extern "C" {
 int gpe_fno_gemm(const gpe_gemm_desc* d, void* stream) {
   if (!d || !d->A || !d->B || !d->C || d->M < 1 || d->N < 1 || d->K < 1 || d->batch < 1 || d->batch > 65535)
     return GPE_ERR_INVALID;
-  const dim3 grid((unsigned)((d->N + BN - 1) / BN), (unsigned)((d->M + BM - 1) / BM), (unsigned)d->batch);
-  if (grid.y > 65535) return GPE_ERR_INVALID;
-  gemm_kernel<<<grid, NTH, 0, (cudaStream_t)stream>>>(*d);
-  return cudaGetLastError() == cudaSuccess ? GPE_OK : GPE_ERR_CUDA;
+  // N tiles of 32 for the narrow products (channel counts, retained modes), else 64
+  return d->N <= 32 ? launch_gemm_tc<32>(d, (cudaStream_t)stream) : launch_gemm_tc<64>(d, (cudaStream_t)stream);
+}
+
+int gpe_fno_take_status(void) {
+  int32_t v = 0, zero = 0;
+  if (cudaMemcpyFromSymbol(&v, g_tc_status, sizeof v) != cudaSuccess) return GPE_ERR_CUDA;
+  if (v && cudaMemcpyToSymbol(g_tc_status, &zero, sizeof zero) != cudaSuccess) return GPE_ERR_CUDA;
+  return v ? GPE_ERR_TIMEOUT : GPE_OK;
 }
 
 int gpe_fno_permute(const float* src, float* dst, const gpe_permute_desc* p, void* stream) {

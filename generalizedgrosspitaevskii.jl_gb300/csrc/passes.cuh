@@ -475,9 +475,12 @@ __device__ __forceinline__ void half_step(typename CT<Real>::T (&u)[M], const Pa
   } else {
     using K = Coef<Real>;
     const Real dth = K::dth(a);
+    // only the densities some active G_j uses, and only the nonzero coefficients (uniform
+    // branches; adding a zero term would not change the sum): the polariton's G_2 =
+    // g |u_2|^2 costs one density and one product instead of two of each
     Real dens[M];
 #pragma unroll
-    for (int l = 0; l < M; ++l) dens[l] = u[l].x * u[l].x + u[l].y * u[l].y;
+    for (int l = 0; l < M; ++l) dens[l] = ((a.dens_mask >> l) & 1) ? u[l].x * u[l].x + u[l].y * u[l].y : (Real)0;
 #pragma unroll
     for (int j = 0; j < M; ++j) {
       hasE[j] = a.nl_on[j] != 0;
@@ -485,8 +488,8 @@ __device__ __forceinline__ void half_step(typename CT<Real>::T (&u)[M], const Pa
         Real gr = K::c(a, j, 0), gi = K::c(a, j, 1);
 #pragma unroll
         for (int l = 0; l < M; ++l) {
-          gr += K::g(a, j, l, 0) * dens[l];
-          gi += K::g(a, j, l, 1) * dens[l];
+          if (K::g(a, j, l, 0) != (Real)0) gr += K::g(a, j, l, 0) * dens[l];
+          if (a.nl_imag[j] && K::g(a, j, l, 1) != (Real)0) gi += K::g(a, j, l, 1) * dens[l];
         }
         if constexpr (std::is_same<Real, float>::value) {
           // E - 1 (see sc_m1): mag cos - 1 = (mag - 1) + mag (cos - 1)

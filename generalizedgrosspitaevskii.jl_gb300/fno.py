@@ -8,8 +8,8 @@ pump amplitude to the field at t + window, window = ``steps_per_window`` solver 
     S_l v = Re iDFT_trunc( R_l(k) . DFT_trunc(v) )   modes x modes retained modes
     out = u + proj(v4)                               pointwise width -> 4, residual
 
-Every linear map (and its gradient) is a BF16 tensor-core GEMM (gpe_fno_gemm, FP32
-accumulation); DFTs along x and y are GEMMs against fixed DFT bases restricted to the
+Every linear map (and its gradient) is a BF16 tensor-core GEMM (gpe_fno_gemm: tcgen05.mma
+with FP32 accumulation in tensor memory); DFTs along x and y are GEMMs against fixed DFT bases restricted to the
 retained modes; the per-mode mixing R_l(k) is a real (2 width) x (2 width) matrix per
 mode (a real-linear map of the complex channel vector), applied as one batched GEMM over
 modes.  Layout changes between the GEMMs are permutation kernels; GELU, bias, loss and
@@ -45,6 +45,7 @@ class PermDesc(ctypes.Structure):
 
 FNO_SIGNATURES = {
     "gpe_fno_gemm": (ctypes.c_int, [ctypes.POINTER(GemmDesc), ctypes.c_void_p]),
+    "gpe_fno_take_status": (ctypes.c_int, []),
     "gpe_fno_permute": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.POINTER(PermDesc), ctypes.c_void_p]),
     "gpe_fno_bias_act": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int64,
                                         ctypes.c_int64, ctypes.c_int64, ctypes.c_int, ctypes.c_void_p]),
@@ -95,6 +96,11 @@ def gemm(A, B, C, M, N, K, a, b, c, batch=1, alpha=1.0, beta=0.0):
     d = GemmDesc(_ptr(A), _ptr(B), _ptr(C), M, N, K, a[0], a[1], a[2] if len(a) > 2 else 0,
                  b[0], b[1], b[2] if len(b) > 2 else 0, c[0], c[1], c[2] if len(c) > 2 else 0, batch, alpha, beta)
     _chk(_lib().gpe_fno_gemm(ctypes.byref(d), _stream()))
+
+
+def take_status() -> int:
+    """GPE_ERR_TIMEOUT if a GEMM's bounded wait ran out since the last call, else 0."""
+    return int(_lib().gpe_fno_take_status())
 
 
 def permute(src, dst, dims, perm):

@@ -20,8 +20,10 @@ extern "C" {
 
 /* C[z] = alpha * A[z] * B[z] + beta * C[z] for z < batch; element (i, j) of a matrix X is
  * X + i * x_r + j * x_c, matrix z starts at X + z * x_z.  A is M x K, B is K x N.  The
- * operands are rounded to BF16 as they are staged and multiplied on the tensor cores
- * (mma.sync m16n8k16) with FP32 accumulation. */
+ * operands are rounded to BF16 as they are staged in shared memory and multiplied on the
+ * fifth-generation tensor cores (tcgen05.mma, kind::f16) with FP32 accumulation in tensor
+ * memory.  Every wait of the kernel is bounded (1 s); gpe_fno_take_status reports one that
+ * ran out. */
 typedef struct gpe_gemm_desc {
   const float* A;
   const float* B;
@@ -34,6 +36,9 @@ typedef struct gpe_gemm_desc {
   float alpha, beta;
 } gpe_gemm_desc;
 int gpe_fno_gemm(const gpe_gemm_desc* d, void* stream);
+/* GPE_ERR_TIMEOUT (and clears it) when a GEMM's bounded wait has run out since the last
+ * call, else GPE_OK; synchronises with the device. */
+int gpe_fno_take_status(void);
 
 /* dst = src (row-major dims d[0..nd)) transposed so that dst axis a is src axis perm[a]. */
 typedef struct gpe_permute_desc {

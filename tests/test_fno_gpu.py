@@ -21,7 +21,9 @@ def bf16(x):
 
 
 @pytest.mark.parametrize("M,N,K,ta,tb,batch,beta", [(200, 70, 96, False, False, 1, 0.0), (64, 128, 40, True, False, 3, 0.0),
-                                                     (33, 17, 300, False, True, 2, 1.0), (129, 65, 16, True, True, 1, 1.0)])
+                                                     (33, 17, 300, False, True, 2, 1.0), (129, 65, 16, True, True, 1, 1.0),
+                                                     (4096, 32, 32, True, False, 2, 0.0), (1000, 64, 64, False, True, 1, 1.0),
+                                                     (256, 200, 1024, False, False, 1, 0.0), (128, 32, 8, True, True, 1, 0.0)])
 def test_gemm_matches_numpy(gpe, lib, M, N, K, ta, tb, batch, beta):
     torch = pytest.importorskip("torch")
     F = fno_mod(gpe)
@@ -37,6 +39,7 @@ def test_gemm_matches_numpy(gpe, lib, M, N, K, ta, tb, batch, beta):
     Bop = np.swapaxes(B, 1, 2) if tb else B
     want = 1.5 * np.matmul(bf16(Aop).astype(np.float64), bf16(Bop).astype(np.float64)) + beta * C0
     got = Ct.cpu().numpy()
+    assert F.take_status() == 0  # no bounded wait of the tcgen05 kernel ran out
     assert np.abs(got - want).max() <= 1e-4 * np.abs(want).max() + 1e-5
 
 
