@@ -852,6 +852,48 @@ def run_fno(args):
                       "window_cost_by_batch": per_window}), flush=True)
 
 
+def run_gemm_bench(args):
+    """Throughput of the surrogate's tcgen05 GEMM (gpe_fno_gemm: BF16 operands staged from
+    FP32, FP32 accumulation in tensor memory) on the shapes the network runs at a batch of
+    64 windows (pointwise channel mixing: M = 64 x 128^2 points, N = K = 32; the truncated
+    DFT along x: M = 64 x 32 x 128 rows, N = 32 modes, K = 128) and on a square 8192^3
+    product, against the measured cuBLAS BF16 peak.  CUDA events, after warm-up."""
+    import torch
+    F = __import__("gpe_gb300.fno", fromlist=["FNO"])
+    import __graft_entry__ as G
+    G.load_package()
+    peak = None
+    pk = ROOT / "MEASURED_PEAKS.json"
+    if pk.exists():
+        peak = float(json.loads(pk.read_text())["bf16_tflops"])
+    shapes = [("channel mix, 64 windows", 64 * 128 * 128, 32, 32), ("x DFT, 64 windows", 64 * 32 * 128, 32, 128),
+              ("square", 8192, 8192, 8192)]
+    out = []
+    for name, M, N, K in shapes:
+        A = torch.randn(M, K, device="cuda")
+        B = torch.randn(K, N, device="cuda")
+        C = torch.empty(M, N, device="cuda")
+        run = lambda: F.gemm(A, B, C, M, N, K, (K, 1), (N, 1), (N, 1))
+        for _ in range(3):
+            run()
+        reps = 20 if M * N * K < 1e11 else 5
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        e0.record()
+        for _ in range(reps):
+            run()
+        e1.record()
+        torch.cuda.synchronize()
+        ms = e0.elapsed_time(e1) / reps
+        tf = 2.0 * M * N * K / (ms * 1e-3) / 1e12
+        gbs = 4.0 * (M * K + K * N + M * N) / (ms * 1e-3) / 1e9
+        out.append({"shape": name, "M": M, "N": N, "K": K, "ms": ms, "tflops": tf, "operand_gbs": gbs,
+                    "frac_of_bf16_peak": (tf / peak) if peak else None})
+        del A, B, C
+    assert F.take_status() == 0
+    print(json.dumps({"metric": "tcgen05 GEMM throughput", "bf16_peak_tflops": peak, "runs": out}), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -883,6 +925,7 @@ def main():
     ap.add_argument("--fno-epochs", type=int, default=10)
     ap.add_argument("--fno-rollout", type=int, default=400)
     ap.add_argument("--fno-window", type=int, default=20, help="solver steps one surrogate window replaces")
+    ap.add_argument("--gemm-bench", action="store_true", help="time the surrogate's tcgen05 GEMM on its shapes")
     args = ap.parse_args()
     if args.warmup < 3:
         ap.error("--warmup must be >= 3")
@@ -894,6 +937,10 @@ def main():
     if args.fno:
         if rank == 0:
             run_fno(args)
+        return
+    if args.gemm_bench:
+        if rank == 0:
+            run_gemm_bench(args)
         return
     if args.impl == "reference":
         run_reference(args, rank, world)

@@ -868,6 +868,11 @@ static PassArgs base_args(gpe_handle* h) {
   for (int j = 0; j < h->M; ++j)
     for (int l = 0; l < h->M; ++l)
       if (h->nl_on[j] && (h->g[j][l][0] != 0.0 || h->g[j][l][1] != 0.0)) a.dens_mask |= 1 << l;
+  a.g_nz = 0;
+  for (int j = 0; j < 2; ++j)
+    for (int l = 0; l < 2; ++l)
+      for (int r = 0; r < 2; ++r)
+        if (h->g[j][l][r] != 0.0) a.g_nz |= 1 << (j * 4 + l * 2 + r);
   for (int j = 0; j < 2; ++j) {
     a.nl_on[j] = h->nl_on[j];
     a.nl_imag[j] = h->c[j][1] != 0.0;

@@ -35,6 +35,7 @@ struct PassArgs {
   // double-word form, so no pass converts per point.
   int32_t nl_on[2], nl_imag[2];
   int32_t dens_mask;  // bit l: some active G_j depends on |u_l|^2
+  int32_t g_nz;       // bit j*4 + l*2 + r: g[j][l][r] != 0 (tested on the integer pipe)
   double g[2][2][2];
   double c[2][2];
   float gf[2][2][2], gl[2][2][2];

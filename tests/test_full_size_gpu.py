@@ -106,3 +106,41 @@ def test_polariton_full_length_run(gpe, oracle, lib, fp64):
     ots, ores = oracle.solve(orc, (0.0, 200.0), 0.05, 100)
     assert np.array_equal(ts, ots)
     assert_close(oracle, res, ores, 1e-10)
+
+
+_C1 = {}
+
+
+def _c1_oracle(oracle, fp32: bool):
+    """Saves of the C oracle on the polariton configuration at its own size (512^2,
+    tspan (0, 200), dt 0.05: 4000 steps, 100 saves), FP64 or the reference's FP32."""
+    if fp32 not in _C1:
+        from oracle import gpe_oracle_c as OC
+        _, orc = polariton2d(N=512, L=256.0, A=5.0, ramp=200.0)
+        _C1[fp32] = OC.solve(orc, (0.0, 200.0), 0.05, 100, fp32=fp32)
+    return _C1[fp32]
+
+
+@pytest.mark.parametrize("dtype,fp64", [(np.complex128, "native"), (np.complex64, "native")], ids=["f64", "f32"])
+def test_polariton_c1_full_size_every_save(gpe, oracle, lib, dtype, fp64):
+    """The polariton configuration exactly as specified (512^2, two components, 2x2
+    dispersion, pump ramp over t in [0, 200], 4000 steps, 100 saves) against the C oracle
+    at every save: ComplexF64 <= 1e-10; ComplexF32 <= 1e-5 where the reference's own
+    ComplexF32 arithmetic (the C oracle's fp32 mode) stays within 1e-5, else within 2x it."""
+    gkw, _ = polariton2d(N=512, L=256.0, A=5.0, ramp=200.0, dtype=dtype)
+    ts, res = gpe.solve(gpe.GrossPitaevskiiProblem(**gkw), gpe.StrangSplitting(), (0.0, 200.0), dt=0.05,
+                        nsaves=100, fp64=fp64)
+    ots, ores = _c1_oracle(oracle, False)
+    assert np.array_equal(ts, ots)
+    got = np.stack([c_order(r) for r in res], 0).astype(np.complex128)  # (M, nsaves+1, y, x)
+    errs = [oracle.rel_l2(got[:, s], ores[:, s]) for s in range(1, 101)]
+    if dtype == np.complex128:
+        print(f"C1 f64: worst save {max(errs):.2e}")
+        assert max(errs) <= 1e-10, max(errs)
+        return
+    _, r32 = _c1_oracle(oracle, True)
+    ref32 = [oracle.rel_l2(r32[:, s], ores[:, s]) for s in range(1, 101)]
+    print(f"C1 f32: worst save {max(errs):.2e}, reference FP32 arithmetic worst {max(ref32):.2e}")
+    for s in range(100):
+        bound = 1e-5 if ref32[s] <= 1e-5 else 2.0 * ref32[s]
+        assert errs[s] <= bound, (s, errs[s], ref32[s])
