@@ -36,3 +36,28 @@ def test_smooth_kerr_1000_steps(gpe, oracle, lib):
     err = run(gpe, oracle, 1.0)
     assert err["dw"] <= 1e-11 and err["native"] <= 1e-12, err
 
+
+
+@pytest.mark.parametrize("g", [0.0, 1.0], ids=["dispersion-only", "kerr"])
+def test_fp32_norm_drift_stays_at_rounding_level(gpe, lib, g):
+    """FP32 fields with FP64-accurate constants and the nonlinear phase added as one
+    increment: the norm, conserved exactly by the split step for real D and G, stays within
+    3e-6 over 1000 steps on 512^2 (a constant rounded to FP32, or the phase added in two
+    roundings, gave a steady drift reaching 2e-5 to 2e-4)."""
+    N = 512
+    x = np.arange(N) * (LB / N)
+    X, Y = np.meshgrid(x, x, indexing="ij")
+    u0 = np.exp(-((X - 16) ** 2 + (Y - 16) ** 2) / 4.0).astype(np.complex64)
+    kw = dict(dispersion=lambda k, p: (k[0] ** 2 + k[1] ** 2) / 2)
+    if g:
+        kw["nonlinearity"] = lambda u, p: g * np.abs(u[0]) ** 2
+    it = gpe.init(gpe.GrossPitaevskiiProblem((u0,), (LB, LB), **kw), gpe.StrangSplitting(), (0.0, NSTEPS * DT),
+                  dt=DT, nsaves=20)
+    n0 = it.norm()[0]
+    drift = []
+    for _ in range(10):
+        it.step(NSTEPS // 10)
+        drift.append(it.norm()[0] / n0 - 1)
+    it.close()
+    print(f"FP32 norm drift (g={g}) every 100 steps: " + " ".join(f"{d:.1e}" for d in drift))
+    assert max(abs(d) for d in drift) <= 3e-6, drift
