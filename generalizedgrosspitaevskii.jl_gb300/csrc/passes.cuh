@@ -656,17 +656,24 @@ __device__ __forceinline__ void store_save(void* base, int64_t idx, const typena
   }
 }
 
-// conj in place (the inverse transform is conj o FFT o conj, so each kernel holds a
-// single forward FFT instance)
+// Swap real and imaginary parts in place.  With s(z) = i conj(z), s o FFT o s equals
+// conj o FFT o conj, the inverse transform: each kernel holds a single forward FFT
+// instance, and the inverse costs register moves, no floating-point instruction (a
+// negation under the run-time direction test could take an FP64 pipe slot).
 template <typename C, int E>
-__device__ __forceinline__ void conj_all(C (&x)[E]) {
+__device__ __forceinline__ void swap_all(C (&x)[E]) {
 #pragma unroll
   for (int i = 0; i < E; ++i) {
     if constexpr (std::is_same<C, dwc>::value) {
-      x[i].yh = -x[i].yh;
-      x[i].yl = -x[i].yl;
+      const float h = x[i].xh, l = x[i].xl;
+      x[i].xh = x[i].yh;
+      x[i].xl = x[i].yl;
+      x[i].yh = h;
+      x[i].yl = l;
     } else {
-      x[i].y = -x[i].y;
+      const auto r = x[i].x;
+      x[i].x = x[i].y;
+      x[i].y = r;
     }
   }
 }
@@ -681,19 +688,19 @@ __device__ __forceinline__ void fft_components(C (&x)[M][E], bool inverse, int t
     // all components in one pass (FP32: the twiddle loads and barriers are shared)
     if (inverse) {
 #pragma unroll
-      for (int m = 0; m < M; ++m) conj_all(x[m]);
+      for (int m = 0; m < M; ++m) swap_all(x[m]);
     }
     fft_line_joint<C, N, E, -1, M>(x, t, lay, cstride, tw);
     if (inverse) {
 #pragma unroll
-      for (int m = 0; m < M; ++m) conj_all(x[m]);
+      for (int m = 0; m < M; ++m) swap_all(x[m]);
     }
   } else {
 #pragma unroll 1
     for (int m = 0; m < M; ++m) {
-      if (inverse) conj_all(x[0]);
+      if (inverse) swap_all(x[0]);
       fft_line<C, N, E, -1>(x[0], t, lay, tw, renorm);
-      if (inverse) conj_all(x[0]);
+      if (inverse) swap_all(x[0]);
       if constexpr (M == 2) {
 #pragma unroll
         for (int i = 0; i < E; ++i) {
