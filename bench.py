@@ -859,9 +859,9 @@ def run_gemm_bench(args):
     DFT along x: M = 64 x 32 x 128 rows, N = 32 modes, K = 128) and on a square 8192^3
     product, against the measured cuBLAS BF16 peak.  CUDA events, after warm-up."""
     import torch
-    F = __import__("gpe_gb300.fno", fromlist=["FNO"])
     import __graft_entry__ as G
     G.load_package()
+    F = __import__("gpe_gb300.fno", fromlist=["FNO"])
     peak = None
     pk = ROOT / "MEASURED_PEAKS.json"
     if pk.exists():

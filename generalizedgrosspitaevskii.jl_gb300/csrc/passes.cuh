@@ -507,9 +507,14 @@ __device__ __forceinline__ void half_step(typename CT<Real>::T (&u)[M], const Pa
         } else {
           Real s, c;
           sc<Real>(dth * gr, &s, &c);
-          const Real mag = a.nl_imag[j] ? rexp(dth * gi) : (Real)1;
-          E[j].x = mag * c;
-          E[j].y = -mag * s;
+          if (a.nl_imag[j]) {
+            const Real mag = rexp(dth * gi);
+            E[j].x = mag * c;
+            E[j].y = -mag * s;
+          } else {  // a real G: no magnitude factor to multiply in
+            E[j].x = c;
+            E[j].y = -s;
+          }
         }
       }
     }
