@@ -352,9 +352,34 @@ def measure_fused(pkg, lib, L, args, dtype, fp64: str, B: int, local_rank: int, 
     return out
 
 
+def fp64_roof(m: dict, B: int, sm_mhz):
+    """The FP64-pipe roof of the native FP64 passes: nominal flops per grid point and launch
+    (5 log2 N per point of each complex line transform, the conventional FFT count; 32 for
+    the 2x2 complex k-space mat-vec; 30 per half step for the density, phase, rotation and
+    pump) over the mean event-timed launch duration, against GB300's FP64 peak (two FP64
+    FMAs a clock per SM, as ncu reports it, at the clock sampled during the run)."""
+    try:
+        import torch
+        nsm = torch.cuda.get_device_properties(0).multi_processor_count
+    except Exception:
+        nsm = 152
+    mhz = sm_mhz or 2070.0
+    peak = 2 * 2 * nsm * mhz * 1e6 / 1e12
+    P = N_GRID * N_GRID
+    lg = int(math.log2(N_GRID))
+    flops = {"row": 2 * 2 * 5 * lg + 2 * 30, "col": 2 * 2 * 5 * lg + 32}  # two components
+    out = {}
+    for i, k in enumerate(["row", "col"]):
+        ms = m["kms"][i] / max(m["kn"][i], 1)
+        tf = flops[k] * P * B / (ms * 1e-3) / 1e12
+        out[k] = {"flops_per_point": flops[k], "achieved_tflops": tf, "frac": tf / peak}
+    return {"bound": "fp64 pipe", "unit": "TFLOP/s", "peak": peak,
+            "peak_source": f"2 FP64 FMA per clock per SM x {nsm} SMs x {mhz:.0f} MHz", "kernels": out}
+
+
 def roofline_of(m: dict, dtype, fp64: str, B: int):
     """Dominant kernel's algorithmic bytes per launch over its mean event-timed duration,
-    against the measured HBM copy bandwidth."""
+    against the measured HBM copy bandwidth (and, for native FP64, the FP64-pipe roof)."""
     P = N_GRID * N_GRID
     kms, kn = m["kms"], m["kn"]
     ab = algorithmic_bytes(dtype, B)
@@ -372,7 +397,9 @@ def roofline_of(m: dict, dtype, fp64: str, B: int):
                             "mean_ms": float(kms[i] / max(kn[i], 1)),
                             "achieved_gbs": float(ab[k] * P * B / (kms[i] / max(kn[i], 1) * 1e-3) / 1e9)}
                         for i, k in enumerate(["row", "col"])},
-            "binding_limit": binding_limit(dtype, fp64)}
+            "binding_limit": binding_limit(dtype, fp64),
+            **({"compute_roof": fp64_roof(m, B, (m.get("clocks") or {}).get("sm_mhz"))}
+               if dtype == np.complex128 and fp64 == "native" else {})}
 
 
 def run_gpu(args, rank, world, local_rank):
