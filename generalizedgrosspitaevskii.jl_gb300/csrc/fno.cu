@@ -79,6 +79,72 @@ __device__ __forceinline__ uint32_t core_off(int r, int k) {
   return (uint32_t)((r >> 3) * kSBO + (k >> 3) * kLBO + (r & 7) * 16 + (k & 7) * 2);
 }
 
+__device__ __forceinline__ uint32_t pack_bf16(float a, float b) {
+  const __nv_bfloat162 h = __floats2bfloat162_rn(a, b);  // a in the low half
+  return *reinterpret_cast<const uint32_t*>(&h);
+}
+
+// Stage an R x TBK tile of an FP32 operand, element (r, k) at G[r * sr + k * sk], into the
+// core-matrix layout as BF16 (zero outside r < rlim, k < klim).  mode 1: K contiguous
+// (sk = 1, rows 16-byte aligned): a thread loads 8 consecutive k of one row as two float4
+// and stores them as one 16-byte chunk.  mode 2: rows contiguous (sr = 1, columns 16-byte
+// aligned): a thread loads 4 rows x 8 k as eight float4 along the rows, transposes them in
+// registers and stores four 16-byte chunks.  mode 0 (any strides), and the chunks that
+// cross the matrix edge: one element at a time, consecutive threads along the contiguous
+// index.
+template <int R>
+__device__ __forceinline__ void stage_tile(unsigned char* dst, const float* __restrict__ G, int64_t r0, int64_t k0,
+                                           int64_t rlim, int64_t klim, int64_t sr, int64_t sk, int mode, int tid) {
+  if (mode == 1) {
+    for (int c = tid; c < R * (TBK / 8); c += TNTH) {
+      const int ri = c / (TBK / 8), ki = (c % (TBK / 8)) * 8;
+      const int64_t r = r0 + ri, k = k0 + ki;
+      uint4 q;
+      if (r < rlim && k + 7 < klim) {
+        const float4 a = __ldg(reinterpret_cast<const float4*>(G + r * sr + k));
+        const float4 b = __ldg(reinterpret_cast<const float4*>(G + r * sr + k + 4));
+        q = make_uint4(pack_bf16(a.x, a.y), pack_bf16(a.z, a.w), pack_bf16(b.x, b.y), pack_bf16(b.z, b.w));
+      } else {
+        float v[8];
+#pragma unroll
+        for (int j = 0; j < 8; ++j) v[j] = (r < rlim && k + j < klim) ? G[r * sr + (k + j) * sk] : 0.f;
+        q = make_uint4(pack_bf16(v[0], v[1]), pack_bf16(v[2], v[3]), pack_bf16(v[4], v[5]), pack_bf16(v[6], v[7]));
+      }
+      *reinterpret_cast<uint4*>(dst + core_off(ri, ki)) = q;
+    }
+  } else if (mode == 2) {
+    for (int c = tid; c < (R / 4) * (TBK / 8); c += TNTH) {
+      const int ri = (c % (R / 4)) * 4, ki = (c / (R / 4)) * 8;  // consecutive threads along the rows
+      const int64_t r = r0 + ri, k = k0 + ki;
+      float v[8][4];
+      if (r + 3 < rlim && k + 7 < klim) {
+#pragma unroll
+        for (int j = 0; j < 8; ++j) {
+          const float4 a = __ldg(reinterpret_cast<const float4*>(G + (k + j) * sk + r));
+          v[j][0] = a.x; v[j][1] = a.y; v[j][2] = a.z; v[j][3] = a.w;
+        }
+      } else {
+#pragma unroll
+        for (int j = 0; j < 8; ++j)
+#pragma unroll
+          for (int i = 0; i < 4; ++i) v[j][i] = (r + i < rlim && k + j < klim) ? G[(r + i) * sr + (k + j) * sk] : 0.f;
+      }
+#pragma unroll
+      for (int i = 0; i < 4; ++i)
+        *reinterpret_cast<uint4*>(dst + core_off(ri + i, ki)) =
+            make_uint4(pack_bf16(v[0][i], v[1][i]), pack_bf16(v[2][i], v[3][i]), pack_bf16(v[4][i], v[5][i]),
+                       pack_bf16(v[6][i], v[7][i]));
+    }
+  } else {
+    for (int e = tid; e < R * TBK; e += TNTH) {
+      const int ri = sr == 1 ? e % R : e / TBK, ki = sr == 1 ? e / R : e % TBK;
+      const int64_t r = r0 + ri, k = k0 + ki;
+      const float v = (r < rlim && k < klim) ? G[r * sr + k * sk] : 0.f;
+      *reinterpret_cast<__nv_bfloat16*>(dst + core_off(ri, ki)) = __float2bfloat16_rn(v);
+    }
+  }
+}
+
 template <int BN>
 struct TcSmem {
   static constexpr uint32_t A_BYTES = TBM * TBK * 2, B_BYTES = BN * TBK * 2;
@@ -89,8 +155,9 @@ struct TcSmem {
 };
 
 // C[z] = alpha * A[z] B[z] + beta * C[z], element (i, j) of X at X + i*x_r + j*x_c.
+// vmode: bits 0-1 the staging mode of A (stage_tile), bits 2-3 that of B
 template <int BN>
-__global__ void __launch_bounds__(TNTH, 1) gemm_tc_kernel(gpe_gemm_desc g) {
+__global__ void __launch_bounds__(TNTH, 2) gemm_tc_kernel(gpe_gemm_desc g, int vmode) {
   using S = TcSmem<BN>;
   extern __shared__ __align__(1024) unsigned char tc_raw[];
   unsigned char* sm = tc_raw + ((1024u - (sptr(tc_raw) & 1023u)) & 1023u);
@@ -131,21 +198,10 @@ __global__ void __launch_bounds__(TNTH, 1) gemm_tc_kernel(gpe_gemm_desc g) {
     unsigned char* As = sm + buf * S::STAGE;
     unsigned char* Bs = As + S::A_BYTES;
     const int64_t k0 = t * TBK;
-    // stage A[m0:m0+TBM, k0:k0+TBK] (zero outside), consecutive threads walking the
-    // operand's contiguous index
-    for (int e = tid; e < TBM * TBK; e += TNTH) {
-      const int mi = g.a_r == 1 ? e % TBM : e / TBK, ki = g.a_r == 1 ? e / TBM : e % TBK;
-      const int64_t m = m0 + mi, k = k0 + ki;
-      const float v = (m < g.M && k < g.K) ? A[m * g.a_r + k * g.a_c] : 0.f;
-      *reinterpret_cast<__nv_bfloat16*>(As + core_off(mi, ki)) = __float2bfloat16_rn(v);
-    }
-    // stage B[k0:k0+TBK, n0:n0+BN] as its transpose (n rows, K-major)
-    for (int e = tid; e < BN * TBK; e += TNTH) {
-      const int ni = g.b_c == 1 ? e % BN : e / TBK, ki = g.b_c == 1 ? e / BN : e % TBK;
-      const int64_t n = n0 + ni, k = k0 + ki;
-      const float v = (n < g.N && k < g.K) ? B[k * g.b_r + n * g.b_c] : 0.f;
-      *reinterpret_cast<__nv_bfloat16*>(Bs + core_off(ni, ki)) = __float2bfloat16_rn(v);
-    }
+    // stage A[m0:m0+TBM, k0:k0+TBK] and B[k0:k0+TBK, n0:n0+BN] (as n rows, K-major), zero
+    // outside the matrices
+    stage_tile<TBM>(As, A, m0, k0, g.M, g.K, g.a_r, g.a_c, vmode & 3, tid);
+    stage_tile<BN>(Bs, B, n0, k0, g.N, g.K, g.b_c, g.b_r, (vmode >> 2) & 3, tid);
     // the generic-proxy stores must be visible to the tensor core (async proxy)
     asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
     __syncthreads();
@@ -180,6 +236,8 @@ __global__ void __launch_bounds__(TNTH, 1) gemm_tc_kernel(gpe_gemm_desc g) {
     // warp w reads TMEM lanes 32 (w % 4) .. + 31 (rows of the tile) and half w / 4 of the columns
     const int q = warp & 3, half = warp >> 2;
     constexpr int NC = BN / 2;
+    // rows of C contiguous and 16-byte aligned: vector stores
+    const bool cvec = g.c_c == 1 && g.c_r % 4 == 0 && g.c_z % 4 == 0 && (((uintptr_t)g.C) & 15) == 0;
     const int64_t m = m0 + 32 * q + lane;
 #pragma unroll
     for (int c0 = 0; c0 < NC; c0 += 16) {
@@ -193,7 +251,21 @@ __global__ void __launch_bounds__(TNTH, 1) gemm_tc_kernel(gpe_gemm_desc g) {
           : "r"(taddr)
           : "memory");
       asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
-      if (m < g.M) {
+      const int64_t nb = n0 + half * NC + c0;
+      if (m < g.M && cvec && nb + 15 < g.N) {
+        // 16 consecutive columns of one row: four 16-byte stores
+        float4* c4 = reinterpret_cast<float4*>(C + m * g.c_r + nb);
+#pragma unroll
+        for (int q4 = 0; q4 < 4; ++q4) {
+          float4 o = make_float4(g.alpha * __uint_as_float(r[4 * q4]), g.alpha * __uint_as_float(r[4 * q4 + 1]),
+                                 g.alpha * __uint_as_float(r[4 * q4 + 2]), g.alpha * __uint_as_float(r[4 * q4 + 3]));
+          if (g.beta != 0.f) {
+            const float4 old = c4[q4];
+            o.x += g.beta * old.x; o.y += g.beta * old.y; o.z += g.beta * old.z; o.w += g.beta * old.w;
+          }
+          c4[q4] = o;
+        }
+      } else if (m < g.M) {
 #pragma unroll
         for (int j = 0; j < 16; ++j) {
           const int64_t n = n0 + half * NC + c0 + j;
@@ -337,7 +409,15 @@ int launch_gemm_tc(const gpe_gemm_desc* d, cudaStream_t s) {
       return GPE_ERR_CUDA;
     attr = true;
   }
-  gemm_tc_kernel<BN><<<grid, TNTH, TcSmem<BN>::BYTES, s>>>(*d);
+  // vectorised staging where an operand's rows or columns are contiguous and 16-byte aligned
+  auto mode = [](const float* X, int64_t sr, int64_t sk, int64_t sz) {
+    const bool al = ((uintptr_t)X & 15) == 0 && sz % 4 == 0;
+    if (al && sk == 1 && sr % 4 == 0) return 1;
+    if (al && sr == 1 && sk % 4 == 0) return 2;
+    return 0;
+  };
+  const int vmode = mode(d->A, d->a_r, d->a_c, d->a_z) | (mode(d->B, d->b_c, d->b_r, d->b_z) << 2);
+  gemm_tc_kernel<BN><<<grid, TNTH, TcSmem<BN>::BYTES, s>>>(*d, vmode);
   return cudaGetLastError() == cudaSuccess ? GPE_OK : GPE_ERR_CUDA;
 }
 

@@ -23,15 +23,27 @@ def bf16(x):
 @pytest.mark.parametrize("M,N,K,ta,tb,batch,beta", [(200, 70, 96, False, False, 1, 0.0), (64, 128, 40, True, False, 3, 0.0),
                                                      (33, 17, 300, False, True, 2, 1.0), (129, 65, 16, True, True, 1, 1.0),
                                                      (4096, 32, 32, True, False, 2, 0.0), (1000, 64, 64, False, True, 1, 1.0),
-                                                     (256, 200, 1024, False, False, 1, 0.0), (128, 32, 8, True, True, 1, 0.0)])
-def test_gemm_matches_numpy(gpe, lib, M, N, K, ta, tb, batch, beta):
+                                                     (256, 200, 1024, False, False, 1, 0.0), (128, 32, 8, True, True, 1, 0.0),
+                                                     (512, 64, 64, False, False, 1, 0.0), (512, 64, 64, True, True, 2, 0.0)])
+@pytest.mark.parametrize("shift", [0, 1], ids=["aligned", "shifted"])
+def test_gemm_matches_numpy(gpe, lib, M, N, K, ta, tb, batch, beta, shift):
+    """Every stride pattern in both staging forms: 16-byte aligned operands whose rows or
+    columns are contiguous take the vectorised staging, operands shifted by one element
+    (not 16-byte aligned) the element-wise one."""
     torch = pytest.importorskip("torch")
     F = fno_mod(gpe)
     rng = np.random.default_rng(M + N + K)
     A = rng.standard_normal((batch, K, M) if ta else (batch, M, K)).astype(np.float32)
     B = rng.standard_normal((batch, N, K) if tb else (batch, K, N)).astype(np.float32)
     C0 = rng.standard_normal((batch, M, N)).astype(np.float32)
-    At, Bt, Ct = (torch.tensor(x, device="cuda") for x in (A, B, C0))
+
+    def dev(x):
+        buf = torch.zeros(x.size + shift, device="cuda")
+        buf[shift:] = torch.tensor(x.ravel(), device="cuda")
+        return buf[shift:]  # the operand starts `shift` elements into its buffer
+
+    At, Bt = dev(A), dev(B)
+    Ct = torch.tensor(C0, device="cuda")
     a = (1, M, K * M) if ta else (K, 1, M * K)
     b = (1, K, N * K) if tb else (N, 1, K * N)
     F.gemm(At, Bt, Ct, M, N, K, a, b, (N, 1, M * N), batch=batch, alpha=1.5, beta=beta)
