@@ -210,16 +210,44 @@ __device__ __forceinline__ void dif_layers(C (&v)[R]) {
   }
 }
 
+// bit-reversed register order -> natural order
+template <int R, typename C>
+__device__ __forceinline__ void unscramble(C (&v)[R]) {
+  C tmp[R];
+#pragma unroll
+  for (int k = 0; k < R; ++k) tmp[k] = v[bitrev(k, ilog2(R))];
+#pragma unroll
+  for (int k = 0; k < R; ++k) v[k] = tmp[k];
+}
+
 // In-register DFT of R points (R in {1,2,4,8,16}), natural order in and out.
 template <int R, int DIR, typename C>
 __device__ __forceinline__ void dft_regs(C (&v)[R]) {
   if constexpr (R > 1) {
     dif_layers<R, DIR, R / 2>(v);
-    C tmp[R];
-#pragma unroll
-    for (int k = 0; k < R; ++k) tmp[k] = v[bitrev(k, ilog2(R))];
-#pragma unroll
-    for (int k = 0; k < R; ++k) v[k] = tmp[k];
+    unscramble<R>(v);
+  }
+}
+
+// FP64: the first decimation-in-frequency layer of a twiddled radix-R stage with the
+// twiddle products taken into FMAs.  For the pair (I, I + H), a = x_I w_I and c = x_{I+H}
+// w_{I+H}: a + c is one chain of two FMAs per part on top of a, and a - c = 2a - (a + c)
+// one more FMA per part: 10 FP64 operations a pair instead of 12 (a complex product, a sum
+// and a difference), 6 instead of 8 for I = 0 whose twiddle is 1.  The difference carries
+// the sum's rounding, an error bounded by the pair's norm as an FFT butterfly's is.
+template <int R, int DIR, int H, int I>
+__device__ __forceinline__ void fused_first_layer(double2 (&v)[R], const double2 (&w)[R]) {
+  if constexpr (I < H) {
+    const double2 a = I == 0 ? v[0] : cmul(v[I], w[I]);
+    const double2 c = v[I + H], wc = w[I + H];
+    double2 sum, dif;
+    sum.x = fma(c.x, wc.x, fma(-c.y, wc.y, a.x));
+    sum.y = fma(c.x, wc.y, fma(c.y, wc.x, a.y));
+    dif.x = fma(2.0, a.x, -sum.x);
+    dif.y = fma(2.0, a.y, -sum.y);
+    v[I] = sum;
+    v[I + H] = twc<DIR, 2 * H, I>(dif);
+    fused_first_layer<R, DIR, H, I + 1>(v, w);
   }
 }
 
@@ -267,16 +295,29 @@ __device__ __forceinline__ void fft_stage(C (&x)[E], int t, const Lay& lay, cons
 #pragma unroll
     for (int r = 0; r < R; ++r) v[r] = x[q + r * Q];
     const int j = t + q * T;
-    if constexpr (NS > 1) {
+    if constexpr (std::is_same<C, double2>::value && NS > 1 && DIR < 0 && R > 1) {
+      // FP64 forward stage: twiddles fused into the first butterfly layer
       const int k = j & (NS - 1);
       constexpr int TS = N / (NS * R);
+      double2 w[R];
+      w[0] = make_double2(1.0, 0.0);
 #pragma unroll
-      for (int r = 1; r < R; ++r) {
-        const auto w = ldgc(tw + k * r * TS);
-        v[r] = (DIR < 0) ? twmul(v[r], w) : twmulc(v[r], w);
+      for (int r = 1; r < R; ++r) w[r] = ldgc(tw + k * r * TS);
+      fused_first_layer<R, DIR, R / 2, 0>(v, w);
+      dif_layers<R, DIR, R / 4>(v);
+      unscramble<R>(v);
+    } else {
+      if constexpr (NS > 1) {
+        const int k = j & (NS - 1);
+        constexpr int TS = N / (NS * R);
+#pragma unroll
+        for (int r = 1; r < R; ++r) {
+          const auto w = ldgc(tw + k * r * TS);
+          v[r] = (DIR < 0) ? twmul(v[r], w) : twmulc(v[r], w);
+        }
       }
+      dft_regs<R, DIR>(v);
     }
-    dft_regs<R, DIR>(v);
     if constexpr (LAST) {
 #pragma unroll
       for (int r = 0; r < R; ++r) x[q + r * Q] = v[r];

@@ -85,63 +85,30 @@ __device__ __forceinline__ uint32_t pack_bf16(float a, float b) {
 }
 
 // Stage an R x TBK tile of an FP32 operand, element (r, k) at G[r * sr + k * sk], into the
-// core-matrix layout as BF16 (zero outside r < rlim, k < klim).  mode 1: K contiguous
-// (sk = 1, rows 16-byte aligned): a thread loads 8 consecutive k of one row as two float4
-// and stores them as one 16-byte chunk.  mode 2: rows contiguous (sr = 1, columns 16-byte
-// aligned): a thread loads 4 rows x 8 k as eight float4 along the rows, transposes them in
-// registers and stores four 16-byte chunks.  mode 0 (any strides), and the chunks that
-// cross the matrix edge: one element at a time, consecutive threads along the contiguous
-// index.
+// core-matrix layout as BF16 (zero outside r < rlim, k < klim).  A thread takes 8
+// consecutive k of one row and writes them as one 16-byte chunk; consecutive threads take
+// consecutive rows, so eight of them fill one core matrix's 128 contiguous bytes (no bank
+// conflicts).  mode 1 (K contiguous, rows 16-byte aligned): the 8 values are two float4
+// loads.  Otherwise, and for the chunks that cross the matrix edge: 8 element loads, which
+// are coalesced across the warp when the rows are contiguous (sr = 1).
 template <int R>
 __device__ __forceinline__ void stage_tile(unsigned char* dst, const float* __restrict__ G, int64_t r0, int64_t k0,
                                            int64_t rlim, int64_t klim, int64_t sr, int64_t sk, int mode, int tid) {
-  if (mode == 1) {
-    for (int c = tid; c < R * (TBK / 8); c += TNTH) {
-      const int ri = c / (TBK / 8), ki = (c % (TBK / 8)) * 8;
-      const int64_t r = r0 + ri, k = k0 + ki;
-      uint4 q;
-      if (r < rlim && k + 7 < klim) {
-        const float4 a = __ldg(reinterpret_cast<const float4*>(G + r * sr + k));
-        const float4 b = __ldg(reinterpret_cast<const float4*>(G + r * sr + k + 4));
-        q = make_uint4(pack_bf16(a.x, a.y), pack_bf16(a.z, a.w), pack_bf16(b.x, b.y), pack_bf16(b.z, b.w));
-      } else {
-        float v[8];
+  for (int c = tid; c < R * (TBK / 8); c += TNTH) {
+    const int ri = c % R, ki = (c / R) * 8;
+    const int64_t r = r0 + ri, k = k0 + ki;
+    uint4 q;
+    if (mode == 1 && r < rlim && k + 7 < klim) {
+      const float4 a = __ldg(reinterpret_cast<const float4*>(G + r * sr + k));
+      const float4 b = __ldg(reinterpret_cast<const float4*>(G + r * sr + k + 4));
+      q = make_uint4(pack_bf16(a.x, a.y), pack_bf16(a.z, a.w), pack_bf16(b.x, b.y), pack_bf16(b.z, b.w));
+    } else {
+      float v[8];
 #pragma unroll
-        for (int j = 0; j < 8; ++j) v[j] = (r < rlim && k + j < klim) ? G[r * sr + (k + j) * sk] : 0.f;
-        q = make_uint4(pack_bf16(v[0], v[1]), pack_bf16(v[2], v[3]), pack_bf16(v[4], v[5]), pack_bf16(v[6], v[7]));
-      }
-      *reinterpret_cast<uint4*>(dst + core_off(ri, ki)) = q;
+      for (int j = 0; j < 8; ++j) v[j] = (r < rlim && k + j < klim) ? __ldg(G + r * sr + (k + j) * sk) : 0.f;
+      q = make_uint4(pack_bf16(v[0], v[1]), pack_bf16(v[2], v[3]), pack_bf16(v[4], v[5]), pack_bf16(v[6], v[7]));
     }
-  } else if (mode == 2) {
-    for (int c = tid; c < (R / 4) * (TBK / 8); c += TNTH) {
-      const int ri = (c % (R / 4)) * 4, ki = (c / (R / 4)) * 8;  // consecutive threads along the rows
-      const int64_t r = r0 + ri, k = k0 + ki;
-      float v[8][4];
-      if (r + 3 < rlim && k + 7 < klim) {
-#pragma unroll
-        for (int j = 0; j < 8; ++j) {
-          const float4 a = __ldg(reinterpret_cast<const float4*>(G + (k + j) * sk + r));
-          v[j][0] = a.x; v[j][1] = a.y; v[j][2] = a.z; v[j][3] = a.w;
-        }
-      } else {
-#pragma unroll
-        for (int j = 0; j < 8; ++j)
-#pragma unroll
-          for (int i = 0; i < 4; ++i) v[j][i] = (r + i < rlim && k + j < klim) ? G[(r + i) * sr + (k + j) * sk] : 0.f;
-      }
-#pragma unroll
-      for (int i = 0; i < 4; ++i)
-        *reinterpret_cast<uint4*>(dst + core_off(ri + i, ki)) =
-            make_uint4(pack_bf16(v[0][i], v[1][i]), pack_bf16(v[2][i], v[3][i]), pack_bf16(v[4][i], v[5][i]),
-                       pack_bf16(v[6][i], v[7][i]));
-    }
-  } else {
-    for (int e = tid; e < R * TBK; e += TNTH) {
-      const int ri = sr == 1 ? e % R : e / TBK, ki = sr == 1 ? e / R : e % TBK;
-      const int64_t r = r0 + ri, k = k0 + ki;
-      const float v = (r < rlim && k < klim) ? G[r * sr + k * sk] : 0.f;
-      *reinterpret_cast<__nv_bfloat16*>(dst + core_off(ri, ki)) = __float2bfloat16_rn(v);
-    }
+    *reinterpret_cast<uint4*>(dst + core_off(ri, ki)) = q;
   }
 }
 
@@ -409,12 +376,9 @@ int launch_gemm_tc(const gpe_gemm_desc* d, cudaStream_t s) {
       return GPE_ERR_CUDA;
     attr = true;
   }
-  // vectorised staging where an operand's rows or columns are contiguous and 16-byte aligned
+  // float4 staging loads where an operand's K index is contiguous and 16-byte aligned
   auto mode = [](const float* X, int64_t sr, int64_t sk, int64_t sz) {
-    const bool al = ((uintptr_t)X & 15) == 0 && sz % 4 == 0;
-    if (al && sk == 1 && sr % 4 == 0) return 1;
-    if (al && sr == 1 && sk % 4 == 0) return 2;
-    return 0;
+    return (((uintptr_t)X & 15) == 0 && sz % 4 == 0 && sk == 1 && sr % 4 == 0) ? 1 : 0;
   };
   const int vmode = mode(d->A, d->a_r, d->a_c, d->a_z) | (mode(d->B, d->b_c, d->b_r, d->b_z) << 2);
   gemm_tc_kernel<BN><<<grid, TNTH, TcSmem<BN>::BYTES, s>>>(*d, vmode);

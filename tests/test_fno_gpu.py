@@ -27,9 +27,9 @@ def bf16(x):
                                                      (512, 64, 64, False, False, 1, 0.0), (512, 64, 64, True, True, 2, 0.0)])
 @pytest.mark.parametrize("shift", [0, 1], ids=["aligned", "shifted"])
 def test_gemm_matches_numpy(gpe, lib, M, N, K, ta, tb, batch, beta, shift):
-    """Every stride pattern in both staging forms: 16-byte aligned operands whose rows or
-    columns are contiguous take the vectorised staging, operands shifted by one element
-    (not 16-byte aligned) the element-wise one."""
+    """Every stride pattern in both staging forms: 16-byte aligned operands whose K index
+    is contiguous are staged with float4 loads, the rest and operands shifted by one
+    element (not 16-byte aligned) element by element."""
     torch = pytest.importorskip("torch")
     F = fno_mod(gpe)
     rng = np.random.default_rng(M + N + K)
