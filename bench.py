@@ -278,6 +278,8 @@ def binding_limit(dtype, fp64: str) -> str:
 def arith_name(dtype, fp64: str) -> str:
     if dtype == np.complex64:
         return "f32"
+    if fp64 == "bfp":
+        return "f64 (line transforms in block floating point: 64-bit integers under one exponent a line)"
     return "f64" if fp64 == "native" else "f64-dw (double-word f32 pairs, 2^-48 unit roundoff)"
 
 
@@ -419,8 +421,15 @@ def run_gpu(args, rank, world, local_rank):
     P = N_GRID * N_GRID
     m = measure_fused(pkg, lib, L, args, dtype, args.fp64, B, local_rank, world, dist, with_e2e=True)
     value = m["value"]
-    dw = None
-    if dtype == np.complex128 and args.fp64 == "native" and not args.no_dw:
+    dw = fl = None
+    if dtype == np.complex128 and args.fp64 == "bfp" and not args.no_dw:
+        # FP64 floating point throughout (the reference's arithmetic, transforms included)
+        mfl = measure_fused(pkg, lib, L, args, dtype, "native", B, local_rank, world, dist, with_e2e=False)
+        fl = {"dtype": arith_name(dtype, "native"), "value": mfl["value"], "unit": "grid-point-steps/s",
+              "ms_per_step": mfl["ms_clean"] / args.steps, "gpu_launches": mfl["launches"],
+              "headline_speedup": value / mfl["value"], "roofline": roofline_of(mfl, dtype, "native", B),
+              "clocks": mfl["clocks"]}
+    if dtype == np.complex128 and args.fp64 in ("bfp", "native") and not args.no_dw:
         # the opt-in double-word mode on the same workload, reported beside the FP64 headline
         mdw = measure_fused(pkg, lib, L, args, dtype, "dw", B, local_rank, world, dist, with_e2e=False)
         dw = {"dtype": arith_name(dtype, "dw"), "value": mdw["value"], "unit": "grid-point-steps/s",
@@ -433,7 +442,8 @@ def run_gpu(args, rank, world, local_rank):
         if dtype == np.complex128 and rank == 0:
             plain["rel_l2_fused_vs_plain_f64"] = plain_vs_fused_rel_l2(pkg, local_rank, fp64=args.fp64)
             plain["rel_l2_case"] = (f"one pumped 512^2 field from u = 0, 200 steps, fused "
-                                    f"{'FP64' if args.fp64 == 'native' else 'double-word'} vs plain FP64")
+                                    f"{ {'bfp': 'FP64 (block floating point transforms)', 'native': 'FP64'}.get(args.fp64, 'double-word')} "
+                                    f"vs plain FP64")
 
     if rank != 0:
         return
@@ -451,6 +461,8 @@ def run_gpu(args, rank, world, local_rank):
         "roofline": roofline_of(m, dtype, args.fp64, B),
         "clocks": m["clocks"],
     }
+    if fl is not None:
+        line["fp64_float_transforms"] = fl
     if dw is not None:
         line["double_word"] = dw
     if plain is not None:
@@ -474,7 +486,8 @@ def run_polariton_solve(pkg, lib, device):
     of the stepping alone; FP64 (double-word) and FP32."""
     disp, nonl, pump = polariton_closures()
     out = []
-    for dtype, fp64 in ((np.complex128, "native"), (np.complex128, "dw"), (np.complex64, "native")):
+    for dtype, fp64 in ((np.complex128, "bfp"), (np.complex128, "native"), (np.complex128, "dw"),
+                        (np.complex64, "native")):
         z = np.zeros((N_GRID, N_GRID), dtype, order="F")
         prob = pkg.GrossPitaevskiiProblem((z, z.copy()), (L_BOX, L_BOX), dispersion=disp, nonlinearity=nonl,
                                           pump=pump)
@@ -486,7 +499,8 @@ def run_polariton_solve(pkg, lib, device):
         it.close()
         steps = 4000
         save_bytes = 100 * 2 * N_GRID * N_GRID * np.dtype(dtype).itemsize
-        out.append({"dtype": arith_name(dtype, fp64).split(" ")[0], "steps": steps, "saves": 100,
+        out.append({"dtype": {"bfp": "f64-bfp", "dw": "f64-dw"}.get(fp64, "f64") if dtype == np.complex128 else "f32",
+                    "steps": steps, "saves": 100,
                     "setup_s": t1 - t0, "solve_s": t2 - t1, "total_s": t2 - t0,
                     "point_steps_per_s": N_GRID * N_GRID * steps / (t2 - t1),
                     "saved_bytes": save_bytes, "result_shape": list(res[0].shape),
@@ -507,7 +521,7 @@ def run_kerr1024(pkg, lib, L, device, steps):
     base = np.exp(-((X - 16) ** 2 + (Y - 16) ** 2) / 4.0).astype(np.complex128)
     peak, _ = measured_peaks()
     out = []
-    for B, fp64 in ((1, "dw"), (16, "dw"), (16, "native")):
+    for B, fp64 in ((1, "dw"), (16, "dw"), (16, "native"), (16, "bfp")):
         u0 = np.asfortranarray(np.repeat(base[:, :, None], B, axis=2)) if B > 1 else np.asfortranarray(base)
         prob = pkg.GrossPitaevskiiProblem((u0,), (Lb, Lb), dispersion=lambda k, p: (k[0] ** 2 + k[1] ** 2) / 2,
                                           nonlinearity=lambda u, p: np.abs(u[0]) ** 2)
@@ -518,7 +532,7 @@ def run_kerr1024(pkg, lib, L, device, steps):
         it.close()
         v = N * N * B * steps / (ms * 1e-3)
         gbs = 80.0 * v / 1e9
-        out.append({"batch": B, "arith": "f64-dw" if fp64 == "dw" else "f64", "steps": steps,
+        out.append({"batch": B, "arith": {"dw": "f64-dw", "bfp": "f64-bfp"}.get(fp64, "f64"), "steps": steps,
                     "ms_per_step": ms / steps, "value": v, "unit": "grid-point-steps/s",
                     "algorithmic_gbs": gbs, "frac_of_hbm": gbs / peak,
                     "l2": "field L2-resident (16 MiB)" if B == 1 else "256 MiB of fields, streamed from HBM"})
@@ -929,9 +943,11 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--dtype", default="c128", choices=["c128", "c64"])
     ap.add_argument("--batch", type=int, default=0)
-    ap.add_argument("--fp64", default="native", choices=["native", "dw"],
-                    help="ComplexF64 arithmetic: native FP64 (default) or double-word on the FP32 pipes")
-    ap.add_argument("--no-dw", action="store_true", help="skip the double-word measurement beside the FP64 headline")
+    ap.add_argument("--fp64", default="bfp", choices=["bfp", "native", "dw"],
+                    help="ComplexF64 arithmetic: FP64 with block floating point line transforms (default), FP64 "
+                         "floating point throughout, or double-word on the FP32 pipes")
+    ap.add_argument("--no-dw", action="store_true",
+                    help="skip the FP64-floating-point and double-word measurements beside the FP64 headline")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--twa-steps", type=int, default=2000,
                     help="steps of the batched truncated-Wigner ensemble measurement (0 skips it)")

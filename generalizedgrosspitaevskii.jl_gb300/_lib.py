@@ -25,6 +25,7 @@ GPE_C128 = 0
 GPE_C64 = 1
 GPE_FLAG_FP64_NATIVE = 1
 GPE_FLAG_FP64_DW = 16
+GPE_FLAG_FFT_BFP = 32
 GPE_FLAG_NO_RESIDENT = 2
 GPE_FLAG_NO_TMA = 4
 GPE_FLAG_TMA = 8

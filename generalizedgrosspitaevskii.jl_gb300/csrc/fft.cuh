@@ -96,6 +96,79 @@ __device__ __forceinline__ float2 twmul(float2 v, dwc w) { return cmul_hl(v, w);
 __device__ __forceinline__ float2 twmulc(float2 v, dwc w) { return cmulc_hl(v, w); }
 template <typename C> __device__ __forceinline__ C cmake(double x, double y) { C r; r.x = x; r.y = y; return r; }
 
+// ---------------------------------------------------------------- block floating point
+// FP64 lines can be transformed on the integer pipes: GB300 runs two FP64 operations a
+// clock per SM, but 64-bit integer adds at 32 and 32x32->64 multiply-adds fast enough
+// for a complex product in Q62 fixed point at 2.7x the FP64 rate (both measured on the
+// GB300).  A line is held as 64-bit integers with one exponent for the whole line
+// (block floating point, the scheme of Oppenheim & Weinstein, "Effects of finite
+// register length in digital filtering and the fast Fourier transform", Proc. IEEE
+// 60(8), 1972): the input is scaled so that its largest component is just below 2^58,
+// each radix-8 stage grows the largest component by at most 8 sqrt(2) (below 2^62), and
+// at each exchange every value of the line is shifted right by the bits its largest
+// component grew beyond 2^58 (rounded), so every stage again starts below 2^58.  Sums are
+// exact; each product with a twiddle or an internal constant rounds to within one unit
+// (2^-58 of the line's largest component), where an FP64 transform rounds every sum and
+// product to 2^-53 of its own value.
+struct __align__(16) fxc { long long x, y; };
+// Q62 constant c + i s, each as hi * 2^32 + lo with lo signed (so that products of its
+// halves are signed 32 x 32 -> 64 multiply-adds)
+struct __align__(16) fxw { int ch, cl, sh, sl; };
+template <> struct TwT<fxc> { using T = fxw; };
+__device__ __forceinline__ fxw ldgc(const fxw* p) {
+  const int4 v = __ldg(reinterpret_cast<const int4*>(p));
+  fxw w;
+  w.ch = v.x; w.cl = v.y; w.sh = v.z; w.sl = v.w;
+  return w;
+}
+
+// v << 2 (|v| < 2^61) as h * 2^32 + l, l signed
+__device__ __forceinline__ void fx_split(long long v, int& h, int& l) {
+  const long long s = v << 2;
+  l = (int)(unsigned)s;
+  h = (int)((s - (long long)l) >> 32);
+}
+// v * (c + i s) for Q62 c, s and components |v| < 2^60: (4v)(c + i s) / 2^64 from the
+// 32-bit halves.  The middle partial products (with a rounding half unit) are summed
+// first and shifted down, the low-by-low ones (below 1/8 unit) are dropped: the result is
+// within 0.9 units of the exact product and unbiased.
+__device__ __forceinline__ fxc fx_cmul(fxc v, int ch, int cl, int sh, int sl) {
+  int rh, rl, ih, il;
+  fx_split(v.x, rh, rl);
+  fx_split(v.y, ih, il);
+  long long tr = (long long)rh * cl + (1LL << 31);
+  tr = (long long)rl * ch + tr;
+  tr = (long long)(-ih) * sl + tr;
+  tr = (long long)il * (-sh) + tr;  // il may be -2^31; |sh| <= 2^30
+  long long ti = (long long)rh * sl + (1LL << 31);
+  ti = (long long)rl * sh + ti;
+  ti = (long long)ih * cl + ti;
+  ti = (long long)il * ch + ti;
+  fxc r;
+  r.x = (long long)rh * ch + ((long long)(-ih) * sh + (tr >> 32));
+  r.y = (long long)rh * sh + ((long long)ih * ch + (ti >> 32));
+  return r;
+}
+__device__ __forceinline__ fxc twmul(fxc v, fxw w) { return fx_cmul(v, w.ch, w.cl, w.sh, w.sl); }
+// the table's lo halves are never -2^31 (see the table builder), so -s splits as (-sh, -sl)
+__device__ __forceinline__ fxc twmulc(fxc v, fxw w) { return fx_cmul(v, w.ch, w.cl, -w.sh, -w.sl); }
+
+// Q62 of cos(2 pi k / 16), exactly rounded
+__host__ __device__ constexpr long long q62_cos16(int k) {
+  k &= 15;
+  return k == 0 ? 4611686018427387904LL
+       : k == 1 || k == 15 ? 4260642322793532497LL
+       : k == 2 || k == 14 ? 3260954456333195553LL
+       : k == 3 || k == 13 ? 1764815834521887442LL
+       : k == 4 || k == 12 ? 0LL
+       : k == 5 || k == 11 ? -1764815834521887442LL
+       : k == 6 || k == 10 ? -3260954456333195553LL
+       : k == 7 || k == 9 ? -4260642322793532497LL
+       : -4611686018427387904LL;
+}
+__host__ __device__ constexpr int q62_lo(long long v) { return (int)(unsigned)(unsigned long long)v; }
+__host__ __device__ constexpr int q62_hi(long long v) { return (int)((v - (long long)q62_lo(v)) >> 32); }
+
 // cos(2 pi k / 16), k in [0, 16): exact constants of the regular 16-gon.
 __host__ __device__ constexpr double cos16(int k) {
   k &= 15;
@@ -122,7 +195,20 @@ __host__ __device__ constexpr int bitrev(int v, int bits) {
 template <int DIR, int n, int i, typename C>
 __device__ __forceinline__ C twc(C d) {
   constexpr int k = (i * 16 / n) & 15;
-  if constexpr (std::is_same<C, dwc>::value) {
+  if constexpr (std::is_same<C, fxc>::value) {
+    if constexpr (k == 0) {
+      return d;
+    } else if constexpr (k == 4) {  // w = DIR * i
+      fxc r; r.x = DIR < 0 ? d.y : -d.y; r.y = DIR < 0 ? -d.x : d.x; return r;
+    } else if constexpr (k == 8) {
+      fxc r; r.x = -d.x; r.y = -d.y; return r;
+    } else if constexpr (k == 12) {  // w = -DIR * i
+      fxc r; r.x = DIR < 0 ? -d.y : d.y; r.y = DIR < 0 ? d.x : -d.x; return r;
+    } else {
+      constexpr long long c = q62_cos16(k), s = DIR * q62_cos16(k - 4);
+      return fx_cmul(d, q62_hi(c), q62_lo(c), q62_hi(s), q62_lo(s));
+    }
+  } else if constexpr (std::is_same<C, dwc>::value) {
     if constexpr (k == 0) {
       return d;
     } else if constexpr (k == 4) {  // w = DIR * i: (x, y) -> (-DIR y, DIR x)
@@ -258,6 +344,7 @@ __device__ __forceinline__ void fused_first_layer(double2 (&v)[R], const double2
 // the strided reads of the next stage are free of bank conflicts.
 template <typename C>
 struct RowLayout {
+  template <typename D> using rebind = RowLayout<D>;
   C* base;
   static constexpr int S = 128 / (int)sizeof(C);  // complex slots per 128-byte row
   static constexpr int LOGS = ilog2(S);
@@ -279,6 +366,7 @@ struct RowLayout {
 // times over; 16-byte elements fill all 32 banks either way).
 template <typename C, int CC>
 struct ColLayout {
+  template <typename D> using rebind = ColLayout<D, CC>;
   static constexpr bool PAD = sizeof(C) == 8;
   C* base;  // already offset by the column index
   template <int NS, int R>
@@ -286,8 +374,17 @@ struct ColLayout {
 };
 
 // One Stockham stage.  x: this thread's E points; t: thread index in the line.
+// Block floating point: the high word of |v| (one's complement for negative v) for the
+// bit length of a line's largest component.  Lines are scaled so that their largest
+// component exceeds 2^53, so the high words decide it.
+__device__ __forceinline__ unsigned fx_mag(fxc v) {
+  const int hx = (int)(v.x >> 32), hy = (int)(v.y >> 32);
+  return (unsigned)(hx ^ (hx >> 31)) | (unsigned)(hy ^ (hy >> 31));
+}
+
 template <typename C, int N, int E, int R, int NS, int DIR, bool LAST, class Lay>
-__device__ __forceinline__ void fft_stage(C (&x)[E], int t, const Lay& lay, const typename TwT<C>::T* __restrict__ tw) {
+__device__ __forceinline__ void fft_stage(C (&x)[E], int t, const Lay& lay, const typename TwT<C>::T* __restrict__ tw,
+                                          unsigned* mag = nullptr) {
   constexpr int T = N / E, Q = E / R;
 #pragma unroll
   for (int q = 0; q < Q; ++q) {
@@ -325,6 +422,10 @@ __device__ __forceinline__ void fft_stage(C (&x)[E], int t, const Lay& lay, cons
       const int jb = (j / NS) * NS * R + (j & (NS - 1));
 #pragma unroll
       for (int r = 0; r < R; ++r) lay.base[lay.template addr<NS, R>(jb + r * NS)] = v[r];
+      if constexpr (std::is_same<C, fxc>::value) {
+#pragma unroll
+        for (int r = 0; r < R; ++r) *mag |= fx_mag(v[r]);
+      }
     }
   }
 }
@@ -433,6 +534,161 @@ __device__ __forceinline__ void fft_line_joint(C (&x)[M][E], int t, const Lay& l
   for (int m = 0; m < M; ++m)
 #pragma unroll
     for (int i = 0; i < E; ++i) x[m][i] = bfinish(x[m][i]);
+}
+
+
+// ---------------------------------------------------------------- block floating point lines
+constexpr int FX_TOP = 58;  // a stage's input components stay below 2^FX_TOP
+
+// Maximum over the threads of a line.  The threads of a line are those with equal
+// threadIdx.x % G and equal threadIdx.x / (G * T): row lines (G = 1) are T consecutive
+// threads, the G columns of a column tile interleave.  Lines inside one warp reduce with
+// shuffles.  Wider lines publish one value a warp and column (G < 32), or one a thread
+// (G >= 32, where a warp holds one thread of each of 32 lines), in red and read their
+// line's values back after the caller's barrier.  Blocks narrower than a warp (a few
+// short lines) shuffle under the mask of the threads they have.
+template <int G, int T>
+struct LineMax {
+  static constexpr int W = G * T;
+  static constexpr bool MULTI = W > 32;
+  static constexpr int RED = G < 32 ? 32 * G : W;  // slots of red
+  __device__ __forceinline__ static int warp(int v) {
+    const unsigned mask = blockDim.x >= 32 ? 0xffffffffu : (1u << blockDim.x) - 1u;
+#pragma unroll
+    for (int off = G; off < (W < 32 ? W : 32); off *= 2) v = max(v, __shfl_xor_sync(mask, v, off));
+    return v;
+  }
+  __device__ __forceinline__ static void publish(int v, int* red) {
+    if constexpr (MULTI) {
+      if constexpr (G < 32) {
+        const int lane = threadIdx.x & 31;
+        if (lane < G) red[(threadIdx.x >> 5) * G + lane] = v;
+      } else {
+        red[threadIdx.x % W] = v;
+      }
+    }
+  }
+  __device__ __forceinline__ static int collect(int v, const int* red) {
+    if constexpr (MULTI) {
+      const int c = threadIdx.x % G;
+      if constexpr (G < 32) {
+        const int w0 = (int)(threadIdx.x / W) * (W / 32);
+        int r = red[w0 * G + c];
+#pragma unroll
+        for (int w = 1; w < W / 32; ++w) r = max(r, red[(w0 + w) * G + c]);
+        return r;
+      } else {
+        int r = red[c];
+#pragma unroll
+        for (int j = 1; j < T; ++j) r = max(r, red[c + G * j]);
+        return r;
+      }
+    } else {
+      return v;
+    }
+  }
+};
+
+// round(v * 2^(FX_TOP + 1022 - emax)) for a component v of a line whose largest biased
+// exponent is emax (so |v| < 2^(emax - 1022) maps below 2^FX_TOP); zero and subnormals
+// (below 2^-1022) give 0.  Integer operations only.
+__device__ __forceinline__ long long fx_from_double(double v, int emax) {
+  const long long b = __double_as_longlong(v);
+  const int e = (int)((b >> 52) & 0x7ff);
+  const long long m = (b & 0xfffffffffffffLL) | 0x10000000000000LL;
+  // v = m 2^(e - 1075): shift right by emax - e + 53 - FX_TOP (at least -5)
+  const int sh = emax - e + (53 - FX_TOP);
+  long long r;
+  if (sh <= 0) r = m << (-sh);
+  else r = sh < 64 ? (m + (1LL << (sh - 1))) >> sh : 0;
+  if (e == 0) r = 0;
+  return b < 0 ? -r : r;
+}
+// r * 2^eb rounded to the nearest double (ties away from zero), integer operations only;
+// results below the normal range are flushed to zero
+__device__ __forceinline__ double fx_to_double(long long r, int eb) {
+  const unsigned long long a = r < 0 ? 0ull - (unsigned long long)r : (unsigned long long)r;
+  const int lz = __clzll((long long)a);
+  const unsigned long long n = a << (lz & 63);
+  const unsigned long long mant = ((n >> 10) + 1) >> 1;  // 53 bits, 2^53 when rounding carries
+  // a = mant 2^(11 - lz): biased exponent 1086 - lz + eb; mant's leading bit adds one
+  const int E = 1086 - lz + eb;
+  unsigned long long bits = ((unsigned long long)(E - 1) << 52) + mant;
+  if (a == 0 || E <= 0) bits = 0;
+  if (E >= 2047) bits = 0x7ff0000000000000ull;
+  return __longlong_as_double((long long)(bits | ((unsigned long long)r & 0x8000000000000000ull)));
+}
+
+// Stockham stages on block floating point values: after every stage but the last the
+// line's largest component (bit length from the high words of what each thread wrote) is
+// reduced over the line across the exchange barrier, and the values read back are shifted
+// right by its excess over FX_TOP, rounded; shsum collects the shifts.
+template <int N, int E, int NS, class Lay, class LM>
+__device__ __forceinline__ void fx_stages(fxc (&x)[E], int t, const Lay& lay, const fxw* __restrict__ tw, int* red,
+                                          int& shsum) {
+  static_assert(E <= 8, "radix-16 stages would exceed the 63-bit headroom");
+  constexpr int REM = N / NS;
+  constexpr int R = REM >= E ? E : REM;
+  constexpr bool LAST = (NS * R == N);
+  constexpr int T = N / E;
+  unsigned mag = 0;
+  fft_stage<fxc, N, E, R, NS, -1, LAST>(x, t, lay, tw, &mag);
+  if constexpr (!LAST) {
+    const int lw = LM::warp(mag ? 64 - __clz((int)mag) : 32);
+    LM::publish(lw, red);
+    __syncthreads();
+#pragma unroll
+    for (int i = 0; i < E; ++i) x[i] = lay.base[lay.template addr<NS, R>(t + T * i)];
+    const int sh = max(0, LM::collect(lw, red) - FX_TOP);
+    if (sh > 0) {
+      const long long half = 1LL << (sh - 1);
+#pragma unroll
+      for (int i = 0; i < E; ++i) {
+        x[i].x = (x[i].x + half) >> sh;
+        x[i].y = (x[i].y + half) >> sh;
+      }
+    }
+    shsum += sh;
+    __syncthreads();
+    fx_stages<N, E, NS * R, Lay, LM>(x, t, lay, tw, red, shsum);
+  }
+}
+
+// Forward (unnormalised) transform of one line of FP64 values in block floating point;
+// lay: the line's exchange space viewed as fxc, tw: the Q62 twiddle table.  A line holding
+// an infinity or NaN comes out as NaN.  Every thread of the block calls this the same number
+// of times (it holds barriers); N > E.
+template <int N, int E, int G, class Lay>
+__device__ __forceinline__ void fx_line(double2 (&x)[E], int t, const Lay& lay, const fxw* __restrict__ tw) {
+  static_assert(N > E, "one-stage lines have no exchange to reduce across");
+  using LM = LineMax<G, N / E>;
+  __shared__ int red_in[LM::RED], red_x[LM::RED];
+  // largest biased exponent of the line (from the high words, integer compares)
+  unsigned hm = 0;
+#pragma unroll
+  for (int i = 0; i < E; ++i) {
+    hm = max(hm, (unsigned)__double2hiint(x[i].x) & 0x7fffffffu);
+    hm = max(hm, (unsigned)__double2hiint(x[i].y) & 0x7fffffffu);
+  }
+  int em = LM::warp((int)(hm >> 20));
+  LM::publish(em, red_in);
+  if constexpr (LM::MULTI) __syncthreads();
+  em = LM::collect(em, red_in);
+  fxc v[E];
+#pragma unroll
+  for (int i = 0; i < E; ++i) {
+    v[i].x = fx_from_double(x[i].x, em);
+    v[i].y = fx_from_double(x[i].y, em);
+  }
+  int shsum = 0;
+  fx_stages<N, E, 1, Lay, LM>(v, t, lay, tw, red_x, shsum);
+  const int eb = em - 1022 - FX_TOP + shsum;
+  const bool bad = em == 0x7ff;
+#pragma unroll
+  for (int i = 0; i < E; ++i) {
+    x[i].x = bad ? __longlong_as_double(0x7ff8000000000000LL) : fx_to_double(v[i].x, eb);
+    x[i].y = bad ? __longlong_as_double(0x7ff8000000000000LL) : fx_to_double(v[i].y, eb);
+  }
 }
 
 }  // namespace gpe

@@ -15,6 +15,7 @@
 #include <cmath>
 #include <complex>
 #include <cstdarg>
+#include <cstdint>
 #include <cstdio>
 #include <cstring>
 #include <string>
@@ -246,8 +247,19 @@ static int upload_complex(gpe_handle* h, void** dst, const cd* src, size_t n) {
 // Upload n complex FP64 table entries (exp(-i dt D), exp(-i dt/2 V)) at FP64 accuracy in
 // every pass precision: double2 for FP64 passes, {re.hi, re.lo, im.hi, im.lo} floats for
 // the double-word and FP32 passes (16 bytes an entry either way).
-static int upload_table(gpe_handle* h, void** dst, const cd* src, size_t n) {
-  if (!*dst) CK(h, cudaMalloc(dst, n * 16));
+// Q62 of v (|v| <= 1) as {hi, lo} with v 2^62 = hi 2^32 + lo and lo signed; a lo of -2^31
+// (whose negation would overflow) moves the value by one unit, 2^-62
+static void q62_split(long double v, int32_t out[2]) {
+  long long q = std::llround(std::ldexp(v, 62));
+  if ((int32_t)(uint32_t)(unsigned long long)q == INT32_MIN) q += 1;
+  const int32_t lo = (int32_t)(uint32_t)(unsigned long long)q;
+  out[0] = (int32_t)((q - (long long)lo) >> 32);
+  out[1] = lo;
+}
+// Upload n complex FP64 entries (double2 for FP64 passes, hi/lo float pairs otherwise),
+// with room for `extra` further 16-byte entries after them.
+static int upload_table(gpe_handle* h, void** dst, const cd* src, size_t n, size_t extra = 0) {
+  if (!*dst) CK(h, cudaMalloc(dst, (n + extra) * 16));
   if (h->prec == gpe::PREC_F64) {
     CK(h, cudaMemcpy(*dst, src, n * 16, cudaMemcpyHostToDevice));
   } else {
@@ -366,6 +378,10 @@ int gpe_create(const gpe_desc* desc, gpe_handle** out) {
     return fail(nullptr, GPE_ERR_INVALID, "GPE_FLAG_FP64_DW and GPE_FLAG_FP64_NATIVE exclude each other");
   if ((desc->flags & GPE_FLAG_FP64_DW) && desc->dtype != GPE_C128)
     return fail(nullptr, GPE_ERR_INVALID, "GPE_FLAG_FP64_DW applies to GPE_C128 fields only");
+  if ((desc->flags & GPE_FLAG_FFT_BFP) && (desc->flags & (GPE_FLAG_FP64_DW | GPE_FLAG_FP64_NATIVE)))
+    return fail(nullptr, GPE_ERR_INVALID, "GPE_FLAG_FFT_BFP, GPE_FLAG_FP64_NATIVE and GPE_FLAG_FP64_DW exclude each other");
+  if ((desc->flags & (GPE_FLAG_FFT_BFP | GPE_FLAG_FP64_NATIVE)) && desc->dtype != GPE_C128)
+    return fail(nullptr, GPE_ERR_INVALID, "GPE_FLAG_FFT_BFP and GPE_FLAG_FP64_NATIVE apply to GPE_C128 fields only");
   if (!(desc->dt > 0) || !std::isfinite(desc->dt)) return fail(nullptr, GPE_ERR_INVALID, "dt must be positive and finite");
   if (!std::isfinite(desc->t0)) return fail(nullptr, GPE_ERR_INVALID, "t0 must be finite");
   for (int a = 0; a < desc->ndim; ++a) {
@@ -435,8 +451,18 @@ int gpe_create(const gpe_desc* desc, gpe_handle** out) {
       const double th = -2.0 * M_PI * (double)k / (double)N;
       w[(size_t)k] = cd(std::cos(th), std::sin(th));
     }
-    int rc = upload_table(h, &h->tw[a], w.data(), (size_t)N);  // FP32 passes: hi/lo pairs
+    int rc = upload_table(h, &h->tw[a], w.data(), (size_t)N, h->prec == gpe::PREC_F64 ? (size_t)N : 0);
     if (rc) { g_create_error = h->err; return bail(rc); }
+    if (h->prec == gpe::PREC_F64) {
+      // Q62 twiddles of the block floating point transforms after the FP64 ones
+      std::vector<int32_t> q(4 * (size_t)N);
+      for (int64_t k = 0; k < N; ++k) {
+        const long double th = -2.0L * 3.141592653589793238462643383279502884L * (long double)k / (long double)N;
+        q62_split(std::cos(th), &q[4 * (size_t)k]);
+        q62_split(std::sin(th), &q[4 * (size_t)k + 2]);
+      }
+      CK(h, cudaMemcpy((char*)h->tw[a] + 16 * (size_t)N, q.data(), 16 * (size_t)N, cudaMemcpyHostToDevice));
+    }
   }
   cudaDeviceSynchronize();
   *out = h;
@@ -857,6 +883,7 @@ static PassArgs base_args(gpe_handle* h) {
   a.B = h->B;
   a.nsm = h->nsm;
   a.col_tma = (h->d.flags & GPE_FLAG_NO_TMA) ? 0 : (h->d.flags & GPE_FLAG_TMA) ? 1 : 2;
+  a.fx = (h->prec == gpe::PREC_F64 && !(h->d.flags & GPE_FLAG_FP64_NATIVE)) ? 1 : 0;
   a.status = h->dstat;
   for (int m = 0; m < h->M; ++m) a.u[m] = h->u[m];
   a.ktab = h->ktab;
@@ -879,6 +906,7 @@ static PassArgs base_args(gpe_handle* h) {
     for (int l = 0; l < 2; ++l)
       for (int r = 0; r < 2; ++r) {
         a.g[j][l][r] = h->g[j][l][r];
+        a.gd[j][l][r] = 0.5 * h->d.dt * h->g[j][l][r];
         split_dw(h->g[j][l][r], hl);
         a.gf[j][l][r] = hl[0];
         a.gl[j][l][r] = hl[1];
@@ -886,6 +914,8 @@ static PassArgs base_args(gpe_handle* h) {
       }
     for (int r = 0; r < 2; ++r) {
       a.c[j][r] = h->c[j][r];
+      a.cd[j][r] = 0.5 * h->d.dt * h->c[j][r];
+      if (h->c[j][r] != 0.0) a.c_nz |= 1 << (j * 2 + r);
       split_dw(h->c[j][r], hl);
       a.cf[j][r] = hl[0];
       a.cl[j][r] = hl[1];

@@ -38,6 +38,11 @@ struct PassArgs {
   int32_t g_nz;       // bit j*4 + l*2 + r: g[j][l][r] != 0 (tested on the integer pipe)
   double g[2][2][2];
   double c[2][2];
+  // the same times dt/2 (FP64 passes form the phase dt/2 G with one FMA a term) and the
+  // nonzero c terms, bit j*2 + r
+  double gd[2][2][2];
+  double cd[2][2];
+  int32_t c_nz;
   float gf[2][2][2], gl[2][2][2];
   float cf[2][2], cl[2][2];
   // matrix nonlinearity (M = 2), null when off: 24 doubles on the device, g[a][b][l] (re, im)
@@ -78,6 +83,9 @@ struct PassArgs {
   // TMA staging of 2D column tiles: 0 never, 1 wherever the shape and shared memory
   // allow, 2 by the measured rule (one-component lines of at most 512 points)
   int32_t col_tma;
+  // FP64 line transforms of the row and column passes in block floating point on the
+  // integer pipes (Q62 twiddles after the FP64 ones in the table)
+  int32_t fx;
   // host-mapped status word: a device wait that ran out of time stores 1 here
   int32_t* status;
 };

@@ -109,22 +109,16 @@ struct LineCfg {
 // ------------------------------------------------------------------ scalar helpers
 template <typename Real> __device__ __forceinline__ void sc(Real x, Real* s, Real* c);
 // FP64 sin/cos of the nonlinear phase.  FP64 runs at 1/64 of the FP32 rate on GB300, so
-// small angles (the usual case: |dt/2 * G| << 1) use Taylor series of sin and cos with as
-// many terms as FP64 needs on their interval: for |x| < 2^-6 through x^7 / x^6 (the first
-// dropped terms, x^9/9! and x^8/8!, are below 1e-19 of the result), for |x| < 1/8 through
-// x^9 / x^10 (below 3e-17 relative and 3e-20), about a third and a half of the cost of
-// the general routine, which handles the rest.  The interval is picked from the high word
-// of x on the integer pipe, leaving the FP64 pipe to the arithmetic.
+// small angles (the usual case: |dt/2 * G| << 1) use the Taylor series through x^9 / x^10
+// for |x| < 1/8 (the first dropped terms below 3e-17 relative and 3e-20): 12 FP64
+// operations, a fraction of the general routine, which handles the rest.  The interval is
+// picked from the high word of x on the integer pipe.  One polynomial, not a ladder of
+// shorter ones: the compiler evaluates the rungs of a ladder both and selects.
 template <> __device__ __forceinline__ void sc<double>(double x, double* s, double* c) {
-  const int hx = __double2hiint(x) & 0x7fffffff;  // |x| < 2^-6 iff hx < 0x3f900000, < 1/8 iff < 0x3fc00000
-  if (hx < 0x3f900000) {
+  if ((__double2hiint(x) & 0x7fffffff) < 0x3fc00000) {  // |x| < 1/8
     const double x2 = x * x;
-    *c = 1.0 + x2 * (-1.0 / 2 + x2 * (1.0 / 24 + x2 * (-1.0 / 720)));
-    *s = x * (1.0 + x2 * (-1.0 / 6 + x2 * (1.0 / 120 + x2 * (-1.0 / 5040))));
-  } else if (hx < 0x3fc00000) {
-    const double x2 = x * x;
-    *c = 1.0 + x2 * (-1.0 / 2 + x2 * (1.0 / 24 + x2 * (-1.0 / 720 + x2 * (1.0 / 40320 + x2 * (-1.0 / 3628800)))));
-    *s = x * (1.0 + x2 * (-1.0 / 6 + x2 * (1.0 / 120 + x2 * (-1.0 / 5040 + x2 * (1.0 / 362880)))));
+    *c = fma(x2, fma(x2, fma(x2, fma(x2, fma(x2, -1.0 / 3628800, 1.0 / 40320), -1.0 / 720), 1.0 / 24), -0.5), 1.0);
+    *s = x * fma(x2, fma(x2, fma(x2, fma(x2, 1.0 / 362880, -1.0 / 5040), 1.0 / 120), -1.0 / 6), 1.0);
   } else {
     sincos(x, s, c);
   }
@@ -236,6 +230,18 @@ __device__ __forceinline__ double rpart(const double2& z) { return z.x; }
 __device__ __forceinline__ dw rpart(const dwc& z) { return re(z); }
 template <typename C> __device__ __forceinline__ C pump_mul(const C& coef, const C& prof, int cplx) {
   return cplx ? cmul(coef, prof) : cscale(coef, rpart(prof));
+}
+// u + coef * prof.  FP64: one complex multiply-add whatever the profile (a real profile is
+// loaded with a zero imaginary part), four FMAs; choosing between the real and complex
+// forms at run time makes the compiler evaluate both and select.
+template <typename C> __device__ __forceinline__ C pump_add(const C& u, const C& coef, const C& prof, int cplx) {
+  return cadd(u, pump_mul(coef, prof, cplx));
+}
+__device__ __forceinline__ double2 pump_add(const double2& u, const double2& coef, const double2& prof, int) {
+  double2 r;
+  r.x = fma(coef.x, prof.x, fma(-coef.y, prof.y, u.x));
+  r.y = fma(coef.y, prof.x, fma(coef.x, prof.y, u.y));
+  return r;
 }
 
 // complex normal deviate in the pass precision
@@ -474,7 +480,7 @@ __device__ __forceinline__ void half_step(typename CT<Real>::T (&u)[M], const Pa
     }
   } else {
     using K = Coef<Real>;
-    const Real dth = K::dth(a);
+    [[maybe_unused]] const Real dth = K::dth(a);
     // only the densities some active G_j uses, and only the nonzero coefficients (uniform
     // branches on host-made bit masks, so no FP64 compare; adding a zero term would not
     // change the sum): the polariton's G_2 = g |u_2|^2 costs one density and one product
@@ -486,6 +492,27 @@ __device__ __forceinline__ void half_step(typename CT<Real>::T (&u)[M], const Pa
     for (int j = 0; j < M; ++j) {
       hasE[j] = a.nl_on[j] != 0;
       if (hasE[j]) {
+        if constexpr (std::is_same<Real, double>::value) {
+          // the phase dt/2 G from the dt/2-scaled coefficients, one FMA a nonzero term
+          double pr = ((a.c_nz >> (j * 2)) & 1) ? a.cd[j][0] : 0.0;
+          double pi = ((a.c_nz >> (j * 2 + 1)) & 1) ? a.cd[j][1] : 0.0;
+#pragma unroll
+          for (int l = 0; l < M; ++l) {
+            if ((a.g_nz >> (j * 4 + l * 2)) & 1) pr = fma(a.gd[j][l][0], dens[l], pr);
+            if ((a.g_nz >> (j * 4 + l * 2 + 1)) & 1) pi = fma(a.gd[j][l][1], dens[l], pi);
+          }
+          double s, c;
+          sc<double>(pr, &s, &c);
+          if (a.nl_imag[j]) {
+            const double mag = exp(pi);
+            E[j].x = mag * c;
+            E[j].y = -mag * s;
+          } else {
+            E[j].x = c;
+            E[j].y = -s;
+          }
+          continue;
+        }
         Real gr = K::c(a, j, 0), gi = K::c(a, j, 1);
 #pragma unroll
         for (int l = 0; l < M; ++l) {
@@ -549,7 +576,7 @@ __device__ __forceinline__ void half_step(typename CT<Real>::T (&u)[M], const Pa
     if (a.pprof[j]) {
       prof[j] = ((a.pump_uniform >> j) & 1) ? cunit<C>()
                 : a.pprof_cplx ? ldgc((const C*)a.pprof[j] + p) : Prof<Real>::cplx(a.pprof[j], p);
-      if (!pm[j]) u[j] = cadd(u[j], pump_mul(pn[j], prof[j], a.pprof_cplx));
+      if (!pm[j]) u[j] = pump_add(u[j], pn[j], prof[j], a.pprof_cplx);
     }
   }
   if (a.vkind == TAB_MATRIX && M == 2) {
@@ -585,7 +612,7 @@ __device__ __forceinline__ void half_step(typename CT<Real>::T (&u)[M], const Pa
   }
 #pragma unroll
   for (int j = 0; j < M; ++j)
-    if (a.pprof[j]) u[j] = cadd(u[j], pump_mul(px[j], prof[j], a.pprof_cplx));  // px: pn + px when merged
+    if (a.pprof[j]) u[j] = pump_add(u[j], px[j], prof[j], a.pprof_cplx);  // px: pn + px when merged
   if (a.noise != NOISE_OFF) {
     C xi[M];
     if (xi_pre) {
@@ -686,9 +713,13 @@ __device__ __forceinline__ void swap_all(C (&x)[E]) {
 // Transform every component's line in place: forward (unnormalised) or inverse (the
 // 1/P is folded into the k-space table).  One FFT instance serves all components and
 // both directions: component 1 is swapped into the slot of component 0 and back.
-template <typename C, int N, int E, int M, class Lay, bool JOINT = false>
+// FXG > 0: FP64 lines may take the block floating point transform (fx_line; runtime switch
+// fx), the threads of a line being spread with stride FXG (1 for row lines, the column
+// count for column tiles); the Q62 twiddles follow the N FP64 ones in the table.
+template <typename C, int N, int E, int M, class Lay, bool JOINT = false, int FXG = 0>
 __device__ __forceinline__ void fft_components(C (&x)[M][E], bool inverse, int t, const Lay& lay,
-                                               const typename TwT<C>::T* __restrict__ tw, int cstride = 0, bool renorm = true) {
+                                               const typename TwT<C>::T* __restrict__ tw, int cstride = 0, bool renorm = true,
+                                               bool fx = false) {
   if constexpr (JOINT) {
     // all components in one pass (FP32: the twiddle loads and barriers are shared)
     if (inverse) {
@@ -704,7 +735,16 @@ __device__ __forceinline__ void fft_components(C (&x)[M][E], bool inverse, int t
 #pragma unroll 1
     for (int m = 0; m < M; ++m) {
       if (inverse) swap_all(x[0]);
-      fft_line<C, N, E, -1>(x[0], t, lay, tw, renorm);
+      if constexpr (std::is_same<C, double2>::value && FXG > 0 && N > E) {
+        if (fx) {
+          using LF = typename Lay::template rebind<fxc>;
+          fx_line<N, E, FXG>(x[0], t, LF{reinterpret_cast<fxc*>(lay.base)}, reinterpret_cast<const fxw*>(tw + N));
+        } else {
+          fft_line<C, N, E, -1>(x[0], t, lay, tw, renorm);
+        }
+      } else {
+        fft_line<C, N, E, -1>(x[0], t, lay, tw, renorm);
+      }
       if (inverse) swap_all(x[0]);
       if constexpr (M == 2) {
 #pragma unroll
@@ -838,7 +878,8 @@ row_kernel(const PassArgs a, const int64_t nlines, const int lb) {
         // the inverse transform's values go straight into the half steps' double-word
         // products and sums: no closing renormalisation, unless the pass ends without the
         // forward transform (then they may be stored as they are)
-        fft_components<C, N, E, M, RowLayout<C>, Cfg::JOINT>(x, ph == 0, t, lay, tw, lb * N, ph != 0 || !a.do_fft);
+        fft_components<C, N, E, M, RowLayout<C>, Cfg::JOINT, 1>(x, ph == 0, t, lay, tw, lb * N, ph != 0 || !a.do_fft,
+                                                                a.fx != 0);
       continue;
     }
     const int64_t hr = ph == 2 ? a.hB : a.hA;
@@ -876,8 +917,8 @@ __device__ __forceinline__ void col_tile_work(typename CT<Real>::T (&x)[M][LineC
     if (ph != 1) {
       if (ph == 0 ? a.col_fwd : a.col_inv)
         // the forward transform's values go straight into the table's complex products
-        fft_components<C, N, E, M, ColLayout<C, CC>, Cfg::JOINT>(x, ph == 2, t, lay, tw, CC * Cfg::NPAD,
-                                                                 ph == 2 || !a.ktab);
+        fft_components<C, N, E, M, ColLayout<C, CC>, Cfg::JOINT, CC>(x, ph == 2, t, lay, tw, CC * Cfg::NPAD,
+                                                                     ph == 2 || !a.ktab, a.fx != 0);
       continue;
     }
     if (a.ktab) {
@@ -1046,7 +1087,7 @@ line1d_kernel(const PassArgs a, const int64_t nlines) {
 #pragma unroll 1
     for (int ph = 0; ph < 5; ++ph) {
       if (ph == 1 || ph == 3) {
-        if (a.ktab) fft_components<C, N, E, M>(x, ph == 3, t, lay, tw);
+        if (a.ktab) fft_components<C, N, E, M, RowLayout<C>, false, 1>(x, ph == 3, t, lay, tw, 0, true, a.fx != 0);
       } else if (ph == 2) {
         if (a.ktab) {
 #pragma unroll
@@ -1104,6 +1145,7 @@ struct PlaneCfg {
 
 template <int STRIDE, typename C>
 struct StridedLayout {  // point n of a column at n * STRIDE
+  template <typename D> using rebind = StridedLayout<STRIDE, D>;
   C* base;
   template <int NS, int R>
   __device__ __forceinline__ int addr(int idx) const { return idx * STRIDE; }
@@ -1142,7 +1184,7 @@ plane_kernel(const PassArgs a) {
 #pragma unroll
           for (int i = 0; i < E; ++i) x[m][i] = f[m * P + (ct + T * i) * N + c];
         __syncthreads();  // the column's slots become FFT exchange space
-        fft_components<C, N, E, M>(x, false, ct, lay, twy);
+        fft_components<C, N, E, M, StridedLayout<N, C>, false, LPR>(x, false, ct, lay, twy, 0, true, a.fx != 0);
 #pragma unroll 1
         for (int i = 0; i < E; ++i) {
           C v[M];
@@ -1156,7 +1198,7 @@ plane_kernel(const PassArgs a) {
             x[m][E - 1] = v[m];
           }
         }
-        fft_components<C, N, E, M>(x, true, ct, lay, twy);
+        fft_components<C, N, E, M, StridedLayout<N, C>, false, LPR>(x, true, ct, lay, twy, 0, true, a.fx != 0);
         __syncthreads();
 #pragma unroll
         for (int m = 0; m < M; ++m)
@@ -1178,7 +1220,7 @@ plane_kernel(const PassArgs a) {
 #pragma unroll
         for (int i = 0; i < E; ++i) x[m][i] = f[m * P + y * N + t + T * i];
       __syncthreads();  // the line's slots become FFT exchange space
-      if (!first && a.ktab) fft_components<C, N, E, M>(x, true, t, lay, twx);
+      if (!first && a.ktab) fft_components<C, N, E, M, RowLayout<C>, false, 1>(x, true, t, lay, twx, 0, true, a.fx != 0);
       if (!first) half_points<Real, M, E>(x, a, y * N + t, T, b, 2 * k - 1);
       if (save) {
         const int64_t slot = s / a.save_every - 1;
@@ -1188,7 +1230,7 @@ plane_kernel(const PassArgs a) {
           for (int i = 0; i < E; ++i) store_save<Real>(a.save[m], slot * a.save_stride + b * P + y * N + t + T * i, x[m][i]);
       }
       if (!last) half_points<Real, M, E>(x, a, y * N + t, T, b, 2 * k);
-      if (!last && a.ktab) fft_components<C, N, E, M>(x, false, t, lay, twx);
+      if (!last && a.ktab) fft_components<C, N, E, M, RowLayout<C>, false, 1>(x, false, t, lay, twx, 0, true, a.fx != 0);
       __syncthreads();
 #pragma unroll
       for (int m = 0; m < M; ++m)
@@ -1262,7 +1304,7 @@ __device__ __forceinline__ void matrix_half_step(typename CT<Real>::T (&u)[2], c
     if (a.pprof[j]) {
       prof[j] = ((a.pump_uniform >> j) & 1) ? cunit<C>()
                 : a.pprof_cplx ? ldgc((const C*)a.pprof[j] + p) : Prof<Real>::cplx(a.pprof[j], p);
-      u[j] = cadd(u[j], pump_mul(pn[j], prof[j], a.pprof_cplx));
+      u[j] = pump_add(u[j], pn[j], prof[j], a.pprof_cplx);
     }
   }
   const C y0 = cadd(cmul(Em[0], u[0]), cmul(Em[1], u[1]));
@@ -1271,7 +1313,7 @@ __device__ __forceinline__ void matrix_half_step(typename CT<Real>::T (&u)[2], c
   u[1] = y1;
 #pragma unroll
   for (int j = 0; j < 2; ++j)
-    if (a.pprof[j]) u[j] = cadd(u[j], pump_mul(px[j], prof[j], a.pprof_cplx));
+    if (a.pprof[j]) u[j] = pump_add(u[j], px[j], prof[j], a.pprof_cplx);
   if (a.noise != NOISE_OFF) {
     C xi[2];
     draw_xi<Real, 2>(a, p, b, h, xi);

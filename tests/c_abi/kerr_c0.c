@@ -45,7 +45,11 @@ int main(int argc, char** argv) {
   d.dt = dt;
   d.t0 = 0.0;
   d.device = -1;
-  d.flags = (argc > 2 && strcmp(argv[2], "dw") == 0) ? GPE_FLAG_FP64_DW : 0; /* native FP64 by default */
+  /* block floating point line transforms by default; "native": FP64 floating point
+     throughout; "dw": double-word */
+  d.flags = argc > 2 && strcmp(argv[2], "dw") == 0       ? GPE_FLAG_FP64_DW
+            : argc > 2 && strcmp(argv[2], "native") == 0 ? GPE_FLAG_FP64_NATIVE
+                                                          : 0;
   gpe_handle* h = NULL;
   CHECK(NULL, gpe_create(&d, &h));
 

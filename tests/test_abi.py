@@ -106,6 +106,8 @@ def _desc(L, **kw):
     (dict(n=(100, 64, 1)), -2),
     (dict(n=(8, 64, 1)), -2),
     (dict(n=(64, 8192, 1)), -2),
+    (dict(dtype=1, flags=32), -1),     # block floating point transforms: FP64 fields only
+    (dict(flags=32 | 16), -1),         # ... and not with the double-word mode
 ])
 def test_create_rejects_bad_descriptors(lib, gpe, kw, code):
     L = __import__("gpe_gb300._lib", fromlist=["GpeDesc"])

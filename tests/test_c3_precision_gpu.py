@@ -4,7 +4,8 @@ and g = -2 (a packet driven past the 2D collapse threshold, which amplifies ever
 difference), dt = 0.005, 1000 steps, 20 saves.  Every save of the GPU path is compared with
 the FP64 oracle (the C restatement, pinned to the numpy oracle by tests/test_oracle_c.py):
 
-* ComplexF64 fields in the default native FP64 arithmetic: rel L2 <= 1e-10 at every save;
+* ComplexF64 fields in the default native FP64 arithmetic, and with the line transforms in
+  block floating point ("bfp"): rel L2 <= 1e-10 at every save;
 * the opt-in double-word mode (unit roundoff 2^-48, 32x FP64's): rel L2 <= 1e-10 at every
   save of the smooth case; on the collapsing case it reaches 5e-10 at the collapse (native
   FP64: 5e-11), so there it is held to 1e-9 and does not meet the 1e-10 bar -- runs that
@@ -66,7 +67,7 @@ def rel_l2(a, b):
 
 
 @pytest.mark.parametrize("g", [1.0, -2.0], ids=["g+1", "g-2"])
-@pytest.mark.parametrize("fp64", ["native", "dw"], ids=["f64", "f64-dw"])
+@pytest.mark.parametrize("fp64", ["native", "bfp", "dw"], ids=["f64", "f64-bfp", "f64-dw"])
 def test_c3_fp64_every_save(gpe, lib, g, fp64):
     ref = oracle_saves(g, False)
     runs = gpu_run(gpe, g, np.complex128, fp64)

@@ -14,14 +14,14 @@ pytestmark = pytest.mark.gpu
 ROOT = Path(__file__).resolve().parents[1]
 
 
-@pytest.mark.parametrize("mode", ["dw", "native"])
+@pytest.mark.parametrize("mode", ["dw", "native", "bfp"])
 def test_plain_case_from_c(gpe, lib, tmp_path, mode):
     libdir = Path(lib._name).resolve().parent
     exe = tmp_path / "kerr_c0"
     subprocess.run(["gcc", "-O2", "-I", str(ROOT / "include"), str(ROOT / "tests" / "c_abi" / "kerr_c0.c"),
                     f"-L{libdir}", "-lgpe", f"-Wl,-rpath,{libdir}", "-lm", "-o", str(exe)], check=True)
     out = tmp_path / "out.bin"
-    args = [str(exe), str(out)] + (["dw"] if mode == "dw" else [])
+    args = [str(exe), str(out)] + ([] if mode == "bfp" else [mode])
     r = subprocess.run(args, capture_output=True, text=True, timeout=300)
     assert r.returncode == 0, r.stderr
     raw = np.fromfile(out, np.float64)

@@ -29,7 +29,7 @@ def test_longest_lines(gpe, oracle, lib, dtype, fp64, shape_c):
     assert_close(oracle, res, ores, tol)
 
 
-@pytest.mark.parametrize("fp64", ["dw", "native"])
+@pytest.mark.parametrize("fp64", ["dw", "native", "bfp"])
 def test_polariton_bench_config_full_batch(gpe, oracle, lib, fp64):
     """The throughput workload as benchmarked (512^2, two components, 64 copies): every
     copy equals the single-copy run bit for bit, and that run matches the oracle."""
@@ -64,7 +64,7 @@ def kerr_gaussian(gpe, N, dtype, g=1.0):
                                       nonlinearity=lambda u, p: g * np.abs(u[0]) ** 2)
 
 
-@pytest.mark.parametrize("fp64", ["dw", "native"])
+@pytest.mark.parametrize("fp64", ["dw", "native", "bfp"])
 def test_kerr1024_target_point_matches_oracle(gpe, oracle, lib, fp64):
     """The scalar Kerr 1024^2 FP64 point of the performance target, 10 steps."""
     N, dt, nsteps = 1024, 0.005, 10
@@ -82,7 +82,7 @@ def test_kerr1024_target_point_matches_oracle(gpe, oracle, lib, fp64):
 
 
 @pytest.mark.parametrize("dtype,fp64,tol", [(np.complex128, "dw", 1e-12), (np.complex128, "native", 1e-12),
-                                            (np.complex64, "dw", 5e-5)], ids=PREC_IDS)
+                                            (np.complex128, "bfp", 1e-12), (np.complex64, "dw", 5e-5)], ids=PREC_IDS)
 def test_kerr2048_norm_is_conserved(gpe, lib, dtype, fp64, tol):
     """Real D and G make every split step unitary: the norm of the 2048^2 field is
     conserved to rounding over 100 steps (the precision-sweep grid)."""
@@ -95,7 +95,7 @@ def test_kerr2048_norm_is_conserved(gpe, lib, dtype, fp64, tol):
     assert abs(n1 / n0 - 1) <= tol
 
 
-@pytest.mark.parametrize("fp64", ["dw", "native"])
+@pytest.mark.parametrize("fp64", ["dw", "native", "bfp"])
 def test_polariton_full_length_run(gpe, oracle, lib, fp64):
     """The polariton configuration over its full length (tspan (0, 200), dt 0.05: 4000
     steps, 100 saves, the pump ramp over the whole span) on a 128^2 grid: the error
@@ -121,7 +121,8 @@ def _c1_oracle(oracle, fp32: bool):
     return _C1[fp32]
 
 
-@pytest.mark.parametrize("dtype,fp64", [(np.complex128, "native"), (np.complex64, "native")], ids=["f64", "f32"])
+@pytest.mark.parametrize("dtype,fp64", [(np.complex128, "native"), (np.complex128, "bfp"), (np.complex64, "native")],
+                         ids=["f64", "f64-bfp", "f32"])
 def test_polariton_c1_full_size_every_save(gpe, oracle, lib, dtype, fp64):
     """The polariton configuration exactly as specified (512^2, two components, 2x2
     dispersion, pump ramp over t in [0, 200], 4000 steps, 100 saves) against the C oracle

@@ -155,7 +155,7 @@ def run_case(gpe, oracle, seed, dtype, fp64):
 
 
 @pytest.mark.parametrize("seed", list(range(24)))
-@pytest.mark.parametrize("dtype,fp64", [(np.complex128, "dw"), (np.complex128, "native"), (np.complex64, "dw")],
-                         ids=["c128-dw", "c128-native", "c64"])
+@pytest.mark.parametrize("dtype,fp64", [(np.complex128, "dw"), (np.complex128, "native"), (np.complex128, "bfp"),
+                                        (np.complex64, "dw")], ids=["c128-dw", "c128-native", "c128-bfp", "c64"])
 def test_random_problem(gpe, oracle, lib, seed, dtype, fp64):
     run_case(gpe, oracle, seed, dtype, fp64)

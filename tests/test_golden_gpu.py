@@ -13,7 +13,7 @@ from cases import c_order, jl
 pytestmark = pytest.mark.gpu
 
 GOLDEN = Path(__file__).resolve().parent / "golden"
-FP64 = ["dw", "native"]
+FP64 = ["dw", "native", "bfp"]
 
 
 def rel(a, b):

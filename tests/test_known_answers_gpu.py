@@ -1,6 +1,7 @@
 """The reference's own known-answer tests, run through the GPU path (gpe.solve on
-libgpe) at the reference's parameters and tolerances, in native FP64 (the ComplexF64
-default), in the double-word mode and with ComplexF32 fields:
+libgpe) at the reference's parameters and tolerances, for ComplexF64 fields in the default
+mode (FP64 with block floating point line transforms), in FP64 floating point throughout
+and in the double-word mode, and for ComplexF32 fields:
 
 * test/bistability_cycle.jl:1-71 -- the full 1D cycle to t = 3300 against the analytic
   bistability curve (mean error over saves 140..400 <= 3e-3), and the 27 closure-shape
@@ -22,8 +23,8 @@ import pytest
 
 pytestmark = pytest.mark.gpu
 
-MODES = [(np.complex128, "native"), (np.complex128, "dw"), (np.complex64, "native")]
-IDS = ["f64", "f64-dw", "f32"]
+MODES = [(np.complex128, "bfp"), (np.complex128, "native"), (np.complex128, "dw"), (np.complex64, "native")]
+IDS = ["f64-bfp", "f64", "f64-dw", "f32"]
 ISAPPROX = math.sqrt(np.finfo(np.float64).eps)  # Julia's default rtol for Float64 arrays
 
 

@@ -98,7 +98,7 @@ def test_matrix_nonlinearity_matrix_potential_noise_batch(gpe, oracle, lib, dtyp
     check(oracle, dtype, res, ores, orc, tspan, dt, ns, xi=xi)
 
 
-@pytest.mark.parametrize("fp64", ["dw", "native"])
+@pytest.mark.parametrize("fp64", ["dw", "native", "bfp"])
 def test_matrix_nonlinearity_1d_philox(gpe, oracle, lib, fp64):
     """1D line with in-kernel Philox noise: the draws equal the oracle's restatement."""
     N, L, B = 256, 40.0, 3

@@ -16,10 +16,11 @@ from cases import c_order, jl, kerr2d, polariton2d
 pytestmark = pytest.mark.gpu
 
 TOL = {np.complex128: 1e-10, np.complex64: 1e-5}
-# FP64 fields run in double-word arithmetic by default ("dw") or in native FP64
-FP64_MODES = ["dw", "native"]
-PRECISIONS = [(np.complex128, "dw"), (np.complex128, "native"), (np.complex64, "dw")]
-PREC_IDS = ["c128-dw", "c128-native", "c64"]
+# FP64 fields run in native FP64 by default ("native"), with block floating point line
+# transforms ("bfp") or in double-word arithmetic ("dw")
+FP64_MODES = ["dw", "native", "bfp"]
+PRECISIONS = [(np.complex128, "dw"), (np.complex128, "native"), (np.complex128, "bfp"), (np.complex64, "dw")]
+PREC_IDS = ["c128-dw", "c128-native", "c128-bfp", "c64"]
 
 
 def run_both(gpe, oracle, gpu_kw, orc, tspan, dt, nsaves, save_start=True, xi=None, rng=None, fp64="dw",
