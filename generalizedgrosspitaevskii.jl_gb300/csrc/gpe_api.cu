@@ -873,6 +873,29 @@ static int pass_variant(const gpe_handle* h) {
   return h->M == 2 && h->P * h->B <= kFinePoints ? 2 : 0;
 }
 
+// The compile-time specialised FP64 half step that covers this handle's families, or
+// LEAN_OFF: no potential, no noise, no matrix nonlinearity, a real nonlinearity, real and
+// non-uniform pump profiles, and one of the component patterns of gpe::LeanKind.
+static int lean_kind(const gpe_handle* h, const PassArgs& a) {
+  if (h->prec != gpe::PREC_F64 || h->vkind != GPE_TABLE_NONE || h->noise != GPE_NOISE_OFF || h->nl_matrix ||
+      h->pprof_cplx)
+    return gpe::LEAN_OFF;
+  int gm = 0, pm = 0;
+  for (int j = 0; j < h->M; ++j) {
+    if (a.nl_on[j] && a.nl_imag[j]) return gpe::LEAN_OFF;
+    if (a.nl_on[j]) gm |= 1 << j;
+    if (h->pprof[j]) {
+      if ((h->pump_uniform >> j) & 1) return gpe::LEAN_OFF;
+      pm |= 1 << j;
+    }
+  }
+  const int dm = a.dens_mask;
+  if (h->M == 1 && gm == 1 && dm == 1) return pm ? gpe::LEAN_M1_GP : gpe::LEAN_M1_G;
+  if (h->M == 2 && gm == 2 && dm == 2 && pm == 1) return gpe::LEAN_M2_G1P0;
+  if (h->M == 2 && gm == 3 && dm == 3 && pm == 0) return gpe::LEAN_M2_GG;
+  return gpe::LEAN_OFF;
+}
+
 static PassArgs base_args(gpe_handle* h) {
   PassArgs a;
   memset(&a, 0, sizeof a);
@@ -945,6 +968,7 @@ static PassArgs base_args(gpe_handle* h) {
       a.nfacl[m][r] = hl[1];
     }
   }
+  a.lean = lean_kind(h, a);
   a.dt = h->d.dt;
   split_dw(0.5 * h->d.dt, hl);
   a.dthf = hl[0];

@@ -9,6 +9,16 @@ struct DWR;  // double-word precision tag (defined in fft.cuh)
 
 enum TableKind { TAB_NONE = 0, TAB_SCALAR = 1, TAB_DIAG = 2, TAB_MATRIX = 3 };
 enum NoiseMode { NOISE_OFF = 0, NOISE_PHILOX = 1, NOISE_REPLAY = 2 };
+// FP64 half-step families with a compile-time specialisation (no potential, no noise,
+// real nonlinearity, real non-uniform pump profiles): G = components whose nonlinearity is
+// on, D = the densities it reads, P = pumped components.
+enum LeanKind {
+  LEAN_OFF = 0,
+  LEAN_M1_G = 1,    // one component: G from |u|^2 (Kerr)
+  LEAN_M1_GP = 2,   // one component: G from |u|^2, pumped (driven Kerr)
+  LEAN_M2_G1P0 = 3, // two components: G_2 from |u_2|^2, pump on component 1 (exciton-polariton)
+  LEAN_M2_GG = 4    // two components: G_1, G_2 from both densities, no pump (two-component condensate)
+};
 
 // One launch of a line pass.  Plain data only: it is copied to the kernel's
 // parameter space by value.
@@ -86,6 +96,9 @@ struct PassArgs {
   // FP64 line transforms of the row and column passes in block floating point on the
   // integer pipes (Q62 twiddles after the FP64 ones in the table)
   int32_t fx;
+  // FP64 half steps of the common families specialised at compile time (LeanKind; 0 =
+  // the generic half step)
+  int32_t lean;
   // host-mapped status word: a device wait that ran out of time stores 1 here
   int32_t* status;
 };

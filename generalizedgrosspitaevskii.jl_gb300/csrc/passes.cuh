@@ -758,6 +758,91 @@ __device__ __forceinline__ void fft_components(C (&x)[M][E], bool inverse, int t
   }
 }
 
+// ------------------------------------------------------------------ lean FP64 half steps
+// The generic half step decides its families (potential, pump, noise, which components G
+// touches) at run time.  Short conditional blocks are compiled to predicated code that
+// issues whether or not it applies, so on the two-component polariton the row pass issued
+// about 81 FP64 operations a point for two half steps that need 42 (ncu), on an FP64 pipe
+// that runs at 1/64 of the FP32 rate.  The common families therefore get a half step whose
+// families are template parameters -- GM: components with a (real) nonlinearity, DM: the
+// densities it reads, PM: components with a real, non-uniform pump profile; no potential,
+// no noise -- chosen by the host (PassArgs::lean).  Its arithmetic is the generic half
+// step's operation for operation (src/kernels.jl:37-54): G on u, u + dt/4 a(t_h) p, the
+// phase cis(-dt/2 G) (sc<double>), + dt/4 a(t_{h+1}) p; components without G take both
+// pump terms as one (coefficients summed by load_pump).
+template <int M, int GM, int DM, int PM>
+__device__ __forceinline__ void half_step_lean(double2 (&u)[M], const PassArgs& a, int64_t p,
+                                               const double2 (&pn)[M], const double2 (&px)[M]) {
+  double dens[M], prof[M];
+#pragma unroll
+  for (int l = 0; l < M; ++l) dens[l] = ((DM >> l) & 1) ? u[l].x * u[l].x + u[l].y * u[l].y : 0.0;
+#pragma unroll
+  for (int j = 0; j < M; ++j) {
+    if ((PM >> j) & 1) {
+      prof[j] = __ldg((const double*)a.pprof[j] + p);
+      if ((GM >> j) & 1) {
+        u[j].x = fma(pn[j].x, prof[j], u[j].x);
+        u[j].y = fma(pn[j].y, prof[j], u[j].y);
+      }
+    }
+  }
+#pragma unroll
+  for (int j = 0; j < M; ++j) {
+    if ((GM >> j) & 1) {
+      double pr = a.cd[j][0];
+#pragma unroll
+      for (int l = 0; l < M; ++l)
+        if ((DM >> l) & 1) pr = fma(a.gd[j][l][0], dens[l], pr);
+      double s, c;
+      sc<double>(pr, &s, &c);
+      double2 E;
+      E.x = c;
+      E.y = -s;
+      u[j] = cmul(E, u[j]);
+    }
+  }
+#pragma unroll
+  for (int j = 0; j < M; ++j) {
+    if ((PM >> j) & 1) {
+      u[j].x = fma(px[j].x, prof[j], u[j].x);
+      u[j].y = fma(px[j].y, prof[j], u[j].y);
+    }
+  }
+}
+
+template <int M, int E, int GM, int DM, int PM>
+__device__ __forceinline__ void lean_points(double2 (&x)[M][E], const PassArgs& a, int64_t p0, int T,
+                                            const double2 (&pn)[M], const double2 (&px)[M]) {
+  // one point a trip (the phase routine's general branch is long); the arrays rotate by one
+#pragma unroll 1
+  for (int i = 0; i < E; ++i) {
+    double2 v[M];
+#pragma unroll
+    for (int m = 0; m < M; ++m) v[m] = x[m][0];
+    half_step_lean<M, GM, DM, PM>(v, a, p0 + (int64_t)T * i, pn, px);
+#pragma unroll
+    for (int m = 0; m < M; ++m) {
+#pragma unroll
+      for (int q = 0; q + 1 < E; ++q) x[m][q] = x[m][q + 1];
+      x[m][E - 1] = v[m];
+    }
+  }
+}
+
+// the lean half step of kind a.lean on the E points a thread holds; false if there is none
+template <int M, int E>
+__device__ __forceinline__ bool lean_dispatch(double2 (&x)[M][E], const PassArgs& a, int64_t p0, int T,
+                                              const double2 (&pn)[M], const double2 (&px)[M]) {
+  if constexpr (M == 1) {
+    if (a.lean == LEAN_M1_G) { lean_points<1, E, 1, 1, 0>(x, a, p0, T, pn, px); return true; }
+    if (a.lean == LEAN_M1_GP) { lean_points<1, E, 1, 1, 1>(x, a, p0, T, pn, px); return true; }
+  } else {
+    if (a.lean == LEAN_M2_G1P0) { lean_points<2, E, 2, 2, 1>(x, a, p0, T, pn, px); return true; }
+    if (a.lean == LEAN_M2_GG) { lean_points<2, E, 3, 3, 0>(x, a, p0, T, pn, px); return true; }
+  }
+  return false;
+}
+
 // Half step h on the E points a thread holds (points p0 + T*i).  The point loop is not
 // unrolled, so the kernel holds one copy of the half step (the double-word step is
 // several hundred instructions; eight unrolled copies overflow the instruction cache).
@@ -769,6 +854,9 @@ __device__ __forceinline__ void half_points(typename CT<Real>::T (&x)[M][E], con
   using C = typename CT<Real>::T;
   C pn[M], px[M];
   load_pump<Real, M>(a, h, pn, px, true);
+  if constexpr (std::is_same<Real, double>::value) {
+    if (a.lean != LEAN_OFF && lean_dispatch<M, E>(x, a, p0, T, pn, px)) return;
+  }
 // FP32 points per trip of the half-step loop: 2 measured fastest on the 512^2 polariton
 // row pass (0.61 ms against 0.68 ms with all 8 unrolled, whose code spills out of the
 // instruction cache, and 0.64 ms with 1)
