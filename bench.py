@@ -266,6 +266,10 @@ def algorithmic_bytes(dtype, B: int):
 
 def binding_limit(dtype, fp64: str) -> str:
     """What bounds the passes of this precision (from ncu captures of the same passes)."""
+    if dtype == np.complex128 and fp64 == "bfp":
+        return ("row pass: FP64 pipe (the pointwise half steps; GB300 issues FP64 at 1/64 of the FP32 rate) "
+                "overlapped with the block floating point transforms on the integer pipes; column pass: integer "
+                "ALU pipe (transforms and FP64 <-> fixed point conversions) and issue; DRAM below 10 % of peak")
     if dtype == np.complex128 and fp64 == "native":
         return ("FP64 pipe: 82-83 % active in both passes (GB300 issues FP64 at 1/64 of the FP32 rate, about "
                 "1.2 TFLOP/s); DRAM stays below 10 % of peak")

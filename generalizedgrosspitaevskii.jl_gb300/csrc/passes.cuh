@@ -770,6 +770,37 @@ __device__ __forceinline__ void fft_components(C (&x)[M][E], bool inverse, int t
 // step's operation for operation (src/kernels.jl:37-54): G on u, u + dt/4 a(t_h) p, the
 // phase cis(-dt/2 G) (sc<double>), + dt/4 a(t_{h+1}) p; components without G take both
 // pump terms as one (coefficients summed by load_pump).
+// sin/cos of the phase with the Taylor series as short as the angle allows: |x| < 2^-10
+// through x^4 / x^5 (the first dropped terms below 2e-21, relative for sin), |x| < 2^-6
+// through x^6 / x^7 (below 9e-20), else sc<double>: 6, 8 or 12 FP64 operations.  Each
+// point takes its own tier, so results do not depend on which points share a warp; a warp
+// whose points agree runs that tier alone (warp votes), a mixed warp runs every tier its
+// points need.
+__device__ __forceinline__ void sc_tier0(double x, double* s, double* c) {
+  const double x2 = x * x;
+  *c = fma(x2, fma(x2, 1.0 / 24, -0.5), 1.0);
+  *s = x * fma(x2, fma(x2, 1.0 / 120, -1.0 / 6), 1.0);
+}
+__device__ __forceinline__ void sc_tier1(double x, double* s, double* c) {
+  const double x2 = x * x;
+  *c = fma(x2, fma(x2, fma(x2, -1.0 / 720, 1.0 / 24), -0.5), 1.0);
+  *s = x * fma(x2, fma(x2, fma(x2, -1.0 / 5040, 1.0 / 120), -1.0 / 6), 1.0);
+}
+__device__ __forceinline__ void sc_lean(double x, double* s, double* c) {
+  const int hx = __double2hiint(x) & 0x7fffffff;
+  const int tier = hx < 0x3f500000 ? 0 : hx < 0x3f900000 ? 1 : 2;
+  const unsigned w = __activemask();
+  if (__all_sync(w, tier == 0)) {
+    sc_tier0(x, s, c);
+  } else if (__all_sync(w, tier == 1)) {
+    sc_tier1(x, s, c);
+  } else {
+    sc<double>(x, s, c);
+    if (tier == 1) sc_tier1(x, s, c);
+    if (tier == 0) sc_tier0(x, s, c);
+  }
+}
+
 template <int M, int GM, int DM, int PM>
 __device__ __forceinline__ void half_step_lean(double2 (&u)[M], const PassArgs& a, int64_t p,
                                                const double2 (&pn)[M], const double2 (&px)[M]) {
@@ -794,7 +825,7 @@ __device__ __forceinline__ void half_step_lean(double2 (&u)[M], const PassArgs& 
       for (int l = 0; l < M; ++l)
         if ((DM >> l) & 1) pr = fma(a.gd[j][l][0], dens[l], pr);
       double s, c;
-      sc<double>(pr, &s, &c);
+      sc_lean(pr, &s, &c);
       double2 E;
       E.x = c;
       E.y = -s;
