@@ -342,10 +342,36 @@ __device__ __forceinline__ void fused_first_layer(double2 (&v)[R], const double2
 // after a stage (NS, R) XOR-swizzles the slot within each 128-byte row with a key
 // taken from the row number, chosen so that both the scattered stage writes and
 // the strided reads of the next stage are free of bank conflicts.
-template <typename C>
+//
+// TL > 0: each line is held by TL threads of its own (whole warps, or a part of one warp),
+// and the exchange barriers cover only the line (a named barrier of the line's warps, or
+// the warp), so lines of one block can be at different points of their work.  TL = 0:
+// block-wide barriers.
+template <typename C, int TL = 0>
 struct RowLayout {
-  template <typename D> using rebind = RowLayout<D>;
+  template <typename D> using rebind = RowLayout<D, TL>;
   C* base;
+  __device__ __forceinline__ static void sync() {
+    if constexpr (TL == 0) {
+      __syncthreads();
+    } else if constexpr (TL <= 32) {
+      __syncwarp(blockDim.x >= 32 ? 0xffffffffu : (1u << blockDim.x) - 1u);
+    } else {
+      static_assert(TL % 32 == 0, "a line must be whole warps");
+      // barrier 1 + line index, as immediates so that a block reserves only the ones it
+      // uses; row blocks hold at most 256 threads, so at most NL lines
+      constexpr int NL = TL >= 256 ? 1 : 256 / TL;
+      const int l = threadIdx.x / TL;
+      if (NL == 1 || l == 0) asm volatile("bar.sync 1, %0;" ::"n"(TL) : "memory");
+      else if (NL == 2 || l == 1) asm volatile("bar.sync 2, %0;" ::"n"(TL) : "memory");
+      else if (l == 2) asm volatile("bar.sync 3, %0;" ::"n"(TL) : "memory");
+      else if (NL == 4 || l == 3) asm volatile("bar.sync 4, %0;" ::"n"(TL) : "memory");
+      else if (l == 4) asm volatile("bar.sync 5, %0;" ::"n"(TL) : "memory");
+      else if (l == 5) asm volatile("bar.sync 6, %0;" ::"n"(TL) : "memory");
+      else if (l == 6) asm volatile("bar.sync 7, %0;" ::"n"(TL) : "memory");
+      else asm volatile("bar.sync 8, %0;" ::"n"(TL) : "memory");
+    }
+  }
   static constexpr int S = 128 / (int)sizeof(C);  // complex slots per 128-byte row
   static constexpr int LOGS = ilog2(S);
   template <int NS, int R>
@@ -369,6 +395,7 @@ struct ColLayout {
   template <typename D> using rebind = ColLayout<D, CC>;
   static constexpr bool PAD = sizeof(C) == 8;
   C* base;  // already offset by the column index
+  __device__ __forceinline__ static void sync() { __syncthreads(); }
   template <int NS, int R>
   __device__ __forceinline__ int addr(int idx) const { return (PAD ? idx + (idx >> 3) : idx) * CC; }
 };
@@ -438,10 +465,10 @@ __device__ __forceinline__ void fft_stages(C (&x)[E], int t, const Lay& lay, con
   constexpr int T = N / E;
   fft_stage<C, N, E, R, NS, DIR, LAST>(x, t, lay, tw);
   if constexpr (!LAST) {
-    __syncthreads();
+    lay.sync();
 #pragma unroll
     for (int i = 0; i < E; ++i) x[i] = lay.base[lay.template addr<NS, R>(t + T * i)];
-    __syncthreads();
+    lay.sync();
     fft_stages<C, N, E, DIR, NS * R>(x, t, lay, tw);
   }
 }
@@ -514,14 +541,14 @@ __device__ __forceinline__ void fft_stages_joint(C (&x)[M][E], int t, const Lay&
   constexpr int T = N / E;
   fft_stage_joint<C, N, E, R, NS, DIR, LAST, M>(x, t, lay, cstride, tw);
   if constexpr (!LAST) {
-    __syncthreads();
+    lay.sync();
 #pragma unroll
     for (int i = 0; i < E; ++i) {
       const int ad = lay.template addr<NS, R>(t + T * i);
 #pragma unroll
       for (int m = 0; m < M; ++m) x[m][i] = lay.base[m * cstride + ad];
     }
-    __syncthreads();
+    lay.sync();
     fft_stages_joint<C, N, E, DIR, NS * R, M>(x, t, lay, cstride, tw);
   }
 }
@@ -595,13 +622,13 @@ struct LineMax {
 __device__ __forceinline__ long long fx_from_double(double v, int emax) {
   const long long b = __double_as_longlong(v);
   const int e = (int)((b >> 52) & 0x7ff);
-  const long long m = (b & 0xfffffffffffffLL) | 0x10000000000000LL;
-  // v = m 2^(e - 1075): shift right by emax - e + 53 - FX_TOP (at least -5)
-  const int sh = emax - e + (53 - FX_TOP);
-  long long r;
-  if (sh <= 0) r = m << (-sh);
-  else r = sh < 64 ? (m + (1LL << (sh - 1))) >> sh : 0;
-  if (e == 0) r = 0;
+  // the significand with its leading bit, times 2^6 (below 2^59); zero and subnormals: 0
+  const unsigned long long m6 = e ? ((b & 0xfffffffffffffULL) | 0x10000000000000ULL) << 6 : 0ull;
+  // v 2^(FX_TOP + 1022 - emax) = m 2^(5 - s) = m6 2^-(s + 1), s = emax - e >= 0: shift right by
+  // s, then by one more with the rounding half unit (exact for s <= 5; branch-free)
+  static_assert(FX_TOP == 58, "the shifts below place the top at 2^58");
+  const int s = min(emax - e, 63);
+  const long long r = (long long)(((m6 >> s) + 1) >> 1);
   return b < 0 ? -r : r;
 }
 // r * 2^eb rounded to the nearest double (ties away from zero), integer operations only;
@@ -636,7 +663,7 @@ __device__ __forceinline__ void fx_stages(fxc (&x)[E], int t, const Lay& lay, co
   if constexpr (!LAST) {
     const int lw = LM::warp(mag ? 64 - __clz((int)mag) : 32);
     LM::publish(lw, red);
-    __syncthreads();
+    lay.sync();
 #pragma unroll
     for (int i = 0; i < E; ++i) x[i] = lay.base[lay.template addr<NS, R>(t + T * i)];
     const int sh = max(0, LM::collect(lw, red) - FX_TOP);
@@ -649,7 +676,7 @@ __device__ __forceinline__ void fx_stages(fxc (&x)[E], int t, const Lay& lay, co
       }
     }
     shsum += sh;
-    __syncthreads();
+    lay.sync();
     fx_stages<N, E, NS * R, Lay, LM>(x, t, lay, tw, red, shsum);
   }
 }
@@ -672,7 +699,7 @@ __device__ __forceinline__ void fx_line(double2 (&x)[E], int t, const Lay& lay, 
   }
   int em = LM::warp((int)(hm >> 20));
   LM::publish(em, red_in);
-  if constexpr (LM::MULTI) __syncthreads();
+  if constexpr (LM::MULTI) lay.sync();
   em = LM::collect(em, red_in);
   fxc v[E];
 #pragma unroll

@@ -99,6 +99,8 @@ struct gpe_handle {
   void* tw[3] = {nullptr, nullptr, nullptr};
   void* ktab = nullptr;
   int kkind = GPE_TABLE_NONE;
+  void* ktab_q = nullptr;  // Q62 copy for block floating point column passes (FP64 fields)
+  int kq_exp = 0;
   std::vector<cd> Dsamples;  // dispersion samples kept for gpe_energy
   int dkind = GPE_TABLE_NONE;
   void* vtab = nullptr;
@@ -480,6 +482,7 @@ int gpe_destroy(gpe_handle* h) {
   }
   for (int a = 0; a < 3; ++a) cudaFree(h->tw[a]);
   cudaFree(h->ktab);
+  cudaFree(h->ktab_q);
   cudaFree(h->vtab);
   cudaFree(h->nlm);
   cudaFree(h->save_buf);
@@ -621,10 +624,34 @@ static int check_kind(gpe_handle* h, int kind) {
 
 static int store_ktable(gpe_handle* h, const std::vector<cd>& tab, int kind) {
   cudaFree(h->ktab);
-  h->ktab = nullptr;
+  cudaFree(h->ktab_q);
+  h->ktab = h->ktab_q = nullptr;
   h->kkind = GPE_TABLE_NONE;
   int rc = upload_table(h, &h->ktab, tab.data(), tab.size());
   if (rc) return rc;
+  if (h->prec == gpe::PREC_F64 && !(h->d.flags & GPE_FLAG_FP64_NATIVE)) {
+    // the Q62 copy the block floating point column pass applies on the integer pipes:
+    // entries times P 2^-kexp, kexp the least exponent that keeps every real and imaginary
+    // part within 1 (P = 2^k, so the scaling is exact)
+    double mx = 0.0;
+    for (const cd& v : tab) mx = std::max(mx, std::max(std::fabs(v.real()), std::fabs(v.imag())));
+    mx *= (double)h->P;
+    int kexp = 0;
+    if (mx > 0.0) {
+      std::frexp(mx, &kexp);  // mx = f 2^kexp, f in [0.5, 1)
+    }
+    std::vector<int32_t> q(4 * tab.size());
+    const long double s = std::ldexp((long double)h->P, -kexp);
+    for (size_t i = 0; i < tab.size(); ++i) {
+      q62_split(s * (long double)tab[i].real(), &q[4 * i]);
+      q62_split(s * (long double)tab[i].imag(), &q[4 * i + 2]);
+    }
+    CK(h, cudaMalloc(&h->ktab_q, q.size() * sizeof(int32_t)));
+    CK(h, cudaMemcpy(h->ktab_q, q.data(), q.size() * sizeof(int32_t), cudaMemcpyHostToDevice));
+    int logp = 0;
+    while ((int64_t(1) << logp) < h->P) ++logp;
+    h->kq_exp = kexp - logp;
+  }
   h->kkind = kind;
   return GPE_OK;
 }
@@ -911,6 +938,8 @@ static PassArgs base_args(gpe_handle* h) {
   for (int m = 0; m < h->M; ++m) a.u[m] = h->u[m];
   a.ktab = h->ktab;
   a.kkind = h->kkind;
+  a.ktab_q = h->ktab_q;
+  a.kq_exp = h->kq_exp;
   a.vtab = h->vtab;
   a.vkind = h->vkind;
   float hl[2];

@@ -34,6 +34,10 @@ struct PassArgs {
   // k-space table exp(-i dt D)/P (col pass / 1D) and real-space table exp(-i dt/2 V)
   const void* ktab;
   int32_t kkind;
+  // FP64 passes with block floating point transforms: the k-space table in Q62 fixed point
+  // ({re.hi, re.lo, im.hi, im.lo} 32-bit halves, entries times P 2^-kexp), kq_exp = kexp - log2 P
+  const void* ktab_q;
+  int32_t kq_exp;
   const void* vtab;
   int32_t vkind;
   // twiddles w_N^k, k < N, for the transformed line length (tw2: y lines of the

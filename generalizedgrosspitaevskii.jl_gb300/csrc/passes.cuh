@@ -844,18 +844,24 @@ __device__ __forceinline__ void half_step_lean(double2 (&u)[M], const PassArgs& 
 template <int M, int E, int GM, int DM, int PM>
 __device__ __forceinline__ void lean_points(double2 (&x)[M][E], const PassArgs& a, int64_t p0, int T,
                                             const double2 (&pn)[M], const double2 (&px)[M]) {
-  // one point a trip (the phase routine's general branch is long); the arrays rotate by one
+  // U points a trip, their FP64 chains independent (the phase routine's general branch is
+  // long, so the loop is not unrolled further); the arrays rotate by U
+  constexpr int U = E % 2 == 0 ? 2 : 1;
 #pragma unroll 1
-  for (int i = 0; i < E; ++i) {
-    double2 v[M];
+  for (int i = 0; i < E; i += U) {
+    double2 v[U][M];
 #pragma unroll
-    for (int m = 0; m < M; ++m) v[m] = x[m][0];
-    half_step_lean<M, GM, DM, PM>(v, a, p0 + (int64_t)T * i, pn, px);
+    for (int u = 0; u < U; ++u) {
+#pragma unroll
+      for (int m = 0; m < M; ++m) v[u][m] = x[m][u];
+      half_step_lean<M, GM, DM, PM>(v[u], a, p0 + (int64_t)T * (i + u), pn, px);
+    }
 #pragma unroll
     for (int m = 0; m < M; ++m) {
 #pragma unroll
-      for (int q = 0; q + 1 < E; ++q) x[m][q] = x[m][q + 1];
-      x[m][E - 1] = v[m];
+      for (int q = 0; q + U < E; ++q) x[m][q] = x[m][q + U];
+#pragma unroll
+      for (int u = 0; u < U; ++u) x[m][E - U + u] = v[u][m];
     }
   }
 }
@@ -1018,10 +1024,256 @@ row_kernel(const PassArgs a, const int64_t nlines, const int lb) {
   }
 }
 
+// Row pass of FP64 fields whose line transforms run in block floating point (a.fx):
+// the transforms occupy the integer pipes and the half steps the FP64 pipe, and when every
+// line of a block is in the same phase one pipe idles while the other works.  So each block
+// holds two groups of lines that step through the same work half a cycle apart.  The
+// block's items (LG lines each) alternate between the groups; time is cut into slots
+// closed by a block barrier, and in every slot one group runs half steps (FP64) while the
+// other runs integer work -- the forward transform and store of its last item, then the
+// load and inverse transform of its next:
+//   slot:     0        1        2              3        4  ...
+//   group 0:  iFFT(0)  half(0)  FFT(0) iFFT(2) half(2)  FFT(2) iFFT(4) ...
+//   group 1:  -        iFFT(1)  half(1)        FFT(1) iFFT(3) half(3) ...
+// The transforms' exchanges synchronise per line (named barriers).  Blocks are persistent
+// (two a multiprocessor), block c taking items c, c + gridDim, ...  Every item goes through
+// the same code as in row_kernel, so the results are bit-identical to it.
+template <int LOGN, int M>
+__global__ void __launch_bounds__(LineCfg<double, M, LOGN, 0>::ROW_THREADS, LineCfg<double, M, LOGN, 0>::ROW_MINB)
+row_kernel_pipe(const PassArgs a, const int64_t nlines) {
+  using Cfg = LineCfg<double, M, LOGN, 0>;
+  using C = double2;
+  constexpr int N = Cfg::N, E = Cfg::ER, T = Cfg::TR, L = Cfg::L, LG = L / 2;
+  static_assert(T % 32 == 0 && L % 2 == 0, "groups of whole-warp lines");
+  extern __shared__ __align__(16) unsigned char smraw[];
+  C* sm = reinterpret_cast<C*>(smraw);
+  const int t = threadIdx.x % T, l = threadIdx.x / T;
+  const int grp = l / LG, lg = l % LG;
+  using RL = RowLayout<C, T>;
+  const RL lay{sm + l * N};
+  const auto* tw = (const C*)a.tw;
+  const int64_t lpb = a.P / N;
+  const int64_t nitems = (nlines + LG - 1) / LG;
+  const int G = gridDim.x;
+  // items of group g: (2k + g) G + blockIdx.x for k < n[g]
+  auto count = [&](int g) -> int {
+    const int64_t first = (int64_t)g * G + blockIdx.x;
+    return first < nitems ? (int)((nitems - 1 - first) / (2 * (int64_t)G)) + 1 : 0;
+  };
+  const int n0 = count(0), n1 = count(1), ng = grp ? n1 : n0;
+  const int nslots = n0 > 0 ? 2 * (n0 > n1 ? n0 : n1) + 2 : 0;
+  C x[M][E];
+  int64_t p0 = 0, b = 0;
+  bool active = false;
+  auto locate = [&](int k) {
+    int64_t line = ((int64_t)(2 * k + grp) * G + blockIdx.x) * LG + lg;
+    active = line < nlines;
+    if (!active) line = nlines - 1;  // idle lines compute a copy, store nothing
+    b = line / lpb;
+    p0 = (line - b * lpb) * N + t;
+  };
+  const int64_t hbase = a.kbase ? 2 * *a.kbase : 0;
+  // one call site each for the transform and the half step (as in row_kernel): the inner
+  // loops are not unrolled
+#pragma unroll 1
+  for (int s = 0; s < nslots; ++s) {
+    const int ls = s - grp;
+    const int k = ls >> 1;
+    if (ls >= 0 && (ls & 1) == 0) {
+      // integer slot: j = 0 finishes item k - 1 (forward transform, store), j = 1 starts
+      // item k (load, inverse transform)
+#pragma unroll 1
+      for (int j = 0; j < 2; ++j) {
+        const bool fin = j == 0;
+        if (fin ? (k >= 1 && k - 1 < ng) : (k < ng)) {
+          if (!fin) {
+            locate(k);
+#pragma unroll
+            for (int m = 0; m < M; ++m)
+#pragma unroll
+              for (int i = 0; i < E; ++i) x[m][i] = ((const C*)a.u[m])[b * a.P + p0 + T * i];
+          }
+          if (fin ? a.do_fft : a.do_ifft)
+            fft_components<C, N, E, M, RL, false, 1>(x, !fin, t, lay, tw, 0, fin || !a.do_fft, true);
+          if (fin && active) {
+#pragma unroll
+            for (int m = 0; m < M; ++m)
+#pragma unroll
+              for (int i = 0; i < E; ++i) ((C*)a.u[m])[b * a.P + p0 + T * i] = x[m][i];
+          }
+        }
+      }
+    } else if (ls >= 0 && k < ng) {
+      // FP64 slot: half step A, the save, half step B
+#pragma unroll 1
+      for (int j = 0; j < 2; ++j) {
+        const int64_t hr = j ? a.hB : a.hA;
+        if (hr >= 0) half_points<double, M, E>(x, a, p0, T, b, hr + hbase);
+        if (j == 0 && a.save[0] && active) {
+#pragma unroll
+          for (int m = 0; m < M; ++m)
+#pragma unroll
+            for (int i = 0; i < E; ++i) store_save<double>(a.save[m], b * a.P + p0 + T * i, x[m][i]);
+        }
+      }
+    }
+    __syncthreads();
+  }
+}
+
 // ------------------------------------------------------------------ column pass
 // The work on one tile held in registers: FFT_y, the k-space table, iFFT_y (one FFT
 // instance: the phase loop is not unrolled).  sp0: spatial index of this thread's first
 // point, step: index distance between its points.
+// v 2^-d rounded to the nearest (d > 0, at most 63) or exactly (d <= 0, the result below 2^63)
+__device__ __forceinline__ long long fx_shift(long long v, int d) {
+  if (d > 0) {
+    d = min(d, 63);
+    return (v + (1LL << (d - 1))) >> d;
+  }
+  return v << (-d);
+}
+
+// Column tile of FP64 lines with block floating point transforms and a k-space table
+// (FFT_y, table, iFFT_y in one pass): the forward transforms' outputs stay in fixed point,
+// the table is applied to them on the integer pipes from its Q62 copy (a.ktab_q, entries
+// scaled by 2^-kexp so that no component exceeds 1; a.kq_exp = kexp - log2 P restores the
+// scale), and the inverse transforms start from the products.  Two of the four conversions
+// between FP64 and fixed point of every line, and the FP64 work of the table, drop out.
+// Before the table the lines are shifted to a common exponent (the 2x2 table mixes the
+// components) that puts the largest component below 2^56, so the mat-vec's sums stay below
+// 2^58, the transforms' input bound.  Each product rounds to within a unit of 2^-56 of the
+// larger line's largest component; FP64 rounds each to 2^-53 of its own value.  One
+// transform instance serves the four transforms (runtime direction, components rotated
+// through the registers of component 0, as fft_components does).
+template <int N, int E, int M, int CC>
+__device__ __forceinline__ void col_fx_ktab(double2 (&x)[M][E], const PassArgs& a, int t, double2* xbase,
+                                            int64_t sp0, int64_t step) {
+  using LF = ColLayout<fxc, CC>;
+  using LM = LineMax<CC, N / E>;
+  const LF lf{reinterpret_cast<fxc*>(xbase)};
+  const fxw* twq = reinterpret_cast<const fxw*>((const double2*)a.tw + N);
+  __shared__ int red_in[LM::RED], red_x[LM::RED];
+  constexpr int TOPK = 56;
+  // per component (slot 0 holds the one being transformed; the others rotate with it):
+  // exponent (value = integer 2^e), bit length of the largest component, non-finite input
+  int e[M], top[M];
+  bool bad[M];
+#pragma unroll
+  for (int m = 0; m < M; ++m) { e[m] = 0; top[m] = 0; bad[m] = false; }
+#pragma unroll 1
+  for (int q = 0; q < 2 * M; ++q) {
+    const bool inv = q >= M;
+    if (q == M) {
+      // components back in order: align, then the table
+      const fxw* kq = (const fxw*)a.ktab_q;
+      int d[M];
+      if (a.kkind == TAB_MATRIX) {
+        int ec = top[0];
+#pragma unroll
+        for (int m = 1; m < M; ++m) ec = max(ec, top[m]);
+        ec -= TOPK;
+#pragma unroll
+        for (int m = 0; m < M; ++m) { d[m] = ec - e[m]; e[m] = ec; }
+        const bool b = M == 2 ? (bad[0] || bad[M - 1]) : bad[0];
+#pragma unroll
+        for (int m = 0; m < M; ++m) bad[m] = b;
+      } else {
+#pragma unroll
+        for (int m = 0; m < M; ++m) { d[m] = max(0, top[m] - e[m] - TOPK); e[m] += d[m]; }
+      }
+#pragma unroll
+      for (int i = 0; i < E; ++i) {
+        fxc v[M];
+#pragma unroll
+        for (int m = 0; m < M; ++m) {
+          v[m].x = fx_shift(__double_as_longlong(x[m][i].x), d[m]);
+          v[m].y = fx_shift(__double_as_longlong(x[m][i].y), d[m]);
+        }
+        const int64_t kp = sp0 + step * i;
+        fxc y[M];
+        if (a.kkind == TAB_MATRIX && M == 2) {
+          const fxc p00 = twmul(v[0], ldgc(kq + kp)), p01 = twmul(v[M - 1], ldgc(kq + a.P + kp));
+          const fxc p10 = twmul(v[0], ldgc(kq + 2 * a.P + kp)), p11 = twmul(v[M - 1], ldgc(kq + 3 * a.P + kp));
+          y[0].x = p00.x + p01.x;
+          y[0].y = p00.y + p01.y;
+          y[M - 1].x = p10.x + p11.x;
+          y[M - 1].y = p10.y + p11.y;
+        } else {
+#pragma unroll
+          for (int m = 0; m < M; ++m) y[m] = twmul(v[m], ldgc(kq + (a.kkind == TAB_DIAG ? (int64_t)m * a.P : 0) + kp));
+        }
+#pragma unroll
+        for (int m = 0; m < M; ++m) x[m][i] = make_double2(__longlong_as_double(y[m].x), __longlong_as_double(y[m].y));
+      }
+#pragma unroll
+      for (int m = 0; m < M; ++m) e[m] += a.kq_exp;
+    }
+    fxc v[E];
+    if (!inv) {
+      // largest biased exponent of the line, conversion below 2^FX_TOP
+      unsigned hm = 0;
+#pragma unroll
+      for (int i = 0; i < E; ++i) {
+        hm = max(hm, (unsigned)__double2hiint(x[0][i].x) & 0x7fffffffu);
+        hm = max(hm, (unsigned)__double2hiint(x[0][i].y) & 0x7fffffffu);
+      }
+      int em = LM::warp((int)(hm >> 20));
+      LM::publish(em, red_in);
+      if constexpr (LM::MULTI) lf.sync();
+      em = LM::collect(em, red_in);
+#pragma unroll
+      for (int i = 0; i < E; ++i) {
+        v[i].x = fx_from_double(x[0][i].x, em);
+        v[i].y = fx_from_double(x[0][i].y, em);
+      }
+      e[0] = em - 1022 - FX_TOP;
+      bad[0] = em == 0x7ff;
+    } else {
+      // the inverse transform as the forward one of the values with real and imaginary
+      // parts swapped
+#pragma unroll
+      for (int i = 0; i < E; ++i) {
+        v[i].x = __double_as_longlong(x[0][i].y);
+        v[i].y = __double_as_longlong(x[0][i].x);
+      }
+    }
+    int shsum = 0;
+    fx_stages<N, E, 1, LF, LM>(v, t, lf, twq, red_x, shsum);
+    e[0] += shsum;
+    if (!inv) {
+      // bit length of the line's largest component (from the high words, as the stages do)
+      unsigned mag = 0;
+#pragma unroll
+      for (int i = 0; i < E; ++i) mag |= fx_mag(v[i]);
+      const int lw = LM::warp(mag ? 64 - __clz((int)mag) : 32);
+      LM::publish(lw, red_x);
+      lf.sync();
+      top[0] = e[0] + LM::collect(lw, red_x);
+      lf.sync();  // red_x is written again by the next transform's first stage
+#pragma unroll
+      for (int i = 0; i < E; ++i) x[0][i] = make_double2(__longlong_as_double(v[i].x), __longlong_as_double(v[i].y));
+    } else {
+#pragma unroll
+      for (int i = 0; i < E; ++i) {
+        x[0][i].x = bad[0] ? __longlong_as_double(0x7ff8000000000000LL) : fx_to_double(v[i].y, e[0]);
+        x[0][i].y = bad[0] ? __longlong_as_double(0x7ff8000000000000LL) : fx_to_double(v[i].x, e[0]);
+      }
+    }
+    if constexpr (M == 2) {
+#pragma unroll
+      for (int i = 0; i < E; ++i) {
+        const double2 tmp = x[0][i];
+        x[0][i] = x[1][i];
+        x[1][i] = tmp;
+      }
+      int ti = e[0]; e[0] = e[1]; e[1] = ti;
+      ti = top[0]; top[0] = top[1]; top[1] = ti;
+      const bool tb = bad[0]; bad[0] = bad[1]; bad[1] = tb;
+    }
+  }
+}
+
 template <typename Real, int LOGN, int M, int V>
 __device__ __forceinline__ void col_tile_work(typename CT<Real>::T (&x)[M][LineCfg<Real, M, LOGN, V>::E],
                                               const PassArgs& a, int t,
@@ -1031,6 +1283,12 @@ __device__ __forceinline__ void col_tile_work(typename CT<Real>::T (&x)[M][LineC
   using C = typename CT<Real>::T;
   constexpr int N = Cfg::N, E = Cfg::E, CC = Cfg::CC;
   const auto* tw = (const typename TwT<C>::T*)a.tw;
+  if constexpr (std::is_same<Real, double>::value && !Cfg::JOINT && N > E) {
+    if (a.fx && a.ktab && a.ktab_q && a.col_fwd && a.col_inv) {
+      col_fx_ktab<N, E, M, CC>(x, a, t, lay.base, sp0, step);
+      return;
+    }
+  }
 #pragma unroll 1
   for (int ph = 0; ph < 3; ++ph) {
     if (ph != 1) {
@@ -1266,6 +1524,7 @@ template <int STRIDE, typename C>
 struct StridedLayout {  // point n of a column at n * STRIDE
   template <typename D> using rebind = StridedLayout<STRIDE, D>;
   C* base;
+  __device__ __forceinline__ static void sync() { __syncthreads(); }
   template <int NS, int R>
   __device__ __forceinline__ int addr(int idx) const { return idx * STRIDE; }
 };
@@ -1540,6 +1799,22 @@ static inline int set_smem(K k, size_t bytes) {
 template <typename Real, int M, int LOGN, int V = 0>
 int launch_row_n(const PassArgs& a, int64_t nlines, cudaStream_t s) {
   using Cfg = LineCfg<Real, M, LOGN, V>;
+  if constexpr (std::is_same<Real, double>::value && M == 1 && V == 0 && Cfg::TR % 32 == 0 && Cfg::L % 2 == 0) {
+    // block floating point transforms: the pipelined pass when every block gets at least
+    // four items a group.  One-component lines only: on the two-component polariton (512^2,
+    // 64 copies) it took 1.79 ms against 1.60 ms for row_kernel (each phase then has half
+    // the warps of a block to hide the FP64 pipe's latency), on one-component 1024^2 lines
+    // (16 copies) it gained 7 % of the step.
+    const int64_t blocks = 2 * (int64_t)(a.nsm > 0 ? a.nsm : 152);
+    const int64_t nitems = (nlines + Cfg::L / 2 - 1) / (Cfg::L / 2);
+    if (a.fx && nitems >= 8 * blocks) {
+      auto kp = row_kernel_pipe<LOGN, M>;
+      int e = set_smem(kp, Cfg::ROW_KERNEL_SMEM);
+      if (e) return e;
+      kp<<<(unsigned)blocks, Cfg::ROW_THREADS, Cfg::ROW_KERNEL_SMEM, s>>>(a, nlines);
+      return (int)cudaGetLastError();
+    }
+  }
   auto k = row_kernel<Real, LOGN, M, V>;
   int e = set_smem(k, Cfg::ROW_KERNEL_SMEM);
   if (e) return e;
