@@ -52,14 +52,15 @@ extern "C" {
 
 /* gpe_desc.flags */
 /* GPE_C128 arithmetic.  By default the pointwise steps (nonlinearity, potential, pump,
- * noise, k-space tables) run in FP64 and the line transforms in block floating point on
- * the integer pipes (GPE_FLAG_FFT_BFP): each line held as 64-bit integers under one
- * exponent, rescaled after every radix-8 stage so that its largest component stays below
- * 2^58, twiddles in Q62.  Sums are exact and every product rounds to within 2^-58 of the
- * line's largest component; measured against an FP64 oracle on a 2048^2 Kerr run of 1000
- * steps these transforms land 3-11x closer than FP64 floating-point ones, and GB300 runs
- * them at 2.2x the speed (a Q62 complex product runs 2.7x, a 64-bit add 16x faster than
- * the FP64 operations).
+ * noise) run in FP64 and the line transforms in block floating point on the integer pipes
+ * (GPE_FLAG_FFT_BFP): each line held as 64-bit integers under one exponent, rescaled after
+ * every radix-8 stage so that its largest component stays below 2^58, twiddles in Q62; a
+ * 2D column pass also applies the k-space table between its transforms from a Q62 copy
+ * (its FP64 table scaled by a power of two).  Sums are exact and every product rounds to
+ * within 2^-56 to 2^-58 of the line's largest component; measured against an FP64 oracle
+ * on a 2048^2 Kerr run of 1000 steps the results land 3-11x closer than with FP64
+ * floating-point transforms, and GB300 runs the polariton step 2.7x faster (a Q62 complex
+ * product runs 2.7x, a 64-bit add 16x faster than the FP64 operations).
  * GPE_FLAG_FP64_NATIVE runs the line transforms in FP64 floating point too.
  * GPE_FLAG_FP64_DW: opt-in fast mode, all passes on the FP32 pipes in double-word
  * arithmetic (pairs of floats, 48-bit significands, unit roundoff 2^-48, narrower than
