@@ -383,6 +383,30 @@ def fp64_roof(m: dict, B: int, sm_mhz):
             "peak_source": f"2 FP64 FMA per clock per SM x {nsm} SMs x {mhz:.0f} MHz", "kernels": out}
 
 
+def fp64_issue_roof(m: dict, B: int, sm_mhz):
+    """The FP64-pipe roof of the default FP64 row pass, whose FP64 work is its two half
+    steps (the transforms run on the integer pipes): FP64 instructions per grid point by
+    construction of the polariton's compile-time specialised half step at its shortest
+    phase polynomial (the workload's phases stay below 2^-10) -- per half step the exciton
+    density 2, phase 1, polynomial 6, rotation 4, the photon's merged pump 2 -- over the
+    mean event-timed launch, against two FP64 instructions a clock per SM at the sampled
+    clock.  The column pass holds no FP64 work."""
+    try:
+        import torch
+        nsm = torch.cuda.get_device_properties(0).multi_processor_count
+    except Exception:
+        nsm = 152
+    mhz = sm_mhz or 2070.0
+    peak = 2 * nsm * mhz * 1e6 / 1e12  # tera-instructions/s
+    P = N_GRID * N_GRID
+    per_point = 2 * (2 + 1 + 6 + 4 + 2)
+    ms = m["kms"][0] / max(m["kn"][0], 1)
+    ach = per_point * P * B / (ms * 1e-3) / 1e12
+    return {"bound": "fp64 pipe (row pass)", "unit": "FP64 Tinst/s", "peak": peak,
+            "peak_source": f"2 FP64 instructions per clock per SM x {nsm} SMs x {mhz:.0f} MHz",
+            "fp64_inst_per_point": per_point, "achieved": ach, "frac": ach / peak}
+
+
 def roofline_of(m: dict, dtype, fp64: str, B: int):
     """Dominant kernel's algorithmic bytes per launch over its mean event-timed duration,
     against the measured HBM copy bandwidth (and, for native FP64, the FP64-pipe roof)."""
@@ -405,7 +429,9 @@ def roofline_of(m: dict, dtype, fp64: str, B: int):
                         for i, k in enumerate(["row", "col"])},
             "binding_limit": binding_limit(dtype, fp64),
             **({"compute_roof": fp64_roof(m, B, (m.get("clocks") or {}).get("sm_mhz"))}
-               if dtype == np.complex128 and fp64 == "native" else {})}
+               if dtype == np.complex128 and fp64 == "native" else {}),
+            **({"compute_roof": fp64_issue_roof(m, B, (m.get("clocks") or {}).get("sm_mhz"))}
+               if dtype == np.complex128 and fp64 == "bfp" else {})}
 
 
 def run_gpu(args, rank, world, local_rank):
