@@ -283,7 +283,8 @@ def arith_name(dtype, fp64: str) -> str:
     if dtype == np.complex64:
         return "f32"
     if fp64 == "bfp":
-        return "f64 (line transforms in block floating point: 64-bit integers under one exponent a line)"
+        return ("f64 (FP64 pointwise steps; line transforms and the k-space table between them in block floating "
+                "point: 64-bit integers under one exponent a line)")
     return "f64" if fp64 == "native" else "f64-dw (double-word f32 pairs, 2^-48 unit roundoff)"
 
 

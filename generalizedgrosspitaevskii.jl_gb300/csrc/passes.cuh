@@ -841,15 +841,15 @@ __device__ __forceinline__ void half_step_lean(double2 (&u)[M], const PassArgs& 
   }
 }
 
-template <int M, int E, int GM, int DM, int PM>
-__device__ __forceinline__ void lean_points(double2 (&x)[M][E], const PassArgs& a, int64_t p0, int T,
-                                            const double2 (&pn)[M], const double2 (&px)[M]) {
+template <int M, int E, int GM, int DM, int PM, typename C>
+__device__ __forceinline__ void lean_points(C (&x)[M][E], const PassArgs& a, int64_t p0, int T,
+                                            const C (&pn)[M], const C (&px)[M]) {
   // U points a trip, their FP64 chains independent (the phase routine's general branch is
   // long, so the loop is not unrolled further); the arrays rotate by U
   constexpr int U = E % 2 == 0 ? 2 : 1;
 #pragma unroll 1
   for (int i = 0; i < E; i += U) {
-    double2 v[U][M];
+    C v[U][M];
 #pragma unroll
     for (int u = 0; u < U; ++u) {
 #pragma unroll
@@ -866,10 +866,47 @@ __device__ __forceinline__ void lean_points(double2 (&x)[M][E], const PassArgs& 
   }
 }
 
+// FP32 form of half_step_lean, operation for operation the generic FP32 half step: the
+// phase from the FP32 coefficients, E - 1 by sc_m1, the rotation's whole increment formed
+// before it is added (see half_step).
+template <int M, int GM, int DM, int PM>
+__device__ __forceinline__ void half_step_lean(float2 (&u)[M], const PassArgs& a, int64_t p,
+                                               const float2 (&pn)[M], const float2 (&px)[M]) {
+  float dens[M], prof[M];
+#pragma unroll
+  for (int l = 0; l < M; ++l) dens[l] = ((DM >> l) & 1) ? u[l].x * u[l].x + u[l].y * u[l].y : 0.0f;
+#pragma unroll
+  for (int j = 0; j < M; ++j) {
+    if ((PM >> j) & 1) {
+      prof[j] = __ldg((const float*)a.pprof[j] + p);
+      if ((GM >> j) & 1) u[j] = cadd(u[j], cscale(pn[j], prof[j]));
+    }
+  }
+#pragma unroll
+  for (int j = 0; j < M; ++j) {
+    if ((GM >> j) & 1) {
+      float gr = a.cf[j][0];
+#pragma unroll
+      for (int l = 0; l < M; ++l)
+        if ((DM >> l) & 1) gr += a.gf[j][l][0] * dens[l];
+      float s, cm1;
+      sc_m1(a.dthf * gr, &s, &cm1);
+      const float2 v = u[j];
+      const float dx = __fmaf_rn(cm1, v.x, -__fmul_rn(-s, v.y));
+      const float dy = __fmaf_rn(cm1, v.y, __fmul_rn(-s, v.x));
+      u[j].x = __fadd_rn(v.x, dx);
+      u[j].y = __fadd_rn(v.y, dy);
+    }
+  }
+#pragma unroll
+  for (int j = 0; j < M; ++j)
+    if ((PM >> j) & 1) u[j] = cadd(u[j], cscale(px[j], prof[j]));
+}
+
 // the lean half step of kind a.lean on the E points a thread holds; false if there is none
-template <int M, int E>
-__device__ __forceinline__ bool lean_dispatch(double2 (&x)[M][E], const PassArgs& a, int64_t p0, int T,
-                                              const double2 (&pn)[M], const double2 (&px)[M]) {
+template <int M, int E, typename C>
+__device__ __forceinline__ bool lean_dispatch(C (&x)[M][E], const PassArgs& a, int64_t p0, int T,
+                                              const C (&pn)[M], const C (&px)[M]) {
   if constexpr (M == 1) {
     if (a.lean == LEAN_M1_G) { lean_points<1, E, 1, 1, 0>(x, a, p0, T, pn, px); return true; }
     if (a.lean == LEAN_M1_GP) { lean_points<1, E, 1, 1, 1>(x, a, p0, T, pn, px); return true; }
@@ -891,7 +928,7 @@ __device__ __forceinline__ void half_points(typename CT<Real>::T (&x)[M][E], con
   using C = typename CT<Real>::T;
   C pn[M], px[M];
   load_pump<Real, M>(a, h, pn, px, true);
-  if constexpr (std::is_same<Real, double>::value) {
+  if constexpr (std::is_same<Real, double>::value || std::is_same<Real, float>::value) {
     if (a.lean != LEAN_OFF && lean_dispatch<M, E>(x, a, p0, T, pn, px)) return;
   }
 // FP32 points per trip of the half-step loop: 2 measured fastest on the 512^2 polariton
