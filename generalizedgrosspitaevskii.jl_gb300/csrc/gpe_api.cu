@@ -900,12 +900,11 @@ static int pass_variant(const gpe_handle* h) {
   return h->M == 2 && h->P * h->B <= kFinePoints ? 2 : 0;
 }
 
-// The compile-time specialised half step (FP64 and FP32 passes) that covers this handle's families, or
+// The compile-time specialised half step (every pass precision) that covers this handle's families, or
 // LEAN_OFF: no potential, no noise, no matrix nonlinearity, a real nonlinearity, real and
 // non-uniform pump profiles, and one of the component patterns of gpe::LeanKind.
 static int lean_kind(const gpe_handle* h, const PassArgs& a) {
-  if (h->prec == gpe::PREC_DW || h->vkind != GPE_TABLE_NONE || h->noise != GPE_NOISE_OFF || h->nl_matrix ||
-      h->pprof_cplx)
+  if (h->vkind != GPE_TABLE_NONE || h->noise != GPE_NOISE_OFF || h->nl_matrix || h->pprof_cplx)
     return gpe::LEAN_OFF;
   int gm = 0, pm = 0;
   for (int j = 0; j < h->M; ++j) {

@@ -9,7 +9,7 @@ struct DWR;  // double-word precision tag (defined in fft.cuh)
 
 enum TableKind { TAB_NONE = 0, TAB_SCALAR = 1, TAB_DIAG = 2, TAB_MATRIX = 3 };
 enum NoiseMode { NOISE_OFF = 0, NOISE_PHILOX = 1, NOISE_REPLAY = 2 };
-// Half-step families with a compile-time specialisation (FP64 and FP32; no potential, no noise,
+// Half-step families with a compile-time specialisation (every precision; no potential, no noise,
 // real nonlinearity, real non-uniform pump profiles): G = components whose nonlinearity is
 // on, D = the densities it reads, P = pumped components.
 enum LeanKind {
@@ -100,8 +100,8 @@ struct PassArgs {
   // FP64 line transforms of the row and column passes in block floating point on the
   // integer pipes (Q62 twiddles after the FP64 ones in the table)
   int32_t fx;
-  // FP64 and FP32 half steps of the common families specialised at compile time
-  // (LeanKind; 0 = the generic half step)
+  // half steps of the common families specialised at compile time (LeanKind; 0 = the
+  // generic half step)
   int32_t lean;
   // host-mapped status word: a device wait that ran out of time stores 1 here
   int32_t* status;

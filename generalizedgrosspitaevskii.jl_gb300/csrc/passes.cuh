@@ -841,12 +841,53 @@ __device__ __forceinline__ void half_step_lean(double2 (&u)[M], const PassArgs& 
   }
 }
 
+// Double-word form of half_step_lean, operation for operation the generic double-word half
+// step (the same coefficient sums, dw_sincos, products and sums).
+template <int M, int GM, int DM, int PM>
+__device__ __forceinline__ void half_step_lean(dwc (&u)[M], const PassArgs& a, int64_t p,
+                                               const dwc (&pn)[M], const dwc (&px)[M]) {
+  dw dens[M], prof[M];
+#pragma unroll
+  for (int l = 0; l < M; ++l)
+    dens[l] = ((DM >> l) & 1) ? dot2<+1>(re(u[l]), re(u[l]), im(u[l]), im(u[l])) : dw{0.0f, 0.0f};
+#pragma unroll
+  for (int j = 0; j < M; ++j) {
+    if ((PM >> j) & 1) {
+      const float2 v = __ldg((const float2*)a.pprof[j] + p);
+      prof[j] = dw{v.x, v.y};
+      if ((GM >> j) & 1) u[j] = cadd(u[j], cscale(pn[j], prof[j]));
+    }
+  }
+  const dw dth = {a.dthf, a.dthl};
+#pragma unroll
+  for (int j = 0; j < M; ++j) {
+    if ((GM >> j) & 1) {
+      dw gr = {a.cf[j][0], a.cl[j][0]};
+      bool empty = a.cf[j][0] == 0.0f && a.cl[j][0] == 0.0f;
+#pragma unroll
+      for (int l = 0; l < M; ++l)
+        if (((DM >> l) & 1) && (a.gf[j][l][0] != 0.0f || a.gl[j][l][0] != 0.0f)) {
+          const dw term = dw_mul({a.gf[j][l][0], a.gl[j][l][0]}, dens[l]);
+          gr = empty ? term : dw_add_acc(gr, term);
+          empty = false;
+        }
+      dw s, c;
+      dw_sincos(dw_mul(dth, gr), s, c);
+      u[j] = cmul(mk(c, dw_neg(s)), u[j]);
+    }
+  }
+#pragma unroll
+  for (int j = 0; j < M; ++j)
+    if ((PM >> j) & 1) u[j] = cadd(u[j], cscale(px[j], prof[j]));
+}
+
 template <int M, int E, int GM, int DM, int PM, typename C>
 __device__ __forceinline__ void lean_points(C (&x)[M][E], const PassArgs& a, int64_t p0, int T,
                                             const C (&pn)[M], const C (&px)[M]) {
-  // U points a trip, their FP64 chains independent (the phase routine's general branch is
-  // long, so the loop is not unrolled further); the arrays rotate by U
-  constexpr int U = E % 2 == 0 ? 2 : 1;
+  // U points a trip, their chains independent (the phase routine's general branch is long,
+  // so the loop is not unrolled further; double-word half steps, several hundred
+  // instructions, one a trip); the arrays rotate by U
+  constexpr int U = E % 2 == 0 && !std::is_same<C, dwc>::value ? 2 : 1;
 #pragma unroll 1
   for (int i = 0; i < E; i += U) {
     C v[U][M];
@@ -928,9 +969,7 @@ __device__ __forceinline__ void half_points(typename CT<Real>::T (&x)[M][E], con
   using C = typename CT<Real>::T;
   C pn[M], px[M];
   load_pump<Real, M>(a, h, pn, px, true);
-  if constexpr (std::is_same<Real, double>::value || std::is_same<Real, float>::value) {
-    if (a.lean != LEAN_OFF && lean_dispatch<M, E>(x, a, p0, T, pn, px)) return;
-  }
+  if (a.lean != LEAN_OFF && lean_dispatch<M, E>(x, a, p0, T, pn, px)) return;
 // FP32 points per trip of the half-step loop: 2 measured fastest on the 512^2 polariton
 // row pass (0.61 ms against 0.68 ms with all 8 unrolled, whose code spills out of the
 // instruction cache, and 0.64 ms with 1)
