@@ -747,10 +747,12 @@ def run_twa(pkg, steps: int, tune: bool):
         resident, variant = True, 0
         if tune:
             k = A.key(N, 1, "c64", B, A.gpu_name())
-            resident, variant, chunk_n, _ = A.tune(
+            resident, variant, chunk_n, timings = A.tune(
                 lambda r, v, N=N, B=B: T.make_group(N, B, prm, 400, seed=N, resident=r, variant=v), k,
                 trial_steps=200, variants=(0, 1), resident_ok=A.resident_fits(N, 1, 8))
-            choices[f"{N}x{N}"] = {"resident": resident, "variant": variant, "steps_per_graph": chunk_n}
+            # each candidate timed alone (the group by itself in a graph, 200 steps)
+            choices[f"{N}x{N}"] = {"resident": resident, "variant": variant, "steps_per_graph": chunk_n,
+                                   "ms_per_step_alone": {c: ms / 200 for c, ms in timings.items()}}
             tuned_chunks.append(chunk_n)
         its.append(T.make_group(N, B, prm, steps + 400, seed=N, resident=resident, variant=variant))
     if tuned_chunks and steps % min(tuned_chunks) == 0:
